@@ -1,0 +1,242 @@
+/*
+ * restir_gb300.h -- C ABI of the GB300-native ReSTIR direct-lighting path.
+ *
+ * Drop-in for the compute half of ReSTIR-Vulkan's per-frame pass sequence
+ * (reference paths relative to the reference project root):
+ *
+ *   reference pass (Pass::issueCommands, src/passes/pass.h:103)     entry point here
+ *   ------------------------------------------------------------    -------------------------
+ *   RestirPass          src/passes/restirPass.h:36-62               rg_initial_temporal
+ *     -> src/shaders/restirOmni.glsl:86-212 (software RT variant)
+ *   SpatialReusePass    src/passes/spatialReusePass.h:11-26         rg_spatial_biased
+ *     -> src/shaders/spatialReuse.comp:30-86
+ *   UnbiasedReusePass   src/passes/unbiasedReusePass.h:23-49        rg_spatial_unbiased
+ *     -> src/shaders/unbiasedReuse.glsl:50-185
+ *   LightingPass        src/passes/lightingPass.h:14-42             rg_shade
+ *     -> src/shaders/lighting.frag:43-71,103 (GBUFFER_DEBUG_NONE)
+ *   testVisibility      src/shaders/include/visibilityTest.glsl:26  rg_visibility_batch
+ *   App::_recordMainCommandBuffers  src/app.h:212-262 (+ buffer     rg_render_frame
+ *     wiring src/app.h:264-336, per-frame uniforms src/app.cpp:775-826)
+ *   host preprocessing:
+ *   AabbTree::build     src/aabbTreeBuilder.cpp:52-214              rg_build_bvh
+ *   createAliasTable    src/misc.cpp:418-497                        rg_build_alias_table
+ *   SceneBuffers / AabbTreeBuffers upload (sceneBuffers.h:71-273,   rg_upload_scene
+ *     aabbTreeBuilder.h:25-51)
+ *
+ * Conventions
+ *  - Every call returns RG_OK (0) or a negative RG_ERR_* code; nothing throws
+ *    across the ABI and nothing aborts.  rg_last_error() gives the message of
+ *    the last failure on the calling thread.
+ *  - Pass entry points take DEVICE pointers owned by the caller and launch on
+ *    the given CUDA stream (a cudaStream_t passed as void*; NULL = legacy
+ *    default stream).  They return once the work is enqueued and allocate
+ *    nothing.  Uniform structs are read on the host at call time.
+ *  - Byte layouts of rg_reservoir, rg_aabb_tree_node, rg_triangle,
+ *    rg_point_light, rg_tri_light, rg_alias_table_column, rg_restir_uniforms
+ *    and rg_lighting_uniforms are the reference's std430/std140 layouts
+ *    (src/shaderIncludes.h; src/shaders/include/structs/).
+ *  - G-buffer planes are the reference's attachment formats
+ *    (src/passes/gBufferPass.cpp:75-108) stored as linear row-major buffers.
+ *  - A context is thread-compatible: one host thread at a time.
+ */
+#ifndef RESTIR_GB300_H
+#define RESTIR_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RG_OK 0
+#define RG_ERR_INVALID_ARGUMENT (-1)
+#define RG_ERR_CUDA (-2)
+#define RG_ERR_OUT_OF_MEMORY (-3)
+#define RG_ERR_NO_SCENE (-4)
+#define RG_ERR_TREE_TOO_DEEP (-5)
+#define RG_ERR_UNSUPPORTED (-6)
+#define RG_ERR_TRAVERSAL (-7)
+
+#define RG_FLAG_VISIBILITY_REUSE 1 /* RESTIR_VISIBILITY_REUSE_FLAG, restirStructs.glsl:37 */
+#define RG_FLAG_TEMPORAL_REUSE 2   /* RESTIR_TEMPORAL_REUSE_FLAG, restirStructs.glsl:38 */
+
+/* Deepest BVH the traversal accepts: its stack holds depth+1 entries. */
+#define RG_MAX_TREE_DEPTH 63
+
+typedef struct rg_context rg_context;
+
+/* Reservoir with RESERVOIR_SIZE 1 (restirStructs.glsl:19-34): 64 bytes. */
+typedef struct rg_reservoir {
+    float position_emission_lum[4]; /* sample position, w = emission luminance */
+    float normal[4];                /* light normal; w > 0.5 => triangle light */
+    int32_t light_index;            /* >= 0 point light, < 0: triangle light -1-i */
+    float p_hat;
+    float sum_weights;
+    float w;
+    uint32_t num_stream_samples;    /* M */
+    uint32_t _pad[3];
+} rg_reservoir;
+
+/* AabbTreeNode (structs/aabbTree.glsl:1-8): 80 bytes.  A child < 0 is the
+ * triangle ~child; the root is node 0. */
+typedef struct rg_aabb_tree_node {
+    float left_aabb_min[4], left_aabb_max[4];
+    float right_aabb_min[4], right_aabb_max[4];
+    int32_t left_child, right_child;
+    int32_t _pad[2];
+} rg_aabb_tree_node;
+
+typedef struct rg_triangle { float p1[4], p2[4], p3[4]; } rg_triangle;                 /* 48 B */
+typedef struct rg_point_light { float pos[4]; float color_luminance[4]; } rg_point_light; /* 32 B */
+typedef struct rg_tri_light {                                                           /* 80 B */
+    float p1[4], p2[4], p3[4];
+    float emission_luminance[4];
+    float normal_area[4];
+} rg_tri_light;
+typedef struct rg_alias_table_column { float prob; int32_t alias; float ori_prob; float alias_ori_prob; } rg_alias_table_column; /* 16 B */
+
+/* RestirUniforms (restirStructs.glsl:40-56), std140: 128 bytes. */
+typedef struct rg_restir_uniforms {
+    float prev_frame_projection_view[16]; /* column-major */
+    float camera_pos[4];
+    uint32_t screen_size[2];
+    uint32_t frame;
+    uint32_t initial_light_sample_count;
+    uint32_t temporal_sample_count_multiplier;
+    float spatial_pos_threshold;
+    float spatial_normal_threshold;       /* degrees */
+    uint32_t spatial_neighbors;
+    float spatial_radius;
+    int32_t flags;
+    uint32_t _pad[2];
+} rg_restir_uniforms;
+
+/* LightingPassUniforms (structs/lightingPassStructs.glsl:1-7): 96 bytes. */
+typedef struct rg_lighting_uniforms {
+    float prev_frame_projection_view[16];
+    float camera_pos[4];
+    uint32_t buffer_size[2];
+    int32_t debug_mode;                   /* only GBUFFER_DEBUG_NONE (0) is computed */
+    float gamma;
+} rg_lighting_uniforms;
+
+/* G-buffer planes (device pointers), width*height texels each, row-major. */
+typedef struct rg_gbuffer {
+    int32_t width, height;
+    const void *albedo;     /* R8G8B8A8_SRGB: sRGB-encoded rgb, alpha 255 = emissive */
+    const void *normal;     /* R16G16B16A16_SFLOAT */
+    const void *material;   /* R16G16_UNORM: roughness, metallic */
+    const void *world_pos;  /* R32G32B32A32_SFLOAT */
+    const void *depth;      /* D32_SFLOAT: projected z/w */
+} rg_gbuffer;
+
+/* Writable G-buffer planes, for rg_trace_gbuffer. */
+typedef struct rg_gbuffer_out {
+    int32_t width, height;
+    void *albedo, *normal, *material, *world_pos, *depth;
+} rg_gbuffer_out;
+
+/* Per-triangle surface, indexed like the triangle buffer. */
+typedef struct rg_material {
+    uint8_t albedo_srgb[4];   /* rgb sRGB-encoded; a = 255 for emissive surfaces */
+    uint16_t roughness_unorm; /* 0..65535 */
+    uint16_t metallic_unorm;
+} rg_material;
+
+/* Pinhole camera in the reference's convention (src/camera.h:25-50). */
+typedef struct rg_camera {
+    float position[3];
+    float right[3];           /* unitRight */
+    float up[3];              /* unitUp (view y is -up) */
+    float forward[3];         /* unitForward */
+    float tan_half_fov_y;     /* 1/f */
+    float aspect;             /* width / height */
+    float projection_view[16];/* column-major P*V of this camera (depth output) */
+} rg_camera;
+
+/* Host-side scene as the reference uploads it. */
+typedef struct rg_scene_desc {
+    const rg_aabb_tree_node *nodes; int32_t n_nodes;
+    const rg_triangle *triangles; int32_t n_triangles;
+    const rg_point_light *point_lights; int32_t n_point_lights;
+    const rg_tri_light *tri_lights; int32_t n_tri_lights;
+    const rg_alias_table_column *alias_table; int32_t n_alias; /* one column per light */
+    const rg_material *materials; int32_t n_materials;        /* optional: per triangle, for rg_trace_gbuffer */
+} rg_scene_desc;
+
+/* Frame parameters for the driver (App state, src/app.h:150-174). */
+typedef struct rg_frame_params {
+    rg_restir_uniforms uniforms;     /* frame, flags, counts, thresholds, camera */
+    int32_t unbiased;                /* 1: UnbiasedReusePass, 0: SpatialReusePass pairs */
+    int32_t spatial_iterations;      /* biased: iterations (2 dispatches each); unbiased: passes */
+    int32_t unbiased_neighbors;      /* NUM_NEIGHBORS (reference: 3) */
+    float gamma;
+} rg_frame_params;
+
+typedef struct rg_stats {
+    uint64_t rays_traced;            /* shadow segments traced since the last reset */
+    uint64_t traversal_errors;       /* traversals that hit the iteration limit */
+} rg_stats;
+
+/* ---- context ---- */
+int rg_create(int32_t device, rg_context **out);
+int rg_destroy(rg_context *ctx);
+const char *rg_last_error(void);
+int rg_get_stats(rg_context *ctx, rg_stats *out, int32_t reset);
+
+/* ---- host preprocessing (no GPU needed) ---- */
+/* AabbTree::build on a flat list of n_tris triangles (9 floats each).  Writes
+ * n_tris-1 nodes and n_tris triangles; returns the node count or an error. */
+int rg_build_bvh(const float *tri_xyz, int32_t n_tris, rg_aabb_tree_node *out_nodes, rg_triangle *out_tris);
+/* Depth of the tree (root = 1). */
+int rg_tree_depth(const rg_aabb_tree_node *nodes, int32_t n_nodes);
+/* createAliasTable: point lights if n_point > 0, else triangle lights. */
+int rg_build_alias_table(const rg_point_light *point_lights, int32_t n_point, const rg_tri_light *tri_lights,
+                         int32_t n_tri, rg_alias_table_column *out);
+/* CPU primary-ray G-buffer (host planes, same formats as rg_gbuffer). */
+int rg_trace_gbuffer_host(const rg_scene_desc *scene, const rg_camera *cam, int32_t width, int32_t height,
+                          uint8_t *albedo, uint16_t *normal, uint16_t *material, float *world_pos, float *depth);
+
+/* ---- scene upload (host pointers; copied to device, synchronous) ---- */
+int rg_upload_scene(rg_context *ctx, const rg_scene_desc *scene);
+
+/* ---- passes (device pointers, stream-ordered) ---- */
+int rg_initial_temporal(rg_context *ctx, const rg_gbuffer *cur, const rg_gbuffer *prev,
+                        const rg_reservoir *prev_reservoirs, rg_reservoir *out,
+                        const rg_restir_uniforms *uniforms, void *stream);
+int rg_spatial_biased(rg_context *ctx, const rg_gbuffer *gbuf, const rg_reservoir *in, rg_reservoir *out,
+                      const rg_restir_uniforms *uniforms, int32_t iter, void *stream);
+/* num_neighbors is NUM_NEIGHBORS (reference: 3, unbiasedReuse.glsl:48).  The
+ * reference seeds the pass with frame*17 (:72); pass_index p seeds it with
+ * frame*17 + p so that chained passes draw fresh neighbours (0 = reference). */
+int rg_spatial_unbiased(rg_context *ctx, const rg_gbuffer *gbuf, const rg_reservoir *in, rg_reservoir *out,
+                        const rg_restir_uniforms *uniforms, int32_t num_neighbors, int32_t pass_index,
+                        void *stream);
+int rg_shade(rg_context *ctx, const rg_gbuffer *gbuf, const rg_reservoir *reservoirs,
+             const rg_lighting_uniforms *uniforms, float *rgba_out, void *stream);
+/* p1, p2: n float4 (xyz used).  shadowed[i] = testVisibility(p1[i], p2[i]). */
+int rg_visibility_batch(rg_context *ctx, const float *p1, const float *p2, uint8_t *shadowed, int32_t n,
+                        void *stream);
+/* GPU primary-ray G-buffer on the uploaded scene (needs materials). */
+int rg_trace_gbuffer(rg_context *ctx, const rg_camera *cam, const rg_gbuffer_out *out, void *stream);
+
+/* ---- frame driver: the reference's pass order and reservoir ping-pong ----
+ * Owns two frame reservoir buffers and one temporary buffer sized for
+ * width*height (allocated on first use or size change, zero-filled, as
+ * src/app.h:264-290).  frame_slot selects the current buffer (0/1), the other
+ * one is the previous frame's.  Writes the shaded image (float4 rgba). */
+int rg_render_frame(rg_context *ctx, const rg_gbuffer *cur, const rg_gbuffer *prev, int32_t frame_slot,
+                    const rg_frame_params *params, float *rgba_out, void *stream);
+/* Reservoirs of the last rendered frame in slot frame_slot (device pointer). */
+int rg_frame_reservoirs(rg_context *ctx, int32_t frame_slot, const rg_reservoir **out);
+/* Same as rg_render_frame with HOST planes: copies the current G-buffer in
+ * (the previous frame's G-buffer is kept on the device from the last call),
+ * renders, and copies the image back; returns after the copy completes. */
+int rg_render_frame_host(rg_context *ctx, int32_t width, int32_t height, const uint8_t *albedo,
+                         const uint16_t *normal, const uint16_t *material, const float *world_pos,
+                         const float *depth, const rg_frame_params *params, float *rgba_out_host, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,931 @@
+/*
+ * oracle.c -- CPU oracle for the ReSTIR direct-lighting hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the parity checker.  Only tests/, the smoke()
+ * entry and bench.py's CPU-baseline leg load this library; the product path
+ * never does.
+ *
+ * Single precision throughout (except the FP64 judge at the end), compiled
+ * with -ffp-contract=off so every a*b+c is two rounded operations, exactly as
+ * the CUDA kernels (built with -fmad=false) compute it.  GLSL built-ins are
+ * given one fixed meaning shared with the CUDA path:
+ *   min(x,y) = y<x ? y : x          max(x,y) = x<y ? y : x   (GLSL 4.50 8.3)
+ *   clamp(x,a,b) = min(max(x,a),b)  mix(x,y,a) = x*(1-a) + y*a
+ *   dot(a,b) = (a.x*b.x + a.y*b.y) + a.z*b.z
+ *   normalize(v) = v / sqrt(dot(v,v)) (component-wise IEEE division)
+ *   pow(r, 2.0) = r*r               round() = half away from zero
+ *   sin/cos: Cody-Waite reduction by pi/2 + Taylor polynomials (or_sinf/or_cosf)
+ *   M*v = ((m0*x + m1*y) + m2*z) + m3*w   (column-major)
+ * Reference paths below are relative to the reference project root.
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define PI_F 3.14159274101257324f          /* (float)M_PI, disneyBRDF.glsl:1 as a GLSL float literal */
+#define DEG2RAD_F 0.0174532923847436905f    /* (float)(pi/180): GLSL radians() */
+#define PI_D 3.14159265358979323846
+#define STACK_SIZE 64                        /* reference: 32 (softwareRaytracing.glsl:40), UB on overflow */
+
+/* ------------------------------------------------------------------ vec3 */
+typedef struct { float x, y, z; } v3;
+static inline v3 V(float x, float y, float z) { v3 r; r.x = x; r.y = y; r.z = z; return r; }
+static inline v3 vadd(v3 a, v3 b) { return V(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline v3 vsub(v3 a, v3 b) { return V(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline v3 vmuls(float s, v3 a) { return V(s * a.x, s * a.y, s * a.z); }
+static inline v3 vmul(v3 a, v3 b) { return V(a.x * b.x, a.y * b.y, a.z * b.z); }
+static inline v3 vdivs(v3 a, float s) { return V(a.x / s, a.y / s, a.z / s); }
+static inline v3 vdiv(v3 a, v3 b) { return V(a.x / b.x, a.y / b.y, a.z / b.z); }
+static inline float vdot(v3 a, v3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+static inline v3 vcross(v3 a, v3 b) {
+    return V(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+static inline v3 vnormalize(v3 a) { return vdivs(a, sqrtf(vdot(a, a))); }
+static inline float gmin(float x, float y) { return y < x ? y : x; }
+static inline float gmax(float x, float y) { return x < y ? y : x; }
+static inline float gclamp(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
+static inline float gmix(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+static inline v3 f4xyz(or_f4 f) { return V(f.x, f.y, f.z); }
+static inline int imin(int a, int b) { return b < a ? b : a; }
+static inline int imax(int a, int b) { return a < b ? b : a; }
+static inline int iclamp(int x, int lo, int hi) { return imin(imax(x, lo), hi); }
+
+/* ------------------------------------------------------------------ PCG32 (rand.glsl:7-32) */
+typedef struct { uint64_t state, inc; } pcg_t;
+static inline uint32_t pcg_next(pcg_t *r) {
+    uint64_t old = r->state;
+    r->state = old * 6364136223846793005ULL + r->inc;
+    uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+    uint32_t rot = (uint32_t)(old >> 59u);
+    return (xs >> rot) | (xs << ((0u - rot) & 31u));
+}
+static inline pcg_t pcg_seed(uint64_t seed, uint64_t seq) {
+    pcg_t r;
+    r.state = 0;
+    r.inc = (seq << 1u) | 1u;
+    pcg_next(&r);
+    r.state += seed;
+    pcg_next(&r);
+    return r;
+}
+/* rand.glsl:30-32: uint -> float (round to nearest) / 2^32; may return exactly 1.0 */
+static inline float rand_float(pcg_t *r) { return (float)pcg_next(r) / 4294967296.0f; }
+
+void or_pcg_stream(uint64_t seed, uint64_t seq, int32_t n, uint32_t *out) {
+    pcg_t r = pcg_seed(seed, seq);
+    for (int32_t i = 0; i < n; ++i) out[i] = pcg_next(&r);
+}
+void or_rand_floats(uint64_t seed, uint64_t seq, int32_t n, float *out) {
+    pcg_t r = pcg_seed(seed, seq);
+    for (int32_t i = 0; i < n; ++i) out[i] = rand_float(&r);
+}
+
+/* ------------------------------------------------------------------ sin / cos
+ * Cody-Waite reduction x = k*pi/2 + y with pi/2 = C1 + C2 + C3 (C1 8 bits,
+ * C2 12 bits, so k*C1 and k*C2 are exact for |k| < 2^12), then Taylor
+ * polynomials of sin (to y^9) and cos (to y^10) on |y| <= pi/4, Horner form.
+ * Same constants and operation order as the CUDA kernels. */
+#define CW_2_OVER_PI 0.636619746685028076f
+#define CW_C1 1.5703125f
+#define CW_C2 4.83870506286621094e-4f
+#define CW_C3 -4.37113882867379300e-8f
+#define TS3 0.166666671633720398f
+#define TS5 8.33333376795053482e-3f
+#define TS7 1.98412701138295233e-4f
+#define TS9 2.75573188446287531e-6f
+#define TC4 4.16666679084300995e-2f
+#define TC6 1.38888892251998186e-3f
+#define TC8 2.48015876422869042e-5f
+#define TC10 2.75573199814971304e-7f
+
+static inline void or_sincos(float x, float *s, float *c) {
+    float k = rintf(x * CW_2_OVER_PI);
+    float y = ((x - k * CW_C1) - k * CW_C2) - k * CW_C3;
+    float y2 = y * y;
+    float ps = ((TS9 * y2 - TS7) * y2 + TS5) * y2 - TS3;
+    float sy = y + (y * y2) * ps;
+    float pc = ((TC8 - TC10 * y2) * y2 - TC6) * y2 + TC4;
+    float cy = (1.0f - 0.5f * y2) + (y2 * y2) * pc;
+    int q = ((int)k) & 3;
+    switch (q) {
+    case 0: *s = sy; *c = cy; break;
+    case 1: *s = cy; *c = -sy; break;
+    case 2: *s = -sy; *c = -cy; break;
+    default: *s = -cy; *c = sy; break;
+    }
+}
+static inline float or_cosf(float x) { float s, c; or_sincos(x, &s, &c); return c; }
+
+void or_sincos_batch(int32_t n, const float *x, float *s, float *c) {
+    for (int32_t i = 0; i < n; ++i) or_sincos(x[i], &s[i], &c[i]);
+}
+
+/* ------------------------------------------------------------------ G-buffer decoding
+ * albedo is R8G8B8A8_SRGB (gBufferPass.cpp:75-79): sampling decodes the sRGB
+ * transfer function; the table is evaluated in double and rounded once. */
+static float g_srgb[256];
+static int g_srgb_ready = 0;
+static void srgb_init(void) {
+    if (g_srgb_ready) return;
+    for (int i = 0; i < 256; ++i) {
+        double c = (double)i / 255.0;
+        double l = c <= 0.04045 ? c / 12.92 : pow((c + 0.055) / 1.055, 2.4);
+        g_srgb[i] = (float)l;
+    }
+    g_srgb_ready = 1;
+}
+void or_srgb_lut(float *out256) { srgb_init(); memcpy(out256, g_srgb, sizeof(g_srgb)); }
+
+float or_half_to_float(uint16_t h) {
+    uint32_t sign = (uint32_t)(h & 0x8000u) << 16;
+    uint32_t exp = (h >> 10) & 0x1fu;
+    uint32_t man = h & 0x3ffu;
+    uint32_t bits;
+    if (exp == 0) {
+        if (man == 0) {
+            bits = sign;
+        } else {           /* subnormal half -> normal float */
+            int e = -1;
+            do { ++e; man <<= 1; } while (!(man & 0x400u));
+            bits = sign | ((uint32_t)(127 - 15 - e) << 23) | ((man & 0x3ffu) << 13);
+        }
+    } else if (exp == 31) {
+        bits = sign | 0x7f800000u | (man << 13);
+    } else {
+        bits = sign | ((exp + 112u) << 23) | (man << 13);
+    }
+    float f;
+    memcpy(&f, &bits, 4);
+    return f;
+}
+
+typedef struct {
+    v3 albedo; float albedo_a;
+    v3 normal;
+    float roughness, metallic;
+    v3 wpos;
+    float depth;
+} texel_t;
+
+static inline void fetch_texel(const or_gbuffer *g, int x, int y, texel_t *t) {
+    size_t i = (size_t)y * (size_t)g->width + (size_t)x;
+    const uint8_t *a = g->albedo + 4 * i;
+    t->albedo = V(g_srgb[a[0]], g_srgb[a[1]], g_srgb[a[2]]);
+    t->albedo_a = (float)a[3] / 255.0f;
+    const uint16_t *n = g->normal + 4 * i;
+    t->normal = V(or_half_to_float(n[0]), or_half_to_float(n[1]), or_half_to_float(n[2]));
+    const uint16_t *m = g->material + 2 * i;
+    t->roughness = (float)m[0] / 65535.0f;
+    t->metallic = (float)m[1] / 65535.0f;
+    const float *p = g->world_pos + 4 * i;
+    t->wpos = V(p[0], p[1], p[2]);
+    t->depth = g->depth[i];
+}
+
+/* ------------------------------------------------------------------ BRDF (disneyBRDF.glsl:5-90) */
+static inline float luminance(float r, float g, float b) { /* common.glsl:7-9 */
+    return 0.2126f * r + 0.7152f * g + 0.0722f * b;
+}
+static inline float schlick_fresnel(float c) { /* :5-10 */
+    float m = gclamp(1.0f - c, 0.0f, 1.0f);
+    float sm = m * m;
+    return sm * sm * m;
+}
+static inline float gtr2(float ndoth, float a) { /* :13-18 */
+    float a2 = a * a;
+    float t = 1.0f + (a2 - 1.0f) * ndoth * ndoth;
+    return a2 / (PI_F * t * t);
+}
+static inline float smith_g_ggx(float ndotv, float alpha_g) { /* :20-25 */
+    float a = alpha_g * alpha_g;
+    float b = ndotv * ndotv;
+    return 1.0f / (fabsf(ndotv) + gmax(sqrtf(a + b - a * b), 0.0001f));
+}
+static inline float diffuse_factor(float cos_in, float cos_out, float cos_in_half, float roughness, float metallic) { /* :27-33 */
+    float f_in = schlick_fresnel(cos_in);
+    float f_out = schlick_fresnel(cos_out);
+    float fd90 = 0.5f + 2.0f * cos_in_half * cos_in_half * roughness;
+    float fd = gmix(1.0f, fd90, f_in) * gmix(1.0f, fd90, f_out);
+    return fd * (1.0f - metallic) / PI_F;
+}
+static inline void specular_factors(float cos_in, float cos_out, float cos_half, float cos_in_half,
+                                    float roughness, float *fresnel, float *gd) { /* :42-55 */
+    *fresnel = schlick_fresnel(cos_in_half);
+    float a = gmax(0.001f, roughness * roughness);
+    float ds = gtr2(cos_half, a);
+    float gs = smith_g_ggx(cos_in, a);
+    gs *= smith_g_ggx(cos_out, a);
+    *gd = gs * ds;
+}
+static inline float brdf_lum(float cos_in, float cos_out, float cos_half, float cos_in_half,
+                             float lum, float roughness, float metallic) { /* :82-90 */
+    if (cos_in < 0.0f) return 0.0f;
+    float diffuse = lum * diffuse_factor(cos_in, cos_out, cos_in_half, roughness, metallic);
+    float fr, gd;
+    specular_factors(cos_in, cos_out, cos_half, cos_in_half, roughness, &fr, &gd);
+    float spec_lum = gmix(0.04f, lum, metallic);
+    float fs = gmix(spec_lum, 1.0f, fr);
+    return diffuse + fs * gd;
+}
+static inline v3 brdf_color(float cos_in, float cos_out, float cos_half, float cos_in_half,
+                            v3 albedo, float roughness, float metallic) { /* :73-81 */
+    if (cos_in < 0.0f) return V(0.0f, 0.0f, 0.0f);
+    float df = diffuse_factor(cos_in, cos_out, cos_in_half, roughness, metallic);
+    v3 diffuse = V(albedo.x * df, albedo.y * df, albedo.z * df);
+    float fr, gd;
+    specular_factors(cos_in, cos_out, cos_half, cos_in_half, roughness, &fr, &gd);
+    v3 sc = V(gmix(0.04f, albedo.x, metallic), gmix(0.04f, albedo.y, metallic), gmix(0.04f, albedo.z, metallic));
+    v3 fs = V(gmix(sc.x, 1.0f, fr), gmix(sc.y, 1.0f, fr), gmix(sc.z, 1.0f, fr));
+    return vadd(diffuse, V(fs.x * gd, fs.y * gd, fs.z * gd));
+}
+
+/* ------------------------------------------------------------------ p-hat (restirUtils.glsl:3-55) */
+static float eval_phat(v3 wpos, v3 lpos, v3 cam, v3 n, v3 ln, int use_ln,
+                       float albedo_lum, float emission_lum, float roughness, float metallic) {
+    v3 wi = vsub(lpos, wpos);
+    if (vdot(wi, n) < 0.0f) return 0.0f;
+    float sqr_dist = vdot(wi, wi);
+    wi = vdivs(wi, sqrtf(sqr_dist));
+    v3 wo = vnormalize(vsub(cam, wpos));
+    float cos_in = vdot(n, wi);
+    float cos_out = vdot(n, wo);
+    v3 h = vnormalize(vadd(wi, wo));
+    float cos_half = vdot(n, h);
+    float cos_in_half = vdot(wi, h);
+    float geometry = cos_in / sqr_dist;
+    if (use_ln) geometry *= fabsf(vdot(wi, ln));
+    return emission_lum * brdf_lum(cos_in, cos_out, cos_half, cos_in_half, albedo_lum, roughness, metallic) * geometry;
+}
+static v3 eval_phat_full(v3 wpos, v3 lpos, v3 cam, v3 n, v3 ln, int use_ln,
+                         v3 albedo, v3 emission, float roughness, float metallic) {
+    v3 wi = vsub(lpos, wpos);
+    if (vdot(wi, n) < 0.0f) return V(0.0f, 0.0f, 0.0f);
+    float sqr_dist = vdot(wi, wi);
+    wi = vdivs(wi, sqrtf(sqr_dist));
+    v3 wo = vnormalize(vsub(cam, wpos));
+    float cos_in = vdot(n, wi);
+    float cos_out = vdot(n, wo);
+    v3 h = vnormalize(vadd(wi, wo));
+    float cos_half = vdot(n, h);
+    float cos_in_half = vdot(wi, h);
+    float geometry = cos_in / sqr_dist;
+    if (use_ln) geometry *= fabsf(vdot(wi, ln));
+    v3 f = brdf_color(cos_in, cos_out, cos_half, cos_in_half, albedo, roughness, metallic);
+    v3 e = vmul(emission, f);
+    return V(e.x * geometry, e.y * geometry, e.z * geometry);
+}
+
+void or_eval_phat_batch(int32_t n, const float *a, float *out) {
+    for (int32_t i = 0; i < n; ++i, a += 20)
+        out[i] = eval_phat(V(a[0], a[1], a[2]), V(a[3], a[4], a[5]), V(a[6], a[7], a[8]), V(a[9], a[10], a[11]),
+                           V(a[12], a[13], a[14]), a[15] > 0.5f, a[16], a[17], a[18], a[19]);
+}
+void or_eval_phat_full_batch(int32_t n, const float *a, float *out) {
+    for (int32_t i = 0; i < n; ++i, a += 24) {
+        v3 r = eval_phat_full(V(a[0], a[1], a[2]), V(a[3], a[4], a[5]), V(a[6], a[7], a[8]), V(a[9], a[10], a[11]),
+                              V(a[12], a[13], a[14]), a[15] > 0.5f, V(a[16], a[17], a[18]), V(a[19], a[20], a[21]),
+                              a[22], a[23]);
+        out[3 * i] = r.x; out[3 * i + 1] = r.y; out[3 * i + 2] = r.z;
+    }
+}
+
+/* ------------------------------------------------------------------ traversal (softwareRaytracing.glsl) */
+static inline float max3(v3 v) { return gmax(v.x, gmax(v.y, v.z)); }
+static inline float min3(v3 v) { return gmin(v.x, gmin(v.y, v.z)); }
+static inline int ray_aabb(v3 o, v3 d, v3 bmin, v3 bmax) { /* :9-14 */
+    v3 t0 = vdiv(vsub(bmin, o), d);
+    v3 t1 = vdiv(vsub(bmax, o), d);
+    float rmin = max3(V(gmin(t0.x, t1.x), gmin(t0.y, t1.y), gmin(t0.z, t1.z)));
+    float rmax = min3(V(gmax(t0.x, t1.x), gmax(t0.y, t1.y), gmax(t0.z, t1.z)));
+    return rmin < 1.0f && rmax >= rmin && rmax > 0.0f;
+}
+static inline int ray_tri(v3 p1, v3 p2, v3 p3, v3 o, v3 d) { /* :15-37 */
+    v3 e1 = vsub(p2, p1);
+    v3 e2 = vsub(p3, p1);
+    v3 p = vcross(d, e2);
+    float f = 1.0f / vdot(e1, p);
+    v3 s = vsub(o, p1);
+    float bx = f * vdot(s, p);
+    if (bx < 0.0f || bx > 1.0f) return 0;
+    v3 q = vcross(s, e1);
+    float by = f * vdot(d, q);
+    if (by < 0.0f || by + bx > 1.0f) return 0;
+    f *= vdot(e2, q);
+    return f > 0.0f && f < 1.0f;
+}
+
+typedef struct { uint64_t node_visits, box_tests, tri_tests, overflows; } trav_count;
+
+/* :42-85, same stack discipline and 8-pop batched leaf tests; returns 1 when
+ * the segment origin..origin+dir is unoccluded.  The stack is stack_size deep
+ * (the reference's 32 entries overflow on deep trees); an overflow is counted. */
+static int raytrace(const or_scene *sc, v3 o, v3 d, int stack_size, trav_count *tc) {
+    int stack[256], top = 1;
+    int cand[16], ncand = 0, counter = 0;
+    if (stack_size > 256) stack_size = 256;
+    stack[0] = 0;
+    if (sc->n_nodes <= 0) return 1;
+    while (top > 0) {
+        const or_node *nd = &sc->nodes[stack[--top]];
+        tc->node_visits++;
+        tc->box_tests += 2;
+        int li = ray_aabb(o, d, f4xyz(nd->lmin), f4xyz(nd->lmax));
+        int ri = ray_aabb(o, d, f4xyz(nd->rmin), f4xyz(nd->rmax));
+        if (li) {
+            if (nd->left < 0) cand[ncand++] = ~nd->left;
+            else if (top < stack_size) stack[top++] = nd->left;
+            else tc->overflows++;
+        }
+        if (ri) {
+            if (nd->right < 0) cand[ncand++] = ~nd->right;
+            else if (top < stack_size) stack[top++] = nd->right;
+            else tc->overflows++;
+        }
+        if (++counter == 8) {
+            for (int i = 0; i < ncand; ++i) {
+                const or_tri *t = &sc->tris[cand[i]];
+                tc->tri_tests++;
+                if (ray_tri(f4xyz(t->p1), f4xyz(t->p2), f4xyz(t->p3), o, d)) return 0;
+            }
+            ncand = 0;
+            counter = 0;
+        }
+    }
+    for (int i = 0; i < ncand; ++i) {
+        const or_tri *t = &sc->tris[cand[i]];
+        tc->tri_tests++;
+        if (ray_tri(f4xyz(t->p1), f4xyz(t->p2), f4xyz(t->p3), o, d)) return 0;
+    }
+    return 1;
+}
+
+/* visibilityTest.glsl:1-4,26-29: returns 1 when p1 -> p2 is shadowed */
+static int test_visibility(const or_scene *sc, v3 p1, v3 p2, trav_count *tc) {
+    const float tmin = 0.001f;
+    v3 dir = vsub(p2, p1);
+    v3 off = vmuls(tmin, vnormalize(dir));
+    return !raytrace(sc, vadd(p1, off), vsub(dir, vmuls(2.0f, off)), STACK_SIZE, tc);
+}
+
+static void stats_add(or_stats *st, const trav_count *tc, uint64_t rays) {
+    if (!st) return;
+#pragma omp atomic
+    st->rays += rays;
+#pragma omp atomic
+    st->node_visits += tc->node_visits;
+#pragma omp atomic
+    st->box_tests += tc->box_tests;
+#pragma omp atomic
+    st->tri_tests += tc->tri_tests;
+#pragma omp atomic
+    st->stack_overflows += tc->overflows;
+}
+
+void or_ray_aabb_batch(int32_t n, const float *a, uint8_t *out) {
+    for (int32_t i = 0; i < n; ++i, a += 12)
+        out[i] = (uint8_t)ray_aabb(V(a[0], a[1], a[2]), V(a[3], a[4], a[5]), V(a[6], a[7], a[8]), V(a[9], a[10], a[11]));
+}
+void or_ray_tri_batch(int32_t n, const float *a, uint8_t *out) {
+    for (int32_t i = 0; i < n; ++i, a += 15)
+        out[i] = (uint8_t)ray_tri(V(a[6], a[7], a[8]), V(a[9], a[10], a[11]), V(a[12], a[13], a[14]),
+                                  V(a[0], a[1], a[2]), V(a[3], a[4], a[5]));
+}
+void or_raytrace_batch(const or_scene *sc, int32_t n, const float *rays, uint8_t *out, int32_t stack_size, or_stats *st) {
+    trav_count tot = {0, 0, 0, 0};
+#pragma omp parallel
+    {
+        trav_count tc = {0, 0, 0, 0};
+#pragma omp for schedule(dynamic, 256)
+        for (int32_t i = 0; i < n; ++i) {
+            const float *r = rays + 6 * (size_t)i;
+            out[i] = (uint8_t)raytrace(sc, V(r[0], r[1], r[2]), V(r[3], r[4], r[5]), stack_size, &tc);
+        }
+#pragma omp critical
+        {
+            tot.node_visits += tc.node_visits; tot.box_tests += tc.box_tests;
+            tot.tri_tests += tc.tri_tests; tot.overflows += tc.overflows;
+        }
+    }
+    stats_add(st, &tot, (uint64_t)n);
+}
+void or_test_visibility_batch(const or_scene *sc, int32_t n, const float *p1, const float *p2, uint8_t *out, or_stats *st) {
+    trav_count tot = {0, 0, 0, 0};
+#pragma omp parallel
+    {
+        trav_count tc = {0, 0, 0, 0};
+#pragma omp for schedule(dynamic, 256)
+        for (int32_t i = 0; i < n; ++i) {
+            const float *a = p1 + 3 * (size_t)i, *b = p2 + 3 * (size_t)i;
+            out[i] = (uint8_t)test_visibility(sc, V(a[0], a[1], a[2]), V(b[0], b[1], b[2]), &tc);
+        }
+#pragma omp critical
+        {
+            tot.node_visits += tc.node_visits; tot.box_tests += tc.box_tests;
+            tot.tri_tests += tc.tri_tests; tot.overflows += tc.overflows;
+        }
+    }
+    stats_add(st, &tot, (uint64_t)n);
+}
+
+/* ------------------------------------------------------------------ alias table */
+/* restirOmni.glsl:73-83 */
+static inline void alias_sample(const or_alias *tab, int32_t count, float r1, float r2, int *idx, float *prob) {
+    int col = imin((int)((float)count * r1), count - 1);
+    const or_alias *c = &tab[col];
+    if (c->prob > r2) { *idx = col; *prob = c->ori_prob; }
+    else { *idx = c->alias; *prob = c->alias_ori_prob; }
+}
+void or_alias_sample_batch(const or_alias *tab, int32_t count, int32_t n, const float *r, int32_t *idx, float *prob) {
+    for (int32_t i = 0; i < n; ++i) { int k; float p; alias_sample(tab, count, r[2 * i], r[2 * i + 1], &k, &p); idx[i] = k; prob[i] = p; }
+}
+
+/* misc.cpp:418-497: Vose's method with FIFO work lists, float arithmetic. */
+void or_build_alias_table(const or_point_light *pl, int32_t n_pl, const or_tri_light *tl, int32_t n_tl, or_alias *out) {
+    int32_t n = n_pl > 0 ? n_pl : n_tl;
+    if (n <= 0) return;
+    float *p = (float *)malloc(sizeof(float) * (size_t)n);
+    int32_t *big = (int32_t *)malloc(sizeof(int32_t) * (size_t)n * 2);
+    int32_t *small = (int32_t *)malloc(sizeof(int32_t) * (size_t)n * 2);
+    size_t bh = 0, bt = 0, sh = 0, st = 0; /* FIFO heads / tails; each index is pushed at most n times in total */
+    float sum = 0.0f;
+    for (int32_t i = 0; i < n; ++i) {
+        float v = n_pl > 0 ? pl[i].color_lum.w : tl[i].emission_lum.w * tl[i].normal_area.w;
+        sum += v;
+        p[i] = v;
+    }
+    for (int32_t i = 0; i < n; ++i) {
+        out[i].prob = 0.0f;
+        out[i].alias = -1;
+        out[i].ori_prob = p[i] / sum;
+        p[i] = (float)n * p[i] / sum;
+        if (p[i] >= 1.0f) big[bt++] = i; else small[st++] = i;
+    }
+    while (bh < bt && sh < st) {
+        int32_t g = big[bh++], l = small[sh++];
+        out[l].prob = p[l];
+        out[l].alias = g;
+        p[g] = (p[g] + p[l]) - 1.0f;
+        if (p[g] < 1.0f) small[st++] = g; else big[bt++] = g;
+    }
+    while (bh < bt) { int32_t g = big[bh++]; out[g].prob = 1.0f; out[g].alias = g; }
+    while (sh < st) { int32_t l = small[sh++]; out[l].prob = 1.0f; out[l].alias = l; }
+    for (int32_t i = 0; i < n; ++i) out[i].alias_ori_prob = out[out[i].alias].ori_prob;
+    free(p); free(big); free(small);
+}
+
+/* ------------------------------------------------------------------ reservoirs (reservoir.glsl:6-76) */
+static inline void update_reservoir(or_reservoir *r, float weight, v3 pos, or_f4 nrm, float lum, int32_t idx,
+                                    float p_hat, float w, pcg_t *rng) { /* :6-26 */
+    r->sum_weights += weight;
+    float replace = weight / r->sum_weights;
+    if (rand_float(rng) < replace) {
+        r->pos_lum.x = pos.x; r->pos_lum.y = pos.y; r->pos_lum.z = pos.z; r->pos_lum.w = lum;
+        r->normal = nrm;
+        r->light_index = idx;
+        r->p_hat = p_hat;
+        r->w = w;
+    }
+}
+static inline void add_sample(or_reservoir *r, v3 pos, or_f4 nrm, float lum, int32_t idx, float p_hat,
+                              float sample_p, pcg_t *rng) { /* :28-42 */
+    float weight = p_hat / sample_p;
+    r->m += 1;
+    float w = (r->sum_weights + weight) / ((float)r->m * p_hat);
+    update_reservoir(r, weight, pos, nrm, lum, idx, p_hat, w, rng);
+}
+static inline void combine_reservoirs(or_reservoir *self, const or_reservoir *other, float p_hat, pcg_t *rng) { /* :44-64 */
+    self->m += other->m;
+    float weight = p_hat * other->w * (float)other->m;
+    if (weight > 0.0f)
+        update_reservoir(self, weight, f4xyz(other->pos_lum), other->normal, other->pos_lum.w, other->light_index,
+                         p_hat, other->w, rng);
+    if (self->w > 0.0f) self->w = self->sum_weights / ((float)self->m * self->p_hat);
+}
+/* :66-76; the fields the reference leaves uninitialised are defined as zero */
+static inline void new_reservoir(or_reservoir *r) { memset(r, 0, sizeof(*r)); }
+
+static int crop_ok(const int32_t *crop, int W, int H, int *x0, int *y0, int *cw, int *ch) {
+    if (!crop) { *x0 = 0; *y0 = 0; *cw = W; *ch = H; return 1; }
+    *x0 = crop[0]; *y0 = crop[1]; *cw = crop[2]; *ch = crop[3];
+    return *x0 >= 0 && *y0 >= 0 && *cw >= 0 && *ch >= 0 && *x0 + *cw <= W && *y0 + *ch <= H;
+}
+
+/* ------------------------------------------------------------------ RIS + visibility + temporal (restirOmni.glsl:86-212) */
+int or_initial_temporal(const or_scene *sc, const or_gbuffer *cur, const or_gbuffer *prev,
+                        const or_reservoir *prev_res, or_reservoir *out, const or_uniforms *u,
+                        const int32_t *crop, or_stats *st) {
+    srgb_init();
+    int W = (int)u->size[0], H = (int)u->size[1];
+    int x0, y0, cw, ch;
+    if (W != cur->width || H != cur->height) return -1;
+    if (!crop_ok(crop, W, H, &x0, &y0, &cw, &ch)) return -2;
+    const int use_point = sc->n_point_lights != 0;
+    const v3 cam = f4xyz(u->camera_pos);
+    trav_count tot = {0, 0, 0, 0};
+    uint64_t rays = 0;
+#pragma omp parallel
+    {
+        trav_count tc = {0, 0, 0, 0};
+        uint64_t my_rays = 0;
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t pi = 0; pi < (int64_t)cw * ch; ++pi) {
+            int x = x0 + (int)(pi % cw), y = y0 + (int)(pi / cw);
+            texel_t t;
+            fetch_texel(cur, x, y, &t);
+            float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
+            or_reservoir res;
+            new_reservoir(&res);
+            pcg_t rng = pcg_seed((uint64_t)u->frame, (uint64_t)((uint32_t)y * 10007u + (uint32_t)x));
+            int zero_normal = !(vdot(t.normal, t.normal) != 0.0f);
+            if (!zero_normal) {
+                for (int i = 0; (uint32_t)i < u->initial_light_sample_count; ++i) {
+                    int sel; float prob;
+                    float r1 = rand_float(&rng), r2 = rand_float(&rng);
+                    alias_sample(sc->alias, sc->n_alias, r1, r2, &sel, &prob);
+                    v3 lpos; or_f4 ln; float llum; int32_t lidx;
+                    if (use_point) {
+                        const or_point_light *L = &sc->point_lights[sel];
+                        lpos = f4xyz(L->pos);
+                        llum = L->color_lum.w;
+                        lidx = sel;
+                        ln.x = ln.y = ln.z = ln.w = 0.0f;
+                    } else {
+                        const or_tri_light *L = &sc->tri_lights[sel];
+                        float a = rand_float(&rng), b = rand_float(&rng);
+                        /* pickPointOnTriangle, restirOmni.glsl:68-71 */
+                        float sa = sqrtf(a);
+                        v3 q1 = vmuls(1.0f - sa, f4xyz(L->p1));
+                        v3 q2 = vmuls(sa * (1.0f - b), f4xyz(L->p2));
+                        v3 q3 = vmuls(b * sa, f4xyz(L->p3));
+                        lpos = vadd(vadd(q1, q2), q3);
+                        llum = L->emission_lum.w;
+                        lidx = -1 - sel;
+                        v3 wi = vnormalize(vsub(t.wpos, lpos));
+                        v3 nn = f4xyz(L->normal_area);
+                        prob /= fabsf(vdot(wi, nn)) * L->normal_area.w;
+                        ln.x = nn.x; ln.y = nn.y; ln.z = nn.z; ln.w = 1.0f;
+                    }
+                    float ph = eval_phat(t.wpos, lpos, cam, t.normal, f4xyz(ln), ln.w > 0.5f, albedo_lum, llum,
+                                         t.roughness, t.metallic);
+                    add_sample(&res, lpos, ln, llum, lidx, ph, prob, &rng);
+                }
+            }
+            /* visibility reuse :147-160 -- a background pixel's (zero normal) sample is
+             * undefined in the reference; here it is the zero sample, for which zeroing
+             * w and sumWeights changes nothing, so no ray is traced for it. */
+            if ((u->flags & OR_FLAG_VISIBILITY) && !zero_normal) {
+                ++my_rays;
+                if (test_visibility(sc, t.wpos, f4xyz(res.pos_lum), &tc)) {
+                    res.w = 0.0f;
+                    res.sum_weights = 0.0f;
+                }
+            }
+            /* temporal reuse :162-209 */
+            if ((u->flags & OR_FLAG_TEMPORAL) && prev != NULL && prev_res != NULL) {
+                const float *m = u->prev_pv;
+                float px = ((m[0] * t.wpos.x + m[4] * t.wpos.y) + m[8] * t.wpos.z) + m[12] * 1.0f;
+                float py = ((m[1] * t.wpos.x + m[5] * t.wpos.y) + m[9] * t.wpos.z) + m[13] * 1.0f;
+                float pw = ((m[3] * t.wpos.x + m[7] * t.wpos.y) + m[11] * t.wpos.z) + m[15] * 1.0f;
+                px /= pw;
+                py /= pw;
+                px = (px + 1.0f) * 0.5f * (float)u->size[0];
+                py = (py + 1.0f) * 0.5f * (float)u->size[1];
+                if (px > 0.0f && py > 0.0f && px < (float)u->size[0] && py < (float)u->size[1]) {
+                    int fx = (int)px, fy = (int)py;
+                    texel_t pt;
+                    fetch_texel(prev, fx, fy, &pt);
+                    v3 dp = vsub(t.wpos, pt.wpos);
+                    if (vdot(dp, dp) < 0.01f) {
+                        v3 da = vsub(t.albedo, pt.albedo);
+                        if (vdot(da, da) < 0.01f) {
+                            if (vdot(t.normal, pt.normal) > 0.5f) {
+                                or_reservoir pr = prev_res[(size_t)fy * u->size[0] + (size_t)fx];
+                                uint32_t cap = u->temporal_mult * res.m;
+                                pr.m = pr.m < cap ? pr.m : cap;
+                                float ph = eval_phat(t.wpos, f4xyz(pr.pos_lum), cam, t.normal, f4xyz(pr.normal),
+                                                     pr.normal.w > 0.5f, albedo_lum, pr.pos_lum.w, t.roughness,
+                                                     t.metallic);
+                                combine_reservoirs(&res, &pr, ph, &rng);
+                            }
+                        }
+                    }
+                }
+            }
+            out[(size_t)y * (size_t)W + (size_t)x] = res;
+        }
+#pragma omp critical
+        {
+            tot.node_visits += tc.node_visits; tot.box_tests += tc.box_tests;
+            tot.tri_tests += tc.tri_tests; tot.overflows += tc.overflows;
+            rays += my_rays;
+        }
+    }
+    stats_add(st, &tot, rays);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ biased spatial (spatialReuse.comp:30-86) */
+int or_spatial_biased(const or_scene *sc, const or_gbuffer *g, const or_reservoir *in, or_reservoir *out,
+                      const or_uniforms *u, int32_t iter, const int32_t *crop) {
+    (void)sc;
+    srgb_init();
+    int W = (int)u->size[0], H = (int)u->size[1];
+    int x0, y0, cw, ch;
+    if (W != g->width || H != g->height) return -1;
+    if (!crop_ok(crop, W, H, &x0, &y0, &cw, &ch)) return -2;
+    const v3 cam = f4xyz(u->camera_pos);
+    const float cos_thr = or_cosf(u->normal_threshold * DEG2RAD_F);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t pi = 0; pi < (int64_t)cw * ch; ++pi) {
+        int x = x0 + (int)(pi % cw), y = y0 + (int)(pi / cw);
+        texel_t t;
+        fetch_texel(g, x, y, &t);
+        float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
+        size_t ri = (size_t)y * (size_t)W + (size_t)x;
+        or_reservoir res = in[ri];
+        pcg_t rng = pcg_seed((uint64_t)(u->frame * 31u + (uint32_t)iter), (uint64_t)((uint32_t)y * 10007u + (uint32_t)x));
+        for (uint32_t i = 0; i < u->spatial_neighbors; ++i) {
+            float angle = rand_float(&rng) * 2.0f * PI_F;
+            float radius = sqrtf(rand_float(&rng)) * u->spatial_radius;
+            float s, c;
+            or_sincos(angle, &s, &c);
+            int ox = (int)floorf(c * radius), oy = (int)floorf(s * radius);
+            int nx = iclamp(x + ox, 0, W - 1), ny = iclamp(y + oy, 0, H - 1);
+            size_t ni = (size_t)ny * (size_t)W + (size_t)nx;
+            float nd = g->depth[ni];
+            const uint16_t *nn = g->normal + 4 * ni;
+            v3 nnor = V(or_half_to_float(nn[0]), or_half_to_float(nn[1]), or_half_to_float(nn[2]));
+            if (fabsf(nd - t.depth) > u->pos_threshold * fabsf(t.depth) || vdot(nnor, t.normal) < cos_thr) continue;
+            const or_reservoir *rr = &in[ni];
+            float ph = eval_phat(t.wpos, f4xyz(rr->pos_lum), cam, t.normal, f4xyz(rr->normal), rr->normal.w > 0.5f,
+                                 albedo_lum, rr->pos_lum.w, t.roughness, t.metallic);
+            combine_reservoirs(&res, rr, ph, &rng);
+        }
+        out[ri] = res;
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------ unbiased spatial (unbiasedReuse.glsl:50-185)
+ * num_neighbors is NUM_NEIGHBORS (the reference hard-codes 3, :48).  The
+ * reference seeds with frame*17 (:72); pass_index p seeds with frame*17 + p
+ * so chained passes draw fresh neighbours (p = 0 is the reference). */
+int or_spatial_unbiased(const or_scene *sc, const or_gbuffer *g, const or_reservoir *in, or_reservoir *out,
+                        const or_uniforms *u, int32_t num_neighbors, int32_t pass_index, const int32_t *crop, or_stats *st) {
+    srgb_init();
+    int W = (int)u->size[0], H = (int)u->size[1];
+    int x0, y0, cw, ch;
+    if (W != g->width || H != g->height) return -1;
+    if (!crop_ok(crop, W, H, &x0, &y0, &cw, &ch)) return -2;
+    if (num_neighbors < 0 || num_neighbors > 64) return -3;
+    const v3 cam = f4xyz(u->camera_pos);
+    const int vis = (u->flags & OR_FLAG_VISIBILITY) != 0;
+    trav_count tot = {0, 0, 0, 0};
+    uint64_t rays = 0;
+#pragma omp parallel
+    {
+        trav_count tc = {0, 0, 0, 0};
+        uint64_t my_rays = 0;
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t pi = 0; pi < (int64_t)cw * ch; ++pi) {
+            int x = x0 + (int)(pi % cw), y = y0 + (int)(pi / cw);
+            texel_t t;
+            fetch_texel(g, x, y, &t);
+            float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
+            size_t ri = (size_t)y * (size_t)W + (size_t)x;
+            or_reservoir res = in[ri];
+            pcg_t rng = pcg_seed((uint64_t)(u->frame * 17u + (uint32_t)pass_index), (uint64_t)((uint32_t)y * 10007u + (uint32_t)x));
+            int npx[64], npy[64];
+            uint32_t nm[64];
+            uint32_t orig_m = res.m;
+            for (int i = 0; i < num_neighbors; ++i) {
+                float angle = rand_float(&rng) * 2.0f * PI_F;
+                float radius = sqrtf(rand_float(&rng)) * u->spatial_radius;
+                float s, c;
+                or_sincos(angle, &s, &c);
+                int ox = (int)roundf(c * radius), oy = (int)roundf(s * radius);
+                int nx = iclamp(x + ox, 0, (int)(u->size[0] - 1u)), ny = iclamp(y + oy, 0, (int)(u->size[1] - 1u));
+                const or_reservoir *rr = &in[(size_t)ny * (size_t)W + (size_t)nx];
+                npx[i] = nx; npy[i] = ny;
+                nm[i] = rr->m;
+                res.m += rr->m;
+                float ph = eval_phat(t.wpos, f4xyz(rr->pos_lum), cam, t.normal, f4xyz(rr->normal), rr->normal.w > 0.5f,
+                                     albedo_lum, rr->pos_lum.w, t.roughness, t.metallic);
+                float weight = ph * rr->w * (float)rr->m;
+                if (weight > 0.0f)
+                    update_reservoir(&res, weight, f4xyz(rr->pos_lum), rr->normal, rr->pos_lum.w, rr->light_index, ph,
+                                     rr->w, &rng);
+            }
+            v3 lpos = f4xyz(res.pos_lum);
+            uint32_t ns = orig_m;
+            for (int j = 0; j < num_neighbors; ++j) {
+                texel_t nt;
+                fetch_texel(g, npx[j], npy[j], &nt);
+                if (vdot(vsub(lpos, nt.wpos), nt.normal) < 0.0f) continue;
+                if (vis) {
+                    ++my_rays;
+                    if (test_visibility(sc, nt.wpos, lpos, &tc)) continue;
+                }
+                ns += nm[j];
+            }
+            if (vis) {
+                ++my_rays;
+                if (test_visibility(sc, t.wpos, lpos, &tc)) ns = 0;
+            }
+            if (ns > 0) {
+                res.w = res.sum_weights / ((float)ns * res.p_hat);
+            } else {
+                res.w = 0.0f;
+                res.sum_weights = 0.0f;
+            }
+            out[ri] = res;
+        }
+#pragma omp critical
+        {
+            tot.node_visits += tc.node_visits; tot.box_tests += tc.box_tests;
+            tot.tri_tests += tc.tri_tests; tot.overflows += tc.overflows;
+            rays += my_rays;
+        }
+    }
+    stats_add(st, &tot, rays);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ shading (lighting.frag:43-71,103) */
+int or_shade(const or_scene *sc, const or_gbuffer *g, const or_reservoir *resv, const or_lighting_uniforms *u,
+             float *rgba, const int32_t *crop) {
+    srgb_init();
+    int W = (int)u->size[0], H = (int)u->size[1];
+    int x0, y0, cw, ch;
+    if (W != g->width || H != g->height) return -1;
+    if (!crop_ok(crop, W, H, &x0, &y0, &cw, &ch)) return -2;
+    const v3 cam = f4xyz(u->camera_pos);
+    const float inv_gamma = 1.0f / u->gamma;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t pi = 0; pi < (int64_t)cw * ch; ++pi) {
+        int x = x0 + (int)(pi % cw), y = y0 + (int)(pi / cw);
+        texel_t t;
+        fetch_texel(g, x, y, &t);
+        size_t ri = (size_t)y * (size_t)W + (size_t)x;
+        const or_reservoir *r = &resv[ri];
+        v3 emission;
+        if (r->light_index < 0) {
+            int k = -1 - r->light_index;
+            emission = (k < sc->n_tri_lights) ? f4xyz(sc->tri_lights[k].emission_lum) : V(0.0f, 0.0f, 0.0f);
+        } else {
+            int k = r->light_index;
+            emission = (k < sc->n_point_lights) ? f4xyz(sc->point_lights[k].color_lum) : V(0.0f, 0.0f, 0.0f);
+        }
+        v3 ph = eval_phat_full(t.wpos, f4xyz(r->pos_lum), cam, t.normal, f4xyz(r->normal), r->normal.w > 0.5f,
+                               t.albedo, emission, t.roughness, t.metallic);
+        v3 col = V(0.0f + ph.x * r->w, 0.0f + ph.y * r->w, 0.0f + ph.z * r->w);
+        col = vdivs(col, 1.0f); /* RESERVOIR_SIZE */
+        if (t.albedo_a > 0.5f) col = t.albedo;
+        if (u->gamma != 1.0f) col = V(powf(col.x, inv_gamma), powf(col.y, inv_gamma), powf(col.z, inv_gamma));
+        rgba[4 * ri] = col.x; rgba[4 * ri + 1] = col.y; rgba[4 * ri + 2] = col.z; rgba[4 * ri + 3] = 1.0f;
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------ FP64 brute-force judge
+ * L(x) = sum over every light of emission * BRDF * cos / d^2 * V, with the
+ * reference's BRDF and the reference's shadow segment, both in double, on
+ * the same BVH.  Emissive pixels return their albedo (lighting.frag:69-71). */
+typedef struct { double x, y, z; } d3;
+static inline d3 D(double x, double y, double z) { d3 r; r.x = x; r.y = y; r.z = z; return r; }
+static inline d3 dsub(d3 a, d3 b) { return D(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline d3 dadd(d3 a, d3 b) { return D(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline d3 dmuls(double s, d3 a) { return D(s * a.x, s * a.y, s * a.z); }
+static inline double ddot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline d3 dcross(d3 a, d3 b) { return D(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y); }
+static inline d3 dnorm(d3 a) { double l = sqrt(ddot(a, a)); return D(a.x / l, a.y / l, a.z / l); }
+static inline d3 df4(or_f4 f) { return D(f.x, f.y, f.z); }
+static inline double dmin(double a, double b) { return b < a ? b : a; }
+static inline double dmax(double a, double b) { return a < b ? b : a; }
+
+static int d_ray_aabb(d3 o, d3 d, or_f4 bmin, or_f4 bmax) {
+    double t0x = (bmin.x - o.x) / d.x, t1x = (bmax.x - o.x) / d.x;
+    double t0y = (bmin.y - o.y) / d.y, t1y = (bmax.y - o.y) / d.y;
+    double t0z = (bmin.z - o.z) / d.z, t1z = (bmax.z - o.z) / d.z;
+    double rmin = dmax(dmin(t0x, t1x), dmax(dmin(t0y, t1y), dmin(t0z, t1z)));
+    double rmax = dmin(dmax(t0x, t1x), dmin(dmax(t0y, t1y), dmax(t0z, t1z)));
+    return rmin < 1.0 && rmax >= rmin && rmax > 0.0;
+}
+static int d_ray_tri(const or_tri *t, d3 o, d3 d) {
+    d3 p1 = df4(t->p1);
+    d3 e1 = dsub(df4(t->p2), p1), e2 = dsub(df4(t->p3), p1);
+    d3 p = dcross(d, e2);
+    double f = 1.0 / ddot(e1, p);
+    d3 s = dsub(o, p1);
+    double bx = f * ddot(s, p);
+    if (bx < 0.0 || bx > 1.0) return 0;
+    d3 q = dcross(s, e1);
+    double by = f * ddot(d, q);
+    if (by < 0.0 || by + bx > 1.0) return 0;
+    f *= ddot(e2, q);
+    return f > 0.0 && f < 1.0;
+}
+static int d_shadowed(const or_scene *sc, d3 p1, d3 p2) {
+    d3 dir = dsub(p2, p1);
+    d3 off = dmuls(0.001, dnorm(dir));
+    d3 o = dadd(p1, off), d = dsub(dir, dmuls(2.0, off));
+    int stack[256], top = 1;
+    stack[0] = 0;
+    if (sc->n_nodes <= 0) return 0;
+    while (top > 0) {
+        const or_node *nd = &sc->nodes[stack[--top]];
+        if (d_ray_aabb(o, d, nd->lmin, nd->lmax)) {
+            if (nd->left < 0) { if (d_ray_tri(&sc->tris[~nd->left], o, d)) return 1; }
+            else if (top < 256) stack[top++] = nd->left;
+        }
+        if (d_ray_aabb(o, d, nd->rmin, nd->rmax)) {
+            if (nd->right < 0) { if (d_ray_tri(&sc->tris[~nd->right], o, d)) return 1; }
+            else if (top < 256) stack[top++] = nd->right;
+        }
+    }
+    return 0;
+}
+static double d_schlick(double c) { double m = dmin(dmax(1.0 - c, 0.0), 1.0); double sm = m * m; return sm * sm * m; }
+static double d_smith(double ndotv, double ag) { double a = ag * ag, b = ndotv * ndotv; return 1.0 / (fabs(ndotv) + dmax(sqrt(a + b - a * b), 0.0001)); }
+
+int or_brute_force_fp64(const or_scene *sc, const or_gbuffer *g, const float *cam3, double *rgb_out, const int32_t *crop) {
+    srgb_init();
+    int W = g->width, H = g->height;
+    int x0, y0, cw, ch;
+    if (!crop_ok(crop, W, H, &x0, &y0, &cw, &ch)) return -2;
+    const d3 cam = D(cam3[0], cam3[1], cam3[2]);
+    const int use_point = sc->n_point_lights != 0;
+    const int nl = use_point ? sc->n_point_lights : sc->n_tri_lights;
+    if (!use_point && nl > 0) return -4; /* triangle lights need an area integral; not part of the judge */
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int64_t pi = 0; pi < (int64_t)cw * ch; ++pi) {
+        int x = x0 + (int)(pi % cw), y = y0 + (int)(pi / cw);
+        texel_t t;
+        fetch_texel(g, x, y, &t);
+        double acc[3] = {0.0, 0.0, 0.0};
+        size_t oi = (size_t)(pi) * 3;
+        if (t.albedo_a > 0.5f) {
+            rgb_out[oi] = t.albedo.x; rgb_out[oi + 1] = t.albedo.y; rgb_out[oi + 2] = t.albedo.z;
+            continue;
+        }
+        d3 n = D(t.normal.x, t.normal.y, t.normal.z);
+        d3 wp = D(t.wpos.x, t.wpos.y, t.wpos.z);
+        if (ddot(n, n) == 0.0) { rgb_out[oi] = rgb_out[oi + 1] = rgb_out[oi + 2] = 0.0; continue; }
+        double rough = t.roughness, metal = t.metallic;
+        double alb[3] = {t.albedo.x, t.albedo.y, t.albedo.z};
+        d3 wo = dnorm(dsub(cam, wp));
+        double cos_out = ddot(n, wo);
+        for (int l = 0; l < nl; ++l) {
+            const or_point_light *L = &sc->point_lights[l];
+            d3 lp = df4(L->pos);
+            d3 wi = dsub(lp, wp);
+            if (ddot(wi, n) < 0.0) continue;
+            double sq = ddot(wi, wi);
+            wi = dmuls(1.0 / sqrt(sq), wi);
+            double cos_in = ddot(n, wi);
+            if (cos_in < 0.0) continue;
+            d3 h = dnorm(dadd(wi, wo));
+            double cos_half = ddot(n, h), cos_in_half = ddot(wi, h);
+            double fi = d_schlick(cos_in), fo = d_schlick(cos_out);
+            double fd90 = 0.5 + 2.0 * cos_in_half * cos_in_half * rough;
+            double fd = (1.0 * (1.0 - fi) + fd90 * fi) * (1.0 * (1.0 - fo) + fd90 * fo);
+            double dfac = fd * (1.0 - metal) / PI_D;
+            double fr = d_schlick(cos_in_half);
+            double a = dmax(0.001, rough * rough);
+            double a2 = a * a, tt = 1.0 + (a2 - 1.0) * cos_half * cos_half;
+            double ds = a2 / (PI_D * tt * tt);
+            double gd = d_smith(cos_in, a) * d_smith(cos_out, a) * ds;
+            double geometry = cos_in / sq;
+            if (geometry == 0.0) continue;
+            if (d_shadowed(sc, wp, lp)) continue;
+            double em[3] = {L->color_lum.x, L->color_lum.y, L->color_lum.z};
+            for (int c = 0; c < 3; ++c) {
+                double sc_ = 0.04 * (1.0 - metal) + alb[c] * metal;
+                double fs = sc_ * (1.0 - fr) + 1.0 * fr;
+                acc[c] += em[c] * (alb[c] * dfac + fs * gd) * geometry;
+            }
+        }
+        rgb_out[oi] = acc[0]; rgb_out[oi + 1] = acc[1]; rgb_out[oi + 2] = acc[2];
+    }
+    return 0;
+}
+
+int or_max_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+void or_set_threads(int32_t n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}

@@ -1,0 +1,147 @@
+/*
+ * oracle.h -- CPU oracle for the ReSTIR direct-lighting hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker: the parity tests,
+ * __graft_entry__.smoke() and the CPU-baseline leg of bench.py load it to
+ * compute the expected result of every pass on the same inputs the CUDA path
+ * receives.  Product code never links, loads or calls it.
+ *
+ * It restates, in plain single-precision C with OpenMP over pixels, the
+ * reference's GLSL passes (reference paths are relative to the reference
+ * project root):
+ *   PCG32                src/shaders/include/rand.glsl:7-32
+ *   reservoir ops        src/shaders/include/reservoir.glsl:6-76
+ *   BRDF / p-hat         src/shaders/include/disneyBRDF.glsl:5-90,
+ *                        src/shaders/include/restirUtils.glsl:3-55
+ *   BVH traversal        src/shaders/include/softwareRaytracing.glsl:3-85,
+ *                        src/shaders/include/visibilityTest.glsl:1-30
+ *   RIS+vis+temporal     src/shaders/restirOmni.glsl:68-212
+ *   biased spatial       src/shaders/spatialReuse.comp:30-86
+ *   unbiased spatial     src/shaders/unbiasedReuse.glsl:50-185
+ *   shading              src/shaders/lighting.frag:43-71,103
+ *   alias table (Vose)   src/misc.cpp:418-497
+ * plus an FP64 brute-force judge (sum over every light with exact
+ * visibility) used for image RMSE.
+ *
+ * The byte layouts of every struct below equal the reference's std430/std140
+ * layouts (src/shaderIncludes.h, the files under src/shaders/include/structs/) and the
+ * product's C ABI (include/restir_gb300.h).
+ */
+#ifndef RESTIR_ORACLE_H
+#define RESTIR_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct { float x, y, z, w; } or_f4;
+
+typedef struct {             /* Reservoir with RESERVOIR_SIZE 1: 64 bytes */
+    or_f4 pos_lum;           /* position_emissionLum */
+    or_f4 normal;            /* light normal, w>0.5 => use it */
+    int32_t light_index;     /* negative: triangle light -1-i */
+    float p_hat;
+    float sum_weights;
+    float w;
+    uint32_t m;              /* numStreamSamples */
+    uint32_t pad[3];
+} or_reservoir;
+
+typedef struct { or_f4 lmin, lmax, rmin, rmax; int32_t left, right, pad0, pad1; } or_node;   /* 80 B */
+typedef struct { or_f4 p1, p2, p3; } or_tri;                                                /* 48 B */
+typedef struct { or_f4 pos, color_lum; } or_point_light;                                    /* 32 B */
+typedef struct { or_f4 p1, p2, p3, emission_lum, normal_area; } or_tri_light;               /* 80 B */
+typedef struct { float prob; int32_t alias; float ori_prob; float alias_ori_prob; } or_alias; /* 16 B */
+
+typedef struct {             /* RestirUniforms: 128 bytes */
+    float prev_pv[16];       /* column-major prevFrameProjectionViewMatrix */
+    or_f4 camera_pos;
+    uint32_t size[2];
+    uint32_t frame;
+    uint32_t initial_light_sample_count;
+    uint32_t temporal_mult;
+    float pos_threshold;
+    float normal_threshold;  /* degrees */
+    uint32_t spatial_neighbors;
+    float spatial_radius;
+    int32_t flags;
+    uint32_t pad[2];
+} or_uniforms;
+
+typedef struct {             /* LightingPassUniforms: 96 bytes */
+    float prev_pv[16];
+    or_f4 camera_pos;
+    uint32_t size[2];
+    int32_t debug_mode;
+    float gamma;
+} or_lighting_uniforms;
+
+#define OR_FLAG_VISIBILITY 1
+#define OR_FLAG_TEMPORAL 2
+
+typedef struct {
+    const or_node *nodes; int32_t n_nodes;
+    const or_tri *tris; int32_t n_tris;
+    const or_point_light *point_lights; int32_t n_point_lights;
+    const or_tri_light *tri_lights; int32_t n_tri_lights;
+    const or_alias *alias; int32_t n_alias;
+} or_scene;
+
+typedef struct {             /* headless G-buffer planes, row-major, width*height texels */
+    int32_t width, height;
+    const uint8_t *albedo;   /* RGBA8, sRGB-encoded rgb, a = emissive flag */
+    const uint16_t *normal;  /* RGBA16F bit patterns */
+    const uint16_t *material;/* RG16 unorm (roughness, metallic) */
+    const float *world_pos;  /* RGBA32F */
+    const float *depth;      /* D32F */
+} or_gbuffer;
+
+typedef struct {
+    uint64_t rays;           /* shadow segments traced */
+    uint64_t node_visits;    /* nodes popped */
+    uint64_t box_tests;
+    uint64_t tri_tests;
+    uint64_t stack_overflows;
+} or_stats;
+
+/* ---- primitives ---- */
+void or_pcg_stream(uint64_t seed, uint64_t seq, int32_t n, uint32_t *out);
+void or_rand_floats(uint64_t seed, uint64_t seq, int32_t n, float *out);
+void or_sincos_batch(int32_t n, const float *x, float *s, float *c);
+void or_srgb_lut(float *out256);
+float or_half_to_float(uint16_t h);
+/* args: 20 floats per call: worldPos3 lightPos3 camPos3 normal3 lightNormal3 useLightNormal albedoLum emissionLum roughness metallic */
+void or_eval_phat_batch(int32_t n, const float *args, float *out);
+/* args: 24 floats: worldPos3 lightPos3 camPos3 normal3 lightNormal3 useLightNormal albedo3 emission3 roughness metallic */
+void or_eval_phat_full_batch(int32_t n, const float *args, float *out3);
+void or_ray_aabb_batch(int32_t n, const float *args /*12*/, uint8_t *out);
+void or_ray_tri_batch(int32_t n, const float *args /*15*/, uint8_t *out);
+/* raw traversal: origin3,dir3 per ray; out 1 = unoccluded (reference raytrace() value) */
+void or_raytrace_batch(const or_scene *scene, int32_t n, const float *rays, uint8_t *out, int32_t stack_size, or_stats *stats);
+/* testVisibility: p1[3],p2[3] per ray; out 1 = shadowed */
+void or_test_visibility_batch(const or_scene *scene, int32_t n, const float *p1, const float *p2, uint8_t *out, or_stats *stats);
+void or_alias_sample_batch(const or_alias *table, int32_t count, int32_t n, const float *r, int32_t *idx, float *prob);
+void or_build_alias_table(const or_point_light *pl, int32_t n_pl, const or_tri_light *tl, int32_t n_tl, or_alias *out);
+
+/* ---- passes; crop = {x0, y0, w, h} or NULL for the full frame; out is full-frame sized ---- */
+int or_initial_temporal(const or_scene *scene, const or_gbuffer *cur, const or_gbuffer *prev,
+                        const or_reservoir *prev_res, or_reservoir *out, const or_uniforms *u,
+                        const int32_t *crop, or_stats *stats);
+int or_spatial_biased(const or_scene *scene, const or_gbuffer *g, const or_reservoir *in, or_reservoir *out,
+                      const or_uniforms *u, int32_t iter, const int32_t *crop);
+int or_spatial_unbiased(const or_scene *scene, const or_gbuffer *g, const or_reservoir *in, or_reservoir *out,
+                        const or_uniforms *u, int32_t num_neighbors, int32_t pass_index, const int32_t *crop, or_stats *stats);
+int or_shade(const or_scene *scene, const or_gbuffer *g, const or_reservoir *res, const or_lighting_uniforms *u,
+             float *rgba_out, const int32_t *crop);
+int or_brute_force_fp64(const or_scene *scene, const or_gbuffer *g, const float *camera_pos3,
+                        double *rgb_out, const int32_t *crop);
+
+int or_max_threads(void);
+void or_set_threads(int32_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,155 @@
+"""ctypes binding of the CPU oracle (liboracle.so) and of the reference build
+(_ref/libref.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py as the checker; never by the product.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libref.so"
+REFERENCE_ROOT = Path(os.environ.get("RESTIR_REFERENCE", "/root/reference"))
+
+
+def build(ref: bool | None = None) -> None:
+    """Builds liboracle.so and, when the reference sources exist, _ref/libref.so."""
+    env = dict(os.environ)
+    r = subprocess.run(["make", "-C", str(HERE), "liboracle.so"], capture_output=True, text=True, env=env)
+    if r.returncode != 0:  # retry without OpenMP (toolchains without libgomp)
+        r = subprocess.run(["make", "-C", str(HERE), "liboracle.so", "OMP="], capture_output=True, text=True, env=env)
+        if r.returncode != 0:
+            raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+    if ref is None:
+        ref = (REFERENCE_ROOT / "src" / "aabbTreeBuilder.cpp").exists()
+    if ref:
+        r = subprocess.run(["make", "-C", str(HERE), "ref", f"REF={REFERENCE_ROOT}"], capture_output=True, text=True,
+                           env=env)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference build failed:\n{r.stdout}\n{r.stderr}")
+
+
+class Scene(C.Structure):
+    _fields_ = [("nodes", C.c_void_p), ("n_nodes", C.c_int32), ("tris", C.c_void_p), ("n_tris", C.c_int32),
+                ("point_lights", C.c_void_p), ("n_point_lights", C.c_int32), ("tri_lights", C.c_void_p),
+                ("n_tri_lights", C.c_int32), ("alias", C.c_void_p), ("n_alias", C.c_int32)]
+
+
+class GBuffer(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("albedo", C.c_void_p), ("normal", C.c_void_p),
+                ("material", C.c_void_p), ("world_pos", C.c_void_p), ("depth", C.c_void_p)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("rays", C.c_uint64), ("node_visits", C.c_uint64), ("box_tests", C.c_uint64),
+                ("tri_tests", C.c_uint64), ("stack_overflows", C.c_uint64)]
+
+
+_oracle = None
+_ref = None
+
+
+def oracle():
+    global _oracle
+    if _oracle is None:
+        if not LIB.exists():
+            build(ref=False)
+        _oracle = C.CDLL(str(LIB))
+        _oracle.or_half_to_float.restype = C.c_float
+        _oracle.or_half_to_float.argtypes = [C.c_uint16]
+        _oracle.or_pcg_stream.argtypes = [C.c_uint64, C.c_uint64, C.c_int32, C.c_void_p]
+        _oracle.or_rand_floats.argtypes = [C.c_uint64, C.c_uint64, C.c_int32, C.c_void_p]
+        for name in ("or_initial_temporal", "or_spatial_biased", "or_spatial_unbiased", "or_shade",
+                     "or_brute_force_fp64"):
+            getattr(_oracle, name).restype = C.c_int
+    return _oracle
+
+
+def ref_available() -> bool:
+    return REF_LIB.exists()
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        _ref = C.CDLL(str(REF_LIB))
+    return _ref
+
+
+def P(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def scene_struct(scene) -> tuple[Scene, list]:
+    """Oracle view of a restir_gb300 Scene (keeps the arrays alive)."""
+    keep = [scene.nodes, scene.triangles, scene.point_lights, scene.alias]
+    s = Scene(scene.nodes.ctypes.data, len(scene.nodes), scene.triangles.ctypes.data, len(scene.triangles),
+              scene.point_lights.ctypes.data, len(scene.point_lights), None, 0, scene.alias.ctypes.data,
+              len(scene.alias))
+    return s, keep
+
+
+def gbuffer_struct(g: dict) -> GBuffer:
+    h, w = g["depth"].shape
+    return GBuffer(w, h, g["albedo"].ctypes.data, g["normal"].ctypes.data, g["material"].ctypes.data,
+                   g["world_pos"].ctypes.data, g["depth"].ctypes.data)
+
+
+def crop_arg(crop):
+    return None if crop is None else (C.c_int32 * 4)(*crop)
+
+
+def check(rc, what):
+    if rc != 0:
+        raise RuntimeError(f"oracle {what} failed: {rc}")
+
+
+def initial_temporal(scene, g_cur, g_prev, prev_res, out, uniforms, crop=None, stats=None):
+    s, keep = scene_struct(scene)
+    gc = gbuffer_struct(g_cur)
+    gp = gbuffer_struct(g_prev) if g_prev is not None else None
+    check(oracle().or_initial_temporal(C.byref(s), C.byref(gc), C.byref(gp) if gp else None, P(prev_res), P(out),
+                                       C.byref(uniforms), crop_arg(crop), C.byref(stats) if stats else None),
+          "initial_temporal")
+
+
+def spatial_biased(scene, g, res_in, res_out, uniforms, iteration, crop=None):
+    s, keep = scene_struct(scene)
+    gg = gbuffer_struct(g)
+    check(oracle().or_spatial_biased(C.byref(s), C.byref(gg), P(res_in), P(res_out), C.byref(uniforms),
+                                     C.c_int32(iteration), crop_arg(crop)), "spatial_biased")
+
+
+def spatial_unbiased(scene, g, res_in, res_out, uniforms, neighbors, pass_index=0, crop=None, stats=None):
+    """pass_index p seeds the pass with frame*17 + p (p = 0 is the reference)."""
+    s, keep = scene_struct(scene)
+    gg = gbuffer_struct(g)
+    check(oracle().or_spatial_unbiased(C.byref(s), C.byref(gg), P(res_in), P(res_out), C.byref(uniforms),
+                                       C.c_int32(neighbors), C.c_int32(pass_index), crop_arg(crop),
+                                       C.byref(stats) if stats else None),
+          "spatial_unbiased")
+
+
+def shade(scene, g, res, lighting_uniforms, out_rgba, crop=None):
+    s, keep = scene_struct(scene)
+    gg = gbuffer_struct(g)
+    check(oracle().or_shade(C.byref(s), C.byref(gg), P(res), C.byref(lighting_uniforms), P(out_rgba),
+                            crop_arg(crop)), "shade")
+
+
+def brute_force(scene, g, camera_pos3, crop=None):
+    s, keep = scene_struct(scene)
+    gg = gbuffer_struct(g)
+    h, w = g["depth"].shape
+    cw, ch = (w, h) if crop is None else (crop[2], crop[3])
+    out = np.zeros((ch, cw, 3), np.float64)
+    cam = np.asarray(camera_pos3, np.float32)
+    check(oracle().or_brute_force_fp64(C.byref(s), C.byref(gg), P(cam), P(out), crop_arg(crop)), "brute_force")
+    return out

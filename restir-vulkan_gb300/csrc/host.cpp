@@ -1,0 +1,348 @@
+// host.cpp -- host-side preprocessing of the ReSTIR path: the binned-SAH AABB
+// tree in the reference's node layout, the Vose alias table, scene-buffer
+// repacking for the GPU and the CPU primary-ray G-buffer.
+//
+// Built with -ffp-contract=off so float arithmetic rounds after every
+// operation, as the reference's host build does on x86-64.
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <deque>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "host_internal.h"
+#include "rg_gbuffer.cuh"
+
+namespace {
+
+struct V3 { float x, y, z; };
+inline V3 v3(float x, float y, float z) { V3 r; r.x = x; r.y = y; r.z = z; return r; }
+// nvmath's nv_min / nv_max: (a < b) ? a : b and (a > b) ? a : b per component.
+inline float nvmin(float a, float b) { return (a < b) ? a : b; }
+inline float nvmax(float a, float b) { return (a > b) ? a : b; }
+inline V3 vmin(V3 a, V3 b) { return v3(nvmin(a.x, b.x), nvmin(a.y, b.y), nvmin(a.z, b.z)); }
+inline V3 vmax(V3 a, V3 b) { return v3(nvmax(a.x, b.x), nvmax(a.y, b.y), nvmax(a.z, b.z)); }
+inline float comp(V3 a, int d) { return d == 0 ? a.x : (d == 1 ? a.y : a.z); }
+
+// surfaceAreaHeuristic, aabbTreeBuilder.cpp:16-19
+inline float surface_area(V3 mn, V3 mx) {
+    const V3 s = v3(mx.x - mn.x, mx.y - mn.y, mx.z - mn.z);
+    return s.x * s.y + s.x * s.z + s.y * s.z;
+}
+
+struct Leaf {
+    V3 centroid, bmin, bmax;
+    int32_t geom;
+    size_t bucket;
+};
+struct Bucket {
+    V3 bmin = v3(FLT_MAX, FLT_MAX, FLT_MAX);
+    V3 bmax = v3(-FLT_MAX, -FLT_MAX, -FLT_MAX);
+    size_t count = 0;
+    float heuristic() const { return (float)count * surface_area(bmin, bmax); }
+    static Bucket merge(Bucket l, const Bucket &r) {
+        l.count += r.count;
+        l.bmin = vmin(l.bmin, r.bmin);
+        l.bmax = vmax(l.bmax, r.bmax);
+        return l;
+    }
+};
+struct Step {
+    int32_t *parent;
+    size_t beg, end;
+};
+
+inline void set_box(float *dst4, V3 v) { dst4[0] = v.x; dst4[1] = v.y; dst4[2] = v.z; dst4[3] = 1.0f; }
+
+}  // namespace
+
+// Binned SAH over 12 centroid buckets on the widest centroid axis, BFS node
+// allocation, 2-wide nodes holding both child boxes, leaves as ~triangle.
+// Follows the reference's AabbTree::build (src/aabbTreeBuilder.cpp:52-214)
+// operation for operation so the emitted buffers are byte-identical to the
+// reference's.  Inputs the reference leaves undefined (a range whose
+// centroids all coincide, or with zero surface area) take the median split
+// and are reported through *ref_undefined.
+int host_build_bvh(const float *xyz, int32_t n, rg_aabb_tree_node *out_nodes, rg_triangle *out_tris,
+                   int *ref_undefined) {
+    constexpr size_t kBuckets = 12;
+    if (n < 2) return RG_ERR_INVALID_ARGUMENT;
+    if (ref_undefined) *ref_undefined = 0;
+    std::vector<Leaf> leaves((size_t)n);
+    for (int32_t i = 0; i < n; ++i) {
+        // the reference transforms each vertex by the node's world matrix
+        // (identity here): x*1 + y*0 + z*0 + 0 turns -0 into +0.
+        V3 p[3];
+        for (int k = 0; k < 3; ++k)
+            p[k] = v3(xyz[9 * (size_t)i + 3 * k] + 0.0f, xyz[9 * (size_t)i + 3 * k + 1] + 0.0f,
+                      xyz[9 * (size_t)i + 3 * k + 2] + 0.0f);
+        rg_triangle &t = out_tris[i];
+        set_box(t.p1, p[0]);
+        set_box(t.p2, p[1]);
+        set_box(t.p3, p[2]);
+        Leaf &l = leaves[(size_t)i];
+        l.bmin = l.bmax = p[0];
+        l.bmin = vmin(l.bmin, p[1]);
+        l.bmax = vmax(l.bmax, p[1]);
+        l.bmin = vmin(l.bmin, p[2]);
+        l.bmax = vmax(l.bmax, p[2]);
+        l.geom = i;
+        l.centroid = v3(0.5f * (l.bmin.x + l.bmax.x), 0.5f * (l.bmin.y + l.bmax.y), 0.5f * (l.bmin.z + l.bmax.z));
+        l.bucket = 0;
+    }
+    memset(out_nodes, 0, sizeof(rg_aabb_tree_node) * (size_t)(n - 1));
+    int32_t alloc = 0;
+    int32_t dummy_root = -1;
+    std::deque<Step> q;
+    q.push_back(Step{&dummy_root, 0, (size_t)n});
+    while (!q.empty()) {
+        const Step step = q.front();
+        q.pop_front();
+        const size_t cnt = step.end - step.beg;
+        if (cnt == 1) {
+            *step.parent = ~leaves[step.beg].geom;
+            continue;
+        }
+        if (cnt == 2) {
+            const Leaf &l = leaves[step.beg], &r = leaves[step.beg + 1];
+            const int32_t ni = alloc++;
+            *step.parent = ni;
+            rg_aabb_tree_node &nd = out_nodes[ni];
+            nd.left_child = ~l.geom;
+            nd.right_child = ~r.geom;
+            set_box(nd.left_aabb_min, l.bmin);
+            set_box(nd.left_aabb_max, l.bmax);
+            set_box(nd.right_aabb_min, r.bmin);
+            set_box(nd.right_aabb_max, r.bmax);
+            continue;
+        }
+        V3 cmin = leaves[step.beg].centroid, cmax = cmin;
+        V3 amin = leaves[step.beg].bmin, amax = leaves[step.beg].bmax;
+        for (size_t i = step.beg + 1; i < step.end; ++i) {
+            const Leaf &c = leaves[i];
+            cmin = vmin(cmin, c.centroid);
+            cmax = vmax(cmax, c.centroid);
+            amin = vmin(amin, c.bmin);
+            amax = vmax(amax, c.bmax);
+        }
+        const float outer = surface_area(amin, amax);
+        const V3 span = v3(cmax.x - cmin.x, cmax.y - cmin.y, cmax.z - cmin.z);
+        int dim = span.x > span.y ? 0 : 1;
+        if (span.z > comp(span, dim)) dim = 2;
+        const float range = comp(span, dim) / (float)kBuckets;
+        const bool undefined = !(range > 0.0f) || !(outer > 0.0f);
+        Bucket buckets[kBuckets];
+        for (size_t i = step.beg; i < step.end; ++i) {
+            Leaf &c = leaves[i];
+            float u = undefined ? 0.5f : (comp(c.centroid, dim) - comp(cmin, dim)) / range;
+            u = (u < 0.5f) ? 0.5f : u;
+            u = (u > (float)kBuckets - 0.5f) ? (float)kBuckets - 0.5f : u;
+            c.bucket = (size_t)u;
+            Bucket &b = buckets[c.bucket];
+            b.bmin = vmin(b.bmin, c.bmin);
+            b.bmax = vmax(b.bmax, c.bmax);
+            ++b.count;
+        }
+        Bucket cache[kBuckets - 1];
+        {
+            Bucket cur = buckets[kBuckets - 1];
+            for (size_t i = kBuckets - 1; i > 0;) {
+                cache[--i] = cur;
+                cur = Bucket::merge(cur, buckets[i]);
+            }
+        }
+        size_t opt = 0;
+        V3 lmin = v3(0, 0, 0), lmax = lmin, rmin = lmin, rmax = lmin;
+        bool found = false;
+        {
+            float best = FLT_MAX;
+            Bucket left;
+            for (size_t sp = 0; sp < kBuckets - 1; ++sp) {
+                left = Bucket::merge(left, buckets[sp]);
+                const Bucket &right = cache[sp];
+                const float h = 0.125f + (left.heuristic() + right.heuristic()) / outer;
+                if (h < best) {
+                    best = h;
+                    opt = sp;
+                    lmin = left.bmin; lmax = left.bmax;
+                    rmin = right.bmin; rmax = right.bmax;
+                    found = true;
+                }
+            }
+        }
+        size_t pivot = step.beg;
+        for (size_t i = step.beg; i < step.end; ++i)
+            if (leaves[i].bucket <= opt) std::swap(leaves[i], leaves[pivot++]);
+        if (pivot == step.beg || pivot == step.end || !found) {
+            if (!found && ref_undefined) *ref_undefined = 1;
+            pivot = (step.beg + step.end) / 2;
+            lmin = leaves[step.beg].bmin;
+            lmax = leaves[step.beg].bmax;
+            for (size_t i = step.beg + 1; i < pivot; ++i) {
+                lmin = vmin(lmin, leaves[i].bmin);
+                lmax = vmax(lmax, leaves[i].bmax);
+            }
+            rmin = leaves[pivot].bmin;
+            rmax = leaves[pivot].bmax;
+            for (size_t i = pivot; i < step.end; ++i) {
+                rmin = vmin(rmin, leaves[i].bmin);
+                rmax = vmax(rmax, leaves[i].bmax);
+            }
+        }
+        if (undefined && ref_undefined) *ref_undefined = 1;
+        const int32_t ni = alloc++;
+        *step.parent = ni;
+        rg_aabb_tree_node &nd = out_nodes[ni];
+        set_box(nd.left_aabb_min, lmin);
+        set_box(nd.left_aabb_max, lmax);
+        set_box(nd.right_aabb_min, rmin);
+        set_box(nd.right_aabb_max, rmax);
+        q.push_back(Step{&nd.left_child, step.beg, pivot});
+        q.push_back(Step{&nd.right_child, pivot, step.end});
+    }
+    return alloc;
+}
+
+// Checks that the buffers form one tree rooted at node 0 in which every node
+// and every triangle is reached exactly once, and returns its depth (root = 1)
+// or a negative error.  Traversal relies on this to bound its stack and loop.
+int host_validate_tree(const rg_aabb_tree_node *nodes, int32_t n_nodes, int32_t n_tris) {
+    if (n_nodes <= 0) return n_tris <= 1 ? 0 : RG_ERR_INVALID_ARGUMENT;
+    std::vector<uint8_t> seen_node((size_t)n_nodes, 0), seen_tri((size_t)n_tris, 0);
+    std::vector<std::pair<int32_t, int>> st;
+    st.push_back({0, 1});
+    seen_node[0] = 1;
+    int depth = 0;
+    int32_t nodes_seen = 1, tris_seen = 0;
+    while (!st.empty()) {
+        auto [ni, d] = st.back();
+        st.pop_back();
+        depth = std::max(depth, d);
+        const int32_t ch[2] = {nodes[ni].left_child, nodes[ni].right_child};
+        for (int k = 0; k < 2; ++k) {
+            const int32_t c = ch[k];
+            if (c >= 0) {
+                if (c >= n_nodes || seen_node[(size_t)c]) return RG_ERR_INVALID_ARGUMENT;
+                seen_node[(size_t)c] = 1;
+                ++nodes_seen;
+                st.push_back({c, d + 1});
+            } else {
+                const int32_t t = ~c;
+                if (t >= n_tris || seen_tri[(size_t)t]) return RG_ERR_INVALID_ARGUMENT;
+                seen_tri[(size_t)t] = 1;
+                ++tris_seen;
+            }
+        }
+    }
+    if (nodes_seen != n_nodes || tris_seen != n_tris) return RG_ERR_INVALID_ARGUMENT;
+    return depth;
+}
+
+// Vose's alias method with FIFO work lists in float, as createAliasTable
+// (src/misc.cpp:418-497): point lights weighted by luminance if any, else
+// triangle lights by luminance * area.
+int host_build_alias_table(const rg_point_light *pl, int32_t n_pl, const rg_tri_light *tl, int32_t n_tl,
+                           rg_alias_table_column *out) {
+    const int32_t n = n_pl > 0 ? n_pl : n_tl;
+    if (n <= 0) return RG_ERR_INVALID_ARGUMENT;
+    std::vector<float> p((size_t)n);
+    std::deque<int32_t> big, small;
+    float sum = 0.0f;
+    for (int32_t i = 0; i < n; ++i) {
+        const float v = n_pl > 0 ? pl[i].color_luminance[3] : tl[i].emission_luminance[3] * tl[i].normal_area[3];
+        sum += v;
+        p[(size_t)i] = v;
+    }
+    for (int32_t i = 0; i < n; ++i) {
+        out[i].prob = 0.0f;
+        out[i].alias = -1;
+        out[i].ori_prob = p[(size_t)i] / sum;
+        p[(size_t)i] = (float)n * p[(size_t)i] / sum;
+        if (p[(size_t)i] >= 1.0f) big.push_back(i); else small.push_back(i);
+    }
+    while (!big.empty() && !small.empty()) {
+        const int32_t g = big.front(), l = small.front();
+        big.pop_front();
+        small.pop_front();
+        out[l].prob = p[(size_t)l];
+        out[l].alias = g;
+        p[(size_t)g] = (p[(size_t)g] + p[(size_t)l]) - 1.0f;
+        if (p[(size_t)g] < 1.0f) small.push_back(g); else big.push_back(g);
+    }
+    while (!big.empty()) { const int32_t g = big.front(); big.pop_front(); out[g].prob = 1.0f; out[g].alias = g; }
+    while (!small.empty()) { const int32_t l = small.front(); small.pop_front(); out[l].prob = 1.0f; out[l].alias = l; }
+    for (int32_t i = 0; i < n; ++i) out[i].alias_ori_prob = out[out[i].alias].ori_prob;
+    return RG_OK;
+}
+
+// GNode: a = lmin.xyz lmax.x, b = lmax.yz rmin.xy, c = rmin.z rmax.xyz, d = left right.
+void host_pack_nodes(const rg_aabb_tree_node *src, int32_t n, float *dst16) {
+    for (int32_t i = 0; i < n; ++i) {
+        const rg_aabb_tree_node &s = src[i];
+        float *d = dst16 + 16 * (size_t)i;
+        d[0] = s.left_aabb_min[0]; d[1] = s.left_aabb_min[1]; d[2] = s.left_aabb_min[2];
+        d[3] = s.left_aabb_max[0]; d[4] = s.left_aabb_max[1]; d[5] = s.left_aabb_max[2];
+        d[6] = s.right_aabb_min[0]; d[7] = s.right_aabb_min[1]; d[8] = s.right_aabb_min[2];
+        d[9] = s.right_aabb_max[0]; d[10] = s.right_aabb_max[1]; d[11] = s.right_aabb_max[2];
+        memcpy(&d[12], &s.left_child, 4);
+        memcpy(&d[13], &s.right_child, 4);
+        d[14] = 0.0f;
+        d[15] = 0.0f;
+    }
+}
+
+// GTri: p1.xyz, e1 = p2-p1, e2 = p3-p1 (float subtraction, as the reference's
+// rayTriangleIntersection computes them).
+void host_pack_tris(const rg_triangle *src, int32_t n, float *dst12) {
+    for (int32_t i = 0; i < n; ++i) {
+        const rg_triangle &t = src[i];
+        float *d = dst12 + 12 * (size_t)i;
+        d[0] = t.p1[0]; d[1] = t.p1[1]; d[2] = t.p1[2];
+        d[3] = t.p2[0] - t.p1[0]; d[4] = t.p2[1] - t.p1[1]; d[5] = t.p2[2] - t.p1[2];
+        d[6] = t.p3[0] - t.p1[0]; d[7] = t.p3[1] - t.p1[1]; d[8] = t.p3[2] - t.p1[2];
+        d[9] = d[10] = d[11] = 0.0f;
+    }
+}
+
+// R8G8B8A8_SRGB decode table: IEC 61966-2-1 in double, rounded to float once.
+void srgb_lut_host(float *out256) {
+    for (int i = 0; i < 256; ++i) {
+        const double c = (double)i / 255.0;
+        const double l = c <= 0.04045 ? c / 12.92 : pow((c + 0.055) / 1.055, 2.4);
+        out256[i] = (float)l;
+    }
+}
+
+int host_trace_gbuffer(const float *nodes16, int32_t n_nodes, const float *tris12, int32_t n_tris,
+                       const rg_material *mats, int32_t n_mats, const rg_camera &cam, int32_t w, int32_t h,
+                       uint8_t *albedo, uint16_t *normal, uint16_t *material, float *world_pos, float *depth) {
+    rgm::TraceScene s;
+    s.nodes = nodes16;
+    s.n_nodes = n_nodes;
+    s.tris = tris12;
+    s.n_tris = n_tris;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int32_t y = 0; y < h; ++y) {
+        for (int32_t x = 0; x < w; ++x) {
+            rgm::f3 o, d;
+            rgm::primary_ray(cam, x, y, w, h, o, d);
+            const rgm::Hit hit = rgm::closest_hit(s, o, d);
+            rgm::GTexel g;
+            rgm::shade_texel(s, mats, n_mats, cam, o, d, hit, g);
+            const size_t i = (size_t)y * (size_t)w + (size_t)x;
+            memcpy(albedo + 4 * i, &g.albedo, 4);
+            memcpy(normal + 4 * i, g.normal, 8);
+            memcpy(material + 2 * i, &g.material, 4);
+            memcpy(world_pos + 4 * i, g.wpos, 16);
+            depth[i] = g.depth;
+        }
+    }
+    return RG_OK;
+}

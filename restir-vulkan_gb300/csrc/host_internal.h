@@ -1,0 +1,17 @@
+// host_internal.h -- host-side preprocessing shared by the C ABI (host.cpp).
+#pragma once
+#include <stdint.h>
+
+#include "../../include/restir_gb300.h"
+
+int host_build_bvh(const float *xyz, int32_t n, rg_aabb_tree_node *out_nodes, rg_triangle *out_tris,
+                   int *ref_undefined);
+int host_validate_tree(const rg_aabb_tree_node *nodes, int32_t n_nodes, int32_t n_tris);
+int host_build_alias_table(const rg_point_light *pl, int32_t n_pl, const rg_tri_light *tl, int32_t n_tl,
+                           rg_alias_table_column *out);
+void host_pack_nodes(const rg_aabb_tree_node *src, int32_t n, float *dst16);
+void host_pack_tris(const rg_triangle *src, int32_t n, float *dst12);
+void srgb_lut_host(float *out256);
+int host_trace_gbuffer(const float *nodes16, int32_t n_nodes, const float *tris12, int32_t n_tris,
+                       const rg_material *mats, int32_t n_mats, const rg_camera &cam, int32_t w, int32_t h,
+                       uint8_t *albedo, uint16_t *normal, uint16_t *material, float *world_pos, float *depth);

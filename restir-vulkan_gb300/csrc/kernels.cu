@@ -1,0 +1,545 @@
+// kernels.cu -- sm_103a kernels of the ReSTIR direct-lighting passes.
+//
+// One thread per pixel for the reservoir passes; shadow segments are traced
+// with an any-hit walk of the reference's 2-wide AABB tree.  Any-hit is an OR
+// over every triangle whose whole box path passes the slab test, so the walk
+// may visit nodes in any order and test a leaf as soon as it is reached: the
+// visibility bit equals that of the reference's batched stack walk
+// (src/shaders/include/softwareRaytracing.glsl:42-85) whenever the latter
+// does not overflow its 32-entry stack.
+//
+// Compiled with -fmad=false and IEEE div/sqrt: see rg_math.cuh.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "rg_internal.h"
+#include "rg_math.cuh"
+
+using namespace rgm;
+
+__device__ float g_srgb_lut[256];
+
+cudaError_t upload_srgb_lut(const float *lut256) {
+    return cudaMemcpyToSymbol(g_srgb_lut, lut256, 256 * sizeof(float));
+}
+
+namespace {
+
+constexpr int kStack = RG_MAX_TREE_DEPTH + 1;
+
+struct Texel {
+    f3 albedo;
+    float albedo_a;
+    f3 normal;
+    float roughness, metallic;
+    f3 wpos;
+};
+
+__device__ __forceinline__ f3 load_albedo(const GBufView &g, size_t i, float *alpha) {
+    const uint32_t a = __ldg(g.albedo + i);
+    if (alpha) *alpha = (float)(a >> 24) / 255.0f;
+    return mk(__ldg(&g_srgb_lut[a & 0xffu]), __ldg(&g_srgb_lut[(a >> 8) & 0xffu]), __ldg(&g_srgb_lut[(a >> 16) & 0xffu]));
+}
+__device__ __forceinline__ f3 load_normal(const GBufView &g, size_t i) {
+    const uint2 n = __ldg(g.normal + i);
+    return mk(half_bits_to_float((uint16_t)(n.x & 0xffffu)), half_bits_to_float((uint16_t)(n.x >> 16)),
+              half_bits_to_float((uint16_t)(n.y & 0xffffu)));
+}
+__device__ __forceinline__ void load_material(const GBufView &g, size_t i, float &rough, float &metal) {
+    const uint32_t m = __ldg(g.material + i);
+    rough = (float)(m & 0xffffu) / 65535.0f;
+    metal = (float)(m >> 16) / 65535.0f;
+}
+__device__ __forceinline__ f3 load_wpos(const GBufView &g, size_t i) {
+    const float4 p = __ldg(g.wpos + i);
+    return mk(p.x, p.y, p.z);
+}
+__device__ __forceinline__ void load_texel(const GBufView &g, size_t i, Texel &t) {
+    t.albedo = load_albedo(g, i, &t.albedo_a);
+    t.normal = load_normal(g, i);
+    load_material(g, i, t.roughness, t.metallic);
+    t.wpos = load_wpos(g, i);
+}
+
+// ---------------------------------------------------------------- reservoirs
+struct Res {
+    float4 pos_lum;
+    float4 nrm;
+    int32_t idx;
+    float p_hat, sum_w, w;
+    uint32_t m;
+};
+__device__ __forceinline__ Res load_res(const rg_reservoir *base, size_t i) {
+    const float4 *p = reinterpret_cast<const float4 *>(base + i);
+    Res r;
+    r.pos_lum = __ldg(p);
+    r.nrm = __ldg(p + 1);
+    const float4 c = __ldg(p + 2);
+    const float4 d = __ldg(p + 3);
+    r.idx = __float_as_int(c.x);
+    r.p_hat = c.y;
+    r.sum_w = c.z;
+    r.w = c.w;
+    r.m = __float_as_uint(d.x);
+    return r;
+}
+__device__ __forceinline__ void store_res(rg_reservoir *base, size_t i, const Res &r) {
+    float4 *p = reinterpret_cast<float4 *>(base + i);
+    p[0] = r.pos_lum;
+    p[1] = r.nrm;
+    p[2] = make_float4(__int_as_float(r.idx), r.p_hat, r.sum_w, r.w);
+    p[3] = make_float4(__uint_as_float(r.m), 0.0f, 0.0f, 0.0f);
+}
+__device__ __forceinline__ Res empty_res() {
+    Res r;
+    r.pos_lum = make_float4(0.f, 0.f, 0.f, 0.f);
+    r.nrm = make_float4(0.f, 0.f, 0.f, 0.f);
+    r.idx = 0;
+    r.p_hat = 0.f;
+    r.sum_w = 0.f;
+    r.w = 0.f;
+    r.m = 0u;
+    return r;
+}
+// reservoir.glsl:6-26
+__device__ __forceinline__ void update_res(Res &r, float weight, float4 pos_lum, float4 nrm, int32_t idx, float p_hat,
+                                           float w, Pcg &rng) {
+    r.sum_w += weight;
+    const float replace = weight / r.sum_w;
+    if (rand_float(rng) < replace) {
+        r.pos_lum = pos_lum;
+        r.nrm = nrm;
+        r.idx = idx;
+        r.p_hat = p_hat;
+        r.w = w;
+    }
+}
+// reservoir.glsl:28-42
+__device__ __forceinline__ void add_sample(Res &r, float4 pos_lum, float4 nrm, int32_t idx, float p_hat, float sample_p,
+                                           Pcg &rng) {
+    const float weight = p_hat / sample_p;
+    r.m += 1u;
+    const float w = (r.sum_w + weight) / ((float)r.m * p_hat);
+    update_res(r, weight, pos_lum, nrm, idx, p_hat, w, rng);
+}
+// reservoir.glsl:44-64
+__device__ __forceinline__ void combine_res(Res &self, const Res &other, float p_hat, Pcg &rng) {
+    self.m += other.m;
+    const float weight = p_hat * other.w * (float)other.m;
+    if (weight > 0.0f) update_res(self, weight, other.pos_lum, other.nrm, other.idx, p_hat, other.w, rng);
+    if (self.w > 0.0f) self.w = self.sum_w / ((float)self.m * self.p_hat);
+}
+
+__device__ __forceinline__ f3 xyz(float4 v) { return mk(v.x, v.y, v.z); }
+
+// ---------------------------------------------------------------- any-hit traversal
+__device__ __forceinline__ bool tri_hit(const DevScene &s, int t, f3 o, f3 d) {
+    const GTri *tp = s.tris + t;
+    const float4 a = __ldg(&tp->a), b = __ldg(&tp->b), c = __ldg(&tp->c);
+    return ray_tri(mk(a.x, a.y, a.z), mk(a.w, b.x, b.y), mk(b.z, b.w, c.x), o, d);
+}
+
+// true when the segment o..o+d hits a triangle.  err is set if the walk
+// exceeds one visit per node (only possible for a malformed tree).
+__device__ bool trace_any(const DevScene &s, f3 o, f3 d, bool &err) {
+    if (s.n_nodes <= 0) return false;
+    int stack[kStack];
+    int top = 0;
+    int node = 0;
+    int visits = 0;
+    while (true) {
+        if (++visits > s.n_nodes) { err = true; return false; }
+        const GNode *np = s.nodes + node;
+        const float4 a = __ldg(&np->a), b = __ldg(&np->b), c = __ldg(&np->c);
+        const int4 ch = __ldg(&np->d);
+        const bool hl = ray_aabb(o, d, mk(a.x, a.y, a.z), mk(a.w, b.x, b.y));
+        const bool hr = ray_aabb(o, d, mk(b.z, b.w, c.x), mk(c.y, c.z, c.w));
+        int next = -1;
+        if (hl) {
+            if (ch.x < 0) { if (tri_hit(s, ~ch.x, o, d)) return true; }
+            else next = ch.x;
+        }
+        if (hr) {
+            if (ch.y < 0) { if (tri_hit(s, ~ch.y, o, d)) return true; }
+            else if (next < 0) next = ch.y;
+            else { if (top >= kStack) { err = true; return false; } stack[top++] = ch.y; }
+        }
+        if (next < 0) {
+            if (top == 0) return false;
+            next = stack[--top];
+        }
+        node = next;
+    }
+}
+
+__device__ __forceinline__ bool shadowed(const DevScene &s, f3 p1, f3 p2, bool &err) {
+    f3 o, d;
+    shadow_segment(p1, p2, o, d);
+    return trace_any(s, o, d, err);
+}
+
+__device__ __forceinline__ void count_rays(const DevScene &s, unsigned rays, bool err) {
+    const unsigned mask = __activemask();
+    const unsigned total = __reduce_add_sync(mask, rays);
+    const unsigned errs = __popc(__ballot_sync(mask, err));
+    if ((threadIdx.x & 31u) == (unsigned)(__ffs(mask) - 1)) {
+        if (total) atomicAdd(&s.counters[0], (unsigned long long)total);
+        if (errs) atomicAdd(&s.counters[1], (unsigned long long)errs);
+    }
+}
+
+// ---------------------------------------------------------------- RIS + visibility + temporal (restirOmni.glsl:86-212)
+struct InitialParams {
+    DevScene s;
+    GBufView cur, prev;
+    bool has_prev;
+    const rg_reservoir *prev_res;
+    rg_reservoir *out;
+    rg_restir_uniforms u;
+};
+
+__global__ void __launch_bounds__(128) k_initial_temporal(const InitialParams p) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int W = (int)p.u.screen_size[0], H = (int)p.u.screen_size[1];
+    if (x >= W || y >= H) return;
+    const size_t i = (size_t)y * (size_t)W + (size_t)x;
+    const DevScene &s = p.s;
+    Texel t;
+    load_texel(p.cur, i, t);
+    const float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
+    const f3 cam = mk(p.u.camera_pos[0], p.u.camera_pos[1], p.u.camera_pos[2]);
+    Res r = empty_res();
+    Pcg rng = pcg_seed((uint64_t)p.u.frame, (uint64_t)((uint32_t)y * 10007u + (uint32_t)x));
+    const bool zero_normal = !(dot(t.normal, t.normal) != 0.0f);
+    if (!zero_normal) {
+        const f3 wo = view_dir(cam, t.wpos);
+        const int count = s.n_alias;
+        for (int c = 0; (uint32_t)c < p.u.initial_light_sample_count; ++c) {
+            const float r1 = rand_float(rng), r2 = rand_float(rng);
+            const int col = imin((int)((float)count * r1), count - 1);
+            float4 pos_lum, nrm;
+            float prob;
+            int32_t lidx;
+            if (s.n_point_lights != 0) {
+                const AliasLight *al = s.alias + col;
+                const float4 cc = __ldg(&al->col);
+                if (cc.x > r2) { pos_lum = __ldg(&al->own_pos); prob = cc.z; lidx = col; }
+                else { pos_lum = __ldg(&al->alias_pos); prob = cc.w; lidx = __float_as_int(cc.y); }
+                nrm = make_float4(0.f, 0.f, 0.f, 0.f);
+            } else {
+                const rg_alias_table_column cc = s.tri_alias[col];
+                int sel;
+                if (cc.prob > r2) { sel = col; prob = cc.ori_prob; }
+                else { sel = cc.alias; prob = cc.alias_ori_prob; }
+                const rg_tri_light &L = s.tri_lights[sel];
+                const float ra = rand_float(rng), rb = rand_float(rng);
+                const float sa = sqrtf(ra);  // pickPointOnTriangle, restirOmni.glsl:68-71
+                const f3 lpos = (scale(1.0f - sa, mk(L.p1[0], L.p1[1], L.p1[2])) +
+                                 scale(sa * (1.0f - rb), mk(L.p2[0], L.p2[1], L.p2[2]))) +
+                                scale(rb * sa, mk(L.p3[0], L.p3[1], L.p3[2]));
+                const f3 wi = normalize(t.wpos - lpos);
+                const f3 nn = mk(L.normal_area[0], L.normal_area[1], L.normal_area[2]);
+                prob /= fabsf(dot(wi, nn)) * L.normal_area[3];
+                pos_lum = make_float4(lpos.x, lpos.y, lpos.z, L.emission_luminance[3]);
+                nrm = make_float4(nn.x, nn.y, nn.z, 1.0f);
+                lidx = -1 - sel;
+            }
+            const float ph = eval_phat_wo(t.wpos, xyz(pos_lum), wo, t.normal, xyz(nrm), nrm.w > 0.5f, albedo_lum,
+                                          pos_lum.w, t.roughness, t.metallic);
+            add_sample(r, pos_lum, nrm, lidx, ph, prob, rng);
+        }
+    }
+    unsigned rays = 0;
+    bool err = false;
+    if ((p.u.flags & RG_FLAG_VISIBILITY_REUSE) && !zero_normal) {
+        ++rays;
+        if (shadowed(s, t.wpos, xyz(r.pos_lum), err)) {
+            r.w = 0.0f;
+            r.sum_w = 0.0f;
+        }
+    }
+    if ((p.u.flags & RG_FLAG_TEMPORAL_REUSE) && p.has_prev) {
+        const float *m = p.u.prev_frame_projection_view;
+        float px = ((m[0] * t.wpos.x + m[4] * t.wpos.y) + m[8] * t.wpos.z) + m[12] * 1.0f;
+        float py = ((m[1] * t.wpos.x + m[5] * t.wpos.y) + m[9] * t.wpos.z) + m[13] * 1.0f;
+        const float pw = ((m[3] * t.wpos.x + m[7] * t.wpos.y) + m[11] * t.wpos.z) + m[15] * 1.0f;
+        px /= pw;
+        py /= pw;
+        px = (px + 1.0f) * 0.5f * (float)p.u.screen_size[0];
+        py = (py + 1.0f) * 0.5f * (float)p.u.screen_size[1];
+        if (px > 0.0f && py > 0.0f && px < (float)p.u.screen_size[0] && py < (float)p.u.screen_size[1]) {
+            const int fx = (int)px, fy = (int)py;
+            const size_t pi = (size_t)fy * (size_t)W + (size_t)fx;
+            const f3 dp = t.wpos - load_wpos(p.prev, pi);
+            if (dot(dp, dp) < 0.01f) {
+                const f3 da = t.albedo - load_albedo(p.prev, pi, nullptr);
+                if (dot(da, da) < 0.01f) {
+                    if (dot(t.normal, load_normal(p.prev, pi)) > 0.5f) {
+                        Res pr = load_res(p.prev_res, pi);
+                        const uint32_t cap = p.u.temporal_sample_count_multiplier * r.m;
+                        pr.m = pr.m < cap ? pr.m : cap;
+                        const float ph = eval_phat_wo(t.wpos, xyz(pr.pos_lum), view_dir(cam, t.wpos), t.normal,
+                                                      xyz(pr.nrm), pr.nrm.w > 0.5f, albedo_lum, pr.pos_lum.w,
+                                                      t.roughness, t.metallic);
+                        combine_res(r, pr, ph, rng);
+                    }
+                }
+            }
+        }
+    }
+    store_res(p.out, i, r);
+    count_rays(s, rays, err);
+}
+
+// ---------------------------------------------------------------- biased spatial (spatialReuse.comp:30-86)
+struct SpatialParams {
+    DevScene s;
+    GBufView g;
+    const rg_reservoir *in;
+    rg_reservoir *out;
+    rg_restir_uniforms u;
+    int iter;           // biased: push-constant iter; unbiased: pass index
+    int num_neighbors;  // unbiased: NUM_NEIGHBORS
+    float cos_thr;
+};
+
+__global__ void __launch_bounds__(128) k_spatial_biased(const SpatialParams p) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int W = (int)p.u.screen_size[0], H = (int)p.u.screen_size[1];
+    if (x >= W || y >= H) return;
+    const size_t i = (size_t)y * (size_t)W + (size_t)x;
+    Texel t;
+    load_texel(p.g, i, t);
+    const float depth = __ldg(p.g.depth + i);
+    const float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
+    const f3 cam = mk(p.u.camera_pos[0], p.u.camera_pos[1], p.u.camera_pos[2]);
+    const f3 wo = view_dir(cam, t.wpos);
+    Res r = load_res(p.in, i);
+    Pcg rng = pcg_seed((uint64_t)(p.u.frame * 31u + (uint32_t)p.iter), (uint64_t)((uint32_t)y * 10007u + (uint32_t)x));
+    for (uint32_t k = 0; k < p.u.spatial_neighbors; ++k) {
+        const float angle = rand_float(rng) * 2.0f * kPi;
+        const float radius = sqrtf(rand_float(rng)) * p.u.spatial_radius;
+        float sn, cs;
+        sincos_cw(angle, sn, cs);
+        const int nx = iclamp(x + (int)floorf(cs * radius), 0, W - 1);
+        const int ny = iclamp(y + (int)floorf(sn * radius), 0, H - 1);
+        const size_t ni = (size_t)ny * (size_t)W + (size_t)nx;
+        const float nd = __ldg(p.g.depth + ni);
+        const f3 nn = load_normal(p.g, ni);
+        if (fabsf(nd - depth) > p.u.spatial_pos_threshold * fabsf(depth) || dot(nn, t.normal) < p.cos_thr) continue;
+        const Res rr = load_res(p.in, ni);
+        const float ph = eval_phat_wo(t.wpos, xyz(rr.pos_lum), wo, t.normal, xyz(rr.nrm), rr.nrm.w > 0.5f, albedo_lum,
+                                      rr.pos_lum.w, t.roughness, t.metallic);
+        combine_res(r, rr, ph, rng);
+    }
+    store_res(p.out, i, r);
+}
+
+// ---------------------------------------------------------------- unbiased spatial (unbiasedReuse.glsl:50-185)
+constexpr int kMaxNeighbors = 16;
+
+__global__ void __launch_bounds__(128) k_spatial_unbiased(const SpatialParams p) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int W = (int)p.u.screen_size[0], H = (int)p.u.screen_size[1];
+    if (x >= W || y >= H) return;
+    const DevScene &s = p.s;
+    const size_t i = (size_t)y * (size_t)W + (size_t)x;
+    Texel t;
+    load_texel(p.g, i, t);
+    const float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
+    const f3 cam = mk(p.u.camera_pos[0], p.u.camera_pos[1], p.u.camera_pos[2]);
+    const f3 wo = view_dir(cam, t.wpos);
+    Res r = load_res(p.in, i);
+    Pcg rng = pcg_seed((uint64_t)(p.u.frame * 17u + (uint32_t)p.iter), (uint64_t)((uint32_t)y * 10007u + (uint32_t)x));
+    const int K = p.num_neighbors;
+    uint32_t nidx[kMaxNeighbors];
+    uint32_t nm[kMaxNeighbors];
+    const uint32_t orig_m = r.m;
+    for (int k = 0; k < K; ++k) {
+        const float angle = rand_float(rng) * 2.0f * kPi;
+        const float radius = sqrtf(rand_float(rng)) * p.u.spatial_radius;
+        float sn, cs;
+        sincos_cw(angle, sn, cs);
+        const int nx = iclamp(x + (int)roundf(cs * radius), 0, (int)(p.u.screen_size[0] - 1u));
+        const int ny = iclamp(y + (int)roundf(sn * radius), 0, (int)(p.u.screen_size[1] - 1u));
+        const size_t ni = (size_t)ny * (size_t)W + (size_t)nx;
+        const Res rr = load_res(p.in, ni);
+        nidx[k] = (uint32_t)ni;
+        nm[k] = rr.m;
+        r.m += rr.m;
+        const float ph = eval_phat_wo(t.wpos, xyz(rr.pos_lum), wo, t.normal, xyz(rr.nrm), rr.nrm.w > 0.5f, albedo_lum,
+                                      rr.pos_lum.w, t.roughness, t.metallic);
+        const float weight = ph * rr.w * (float)rr.m;
+        if (weight > 0.0f) update_res(r, weight, rr.pos_lum, rr.nrm, rr.idx, ph, rr.w, rng);
+    }
+    const f3 lpos = xyz(r.pos_lum);
+    const bool vis = (p.u.flags & RG_FLAG_VISIBILITY_REUSE) != 0;
+    uint32_t ns = orig_m;
+    unsigned rays = 0;
+    bool err = false;
+    for (int k = 0; k < K; ++k) {
+        const f3 nw = load_wpos(p.g, nidx[k]);
+        const f3 nn = load_normal(p.g, nidx[k]);
+        if (dot(lpos - nw, nn) < 0.0f) continue;
+        if (vis) {
+            ++rays;
+            if (shadowed(s, nw, lpos, err)) continue;
+        }
+        ns += nm[k];
+    }
+    if (vis) {
+        ++rays;
+        if (shadowed(s, t.wpos, lpos, err)) ns = 0;
+    }
+    if (ns > 0) {
+        r.w = r.sum_w / ((float)ns * r.p_hat);
+    } else {
+        r.w = 0.0f;
+        r.sum_w = 0.0f;
+    }
+    store_res(p.out, i, r);
+    count_rays(s, rays, err);
+}
+
+// ---------------------------------------------------------------- shading (lighting.frag:43-71,103)
+struct ShadeParams {
+    DevScene s;
+    GBufView g;
+    const rg_reservoir *res;
+    float4 *out;
+    rg_lighting_uniforms u;
+};
+
+__global__ void __launch_bounds__(128) k_shade(const ShadeParams p) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int W = (int)p.u.buffer_size[0], H = (int)p.u.buffer_size[1];
+    if (x >= W || y >= H) return;
+    const size_t i = (size_t)y * (size_t)W + (size_t)x;
+    Texel t;
+    load_texel(p.g, i, t);
+    const Res r = load_res(p.res, i);
+    f3 emission = mk(0.f, 0.f, 0.f);
+    if (r.idx < 0) {
+        const int k = -1 - r.idx;
+        if (k < p.s.n_tri_lights) {
+            const rg_tri_light &L = p.s.tri_lights[k];
+            emission = mk(L.emission_luminance[0], L.emission_luminance[1], L.emission_luminance[2]);
+        }
+    } else if (r.idx < p.s.n_point_lights) {
+        const float4 c = __ldg(p.s.pl_color + r.idx);
+        emission = mk(c.x, c.y, c.z);
+    }
+    const f3 cam = mk(p.u.camera_pos[0], p.u.camera_pos[1], p.u.camera_pos[2]);
+    const f3 ph = eval_phat_full(t.wpos, xyz(r.pos_lum), cam, t.normal, xyz(r.nrm), r.nrm.w > 0.5f, t.albedo, emission,
+                                 t.roughness, t.metallic);
+    f3 col = mk(0.0f + ph.x * r.w, 0.0f + ph.y * r.w, 0.0f + ph.z * r.w);
+    col = divs(col, 1.0f);  // RESERVOIR_SIZE
+    if (t.albedo_a > 0.5f) col = t.albedo;
+    if (p.u.gamma != 1.0f) {
+        const float ig = 1.0f / p.u.gamma;
+        col = mk(powf(col.x, ig), powf(col.y, ig), powf(col.z, ig));
+    }
+    p.out[i] = make_float4(col.x, col.y, col.z, 1.0f);
+}
+
+// ---------------------------------------------------------------- visibility batch (testVisibility)
+__global__ void __launch_bounds__(128) k_visibility_batch(const DevScene s, const float4 *p1, const float4 *p2,
+                                                          uint8_t *out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 a = __ldg(p1 + i), b = __ldg(p2 + i);
+    bool err = false;
+    out[i] = shadowed(s, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), err) ? 1 : 0;
+    count_rays(s, 1u, err);
+}
+
+dim3 pixel_grid(int w, int h, dim3 block) {
+    return dim3((unsigned)((w + (int)block.x - 1) / (int)block.x), (unsigned)((h + (int)block.y - 1) / (int)block.y));
+}
+
+}  // namespace
+
+GBufView make_view(const rg_gbuffer *g) {
+    GBufView v;
+    v.w = g->width;
+    v.h = g->height;
+    v.albedo = static_cast<const uint32_t *>(g->albedo);
+    v.normal = static_cast<const uint2 *>(g->normal);
+    v.material = static_cast<const uint32_t *>(g->material);
+    v.wpos = static_cast<const float4 *>(g->world_pos);
+    v.depth = static_cast<const float *>(g->depth);
+    return v;
+}
+
+cudaError_t launch_initial_temporal(const DevScene &s, const GBufView &cur, const GBufView *prev,
+                                    const rg_reservoir *prev_res, rg_reservoir *out, const rg_restir_uniforms &u,
+                                    cudaStream_t st) {
+    InitialParams p;
+    p.s = s;
+    p.cur = cur;
+    p.has_prev = prev != nullptr && prev_res != nullptr;
+    p.prev = prev ? *prev : cur;
+    p.prev_res = prev_res;
+    p.out = out;
+    p.u = u;
+    const dim3 block(32, 4);
+    k_initial_temporal<<<pixel_grid((int)u.screen_size[0], (int)u.screen_size[1], block), block, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spatial_biased(const DevScene &s, const GBufView &g, const rg_reservoir *in, rg_reservoir *out,
+                                  const rg_restir_uniforms &u, int iter, cudaStream_t st) {
+    SpatialParams p;
+    p.s = s;
+    p.g = g;
+    p.in = in;
+    p.out = out;
+    p.u = u;
+    p.iter = iter;
+    p.num_neighbors = 0;
+    p.cos_thr = cos_cw(u.spatial_normal_threshold * kDeg2Rad);
+    const dim3 block(32, 4);
+    k_spatial_biased<<<pixel_grid((int)u.screen_size[0], (int)u.screen_size[1], block), block, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spatial_unbiased(const DevScene &s, const GBufView &g, const rg_reservoir *in, rg_reservoir *out,
+                                    const rg_restir_uniforms &u, int num_neighbors, int pass_index, cudaStream_t st) {
+    if (num_neighbors < 0 || num_neighbors > kMaxNeighbors) return cudaErrorInvalidValue;
+    SpatialParams p;
+    p.s = s;
+    p.g = g;
+    p.in = in;
+    p.out = out;
+    p.u = u;
+    p.iter = pass_index;
+    p.num_neighbors = num_neighbors;
+    p.cos_thr = 0.0f;
+    const dim3 block(32, 4);
+    k_spatial_unbiased<<<pixel_grid((int)u.screen_size[0], (int)u.screen_size[1], block), block, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shade(const DevScene &s, const GBufView &g, const rg_reservoir *res, const rg_lighting_uniforms &u,
+                         float4 *out, cudaStream_t st) {
+    ShadeParams p;
+    p.s = s;
+    p.g = g;
+    p.res = res;
+    p.out = out;
+    p.u = u;
+    const dim3 block(32, 4);
+    k_shade<<<pixel_grid((int)u.buffer_size[0], (int)u.buffer_size[1], block), block, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_visibility_batch(const DevScene &s, const float4 *p1, const float4 *p2, uint8_t *out, int n,
+                                    cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_visibility_batch<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(s, p1, p2, out, n);
+    return cudaGetLastError();
+}

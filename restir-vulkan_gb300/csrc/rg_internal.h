@@ -1,0 +1,79 @@
+// rg_internal.h -- device-side scene layout and kernel launch interface.
+//
+// The reference's buffers are repacked once at upload into layouts a GB300
+// reads with 128-bit loads; the repacking copies values, it never recomputes
+// them, so every test the kernels evaluate sees the reference's floats.
+//   GNode      64 B: both child boxes + child links of one AabbTreeNode
+//              (80 B in the reference: the vec4 w lanes are dropped).
+//   GTri       48 B: p1, e1 = p2-p1, e2 = p3-p1 (the same subtractions the
+//              reference's rayTriangleIntersection performs per test).
+//   AliasLight 48 B: one alias-table column plus the position/luminance of
+//              both lights it can return, so a candidate is one gather.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/restir_gb300.h"
+
+struct GNode {
+    float4 a;  // lmin.x lmin.y lmin.z lmax.x
+    float4 b;  // lmax.y lmax.z rmin.x rmin.y
+    float4 c;  // rmin.z rmax.x rmax.y rmax.z
+    int4 d;    // left right 0 0
+};
+struct GTri {
+    float4 a;  // p1.xyz e1.x
+    float4 b;  // e1.y e1.z e2.x e2.y
+    float4 c;  // e2.z 0 0 0
+};
+struct AliasLight {
+    float4 col;        // prob, alias (int bits), ori_prob, alias_ori_prob
+    float4 own_pos;    // light[column].pos.xyz, luminance
+    float4 alias_pos;  // light[alias].pos.xyz, luminance
+};
+
+struct DevScene {
+    const GNode *nodes;
+    int32_t n_nodes;
+    const GTri *tris;
+    int32_t n_tris;
+    const AliasLight *alias;      // point-light scenes
+    int32_t n_alias;
+    const float4 *pl_color;       // point light color_luminance
+    int32_t n_point_lights;
+    const rg_tri_light *tri_lights;
+    const rg_alias_table_column *tri_alias;  // triangle-light scenes
+    int32_t n_tri_lights;
+    const rg_material *materials;
+    int32_t n_materials;
+    unsigned long long *counters; // [0] rays traced, [1] traversal errors
+};
+
+struct GBufView {
+    int32_t w, h;
+    const uint32_t *albedo;  // RGBA8
+    const uint2 *normal;     // RGBA16F
+    const uint32_t *material;// RG16
+    const float4 *wpos;
+    const float *depth;
+};
+
+GBufView make_view(const rg_gbuffer *g);
+
+// launchers (kernels.cu); return cudaGetLastError()
+cudaError_t launch_initial_temporal(const DevScene &s, const GBufView &cur, const GBufView *prev,
+                                    const rg_reservoir *prev_res, rg_reservoir *out, const rg_restir_uniforms &u,
+                                    cudaStream_t st);
+cudaError_t launch_spatial_biased(const DevScene &s, const GBufView &g, const rg_reservoir *in, rg_reservoir *out,
+                                  const rg_restir_uniforms &u, int iter, cudaStream_t st);
+cudaError_t launch_spatial_unbiased(const DevScene &s, const GBufView &g, const rg_reservoir *in, rg_reservoir *out,
+                                    const rg_restir_uniforms &u, int num_neighbors, int pass_index, cudaStream_t st);
+cudaError_t launch_shade(const DevScene &s, const GBufView &g, const rg_reservoir *res, const rg_lighting_uniforms &u,
+                         float4 *out, cudaStream_t st);
+cudaError_t launch_visibility_batch(const DevScene &s, const float4 *p1, const float4 *p2, uint8_t *out, int n,
+                                    cudaStream_t st);
+cudaError_t launch_trace_gbuffer(const DevScene &s, const rg_camera &cam, const rg_gbuffer_out &out, cudaStream_t st);
+cudaError_t upload_srgb_lut(const float *lut256);
+
+// host helpers (host_bvh.cpp, host_alias.cpp, host_gbuffer.cpp)
+void srgb_lut_host(float *out256);

@@ -1,0 +1,190 @@
+"""Python mirror of the reference's pass interface over the C ABI.
+
+A `Context` owns one rg_context (one GPU).  Its methods are the reference's
+passes (RestirPass, SpatialReusePass, UnbiasedReusePass, LightingPass; see
+src/passes/*.h) taking device buffers; `render_frame` is the reference's
+per-frame command sequence (App::_recordMainCommandBuffers, src/app.h:212-262).
+Device memory is held in torch tensors, used only as allocations; all compute
+runs in librestir_gb300.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, lib
+
+PLANES = {  # name: (dtype, channels)
+    "albedo": (np.uint8, 4),
+    "normal": (np.uint16, 4),
+    "material": (np.uint16, 2),
+    "world_pos": (np.float32, 4),
+    "depth": (np.float32, 1),
+}
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream_handle(stream) -> int | None:
+    if stream is None:
+        torch = _torch()
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+class DeviceGBuffer:
+    """G-buffer planes resident on the GPU (torch tensors)."""
+
+    def __init__(self, width: int, height: int, device="cuda"):
+        torch = _torch()
+        tmap = {np.uint8: torch.uint8, np.uint16: torch.int16, np.float32: torch.float32}
+        self.width, self.height = width, height
+        self.planes = {}
+        for name, (dt, ch) in PLANES.items():
+            shape = (height, width, ch) if ch > 1 else (height, width)
+            self.planes[name] = torch.zeros(shape, dtype=tmap[dt], device=device)
+
+    @classmethod
+    def from_host(cls, g: dict, device="cuda"):
+        h, w = g["depth"].shape
+        d = cls(w, h, device)
+        d.upload(g)
+        return d
+
+    def upload(self, g: dict):
+        torch = _torch()
+        for name, t in self.planes.items():
+            src = np.ascontiguousarray(g[name])
+            if src.dtype == np.uint16:
+                src = src.view(np.int16)
+            t.copy_(torch.from_numpy(src))
+
+    def to_host(self) -> dict:
+        out = {}
+        for name, t in self.planes.items():
+            a = t.cpu().numpy()
+            if a.dtype == np.int16:
+                a = a.view(np.uint16)
+            out[name] = a
+        return out
+
+    def struct(self) -> _lib.GBuffer:
+        p = self.planes
+        return _lib.GBuffer(self.width, self.height, p["albedo"].data_ptr(), p["normal"].data_ptr(),
+                            p["material"].data_ptr(), p["world_pos"].data_ptr(), p["depth"].data_ptr())
+
+    def out_struct(self) -> _lib.GBufferOut:
+        p = self.planes
+        return _lib.GBufferOut(self.width, self.height, p["albedo"].data_ptr(), p["normal"].data_ptr(),
+                               p["material"].data_ptr(), p["world_pos"].data_ptr(), p["depth"].data_ptr())
+
+
+def reservoirs(n: int, device="cuda"):
+    """Zero-filled device reservoir buffer (64 bytes per pixel)."""
+    return _torch().zeros((n, 16), dtype=_torch().int32, device=device)
+
+
+class _DeviceSpan:
+    def __init__(self, ptr: int, nbytes: int):
+        self.__cuda_array_interface__ = {"shape": (nbytes,), "typestr": "|u1", "data": (ptr, False), "version": 3}
+
+
+def device_view(ptr: int, nbytes: int):
+    """A torch uint8 tensor aliasing `nbytes` of device memory at `ptr`
+    (for buffers the library owns, e.g. the frame driver's reservoirs)."""
+    return _torch().as_tensor(_DeviceSpan(ptr, nbytes), device="cuda")
+
+
+def reservoirs_to_numpy(t) -> np.ndarray:
+    return t.cpu().numpy().view(_lib.RESERVOIR_DTYPE).reshape(-1)
+
+
+def reservoirs_from_numpy(a: np.ndarray, device="cuda"):
+    return _torch().from_numpy(np.ascontiguousarray(a).view(np.int32).reshape(-1, 16)).to(device)
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        check(lib().rg_create(device, C.byref(self._h)))
+        self.device = device
+        self.scene = None
+
+    def close(self):
+        if self._h:
+            lib().rg_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload_scene(self, scene):
+        self.scene = scene
+        d = scene.desc()
+        check(lib().rg_upload_scene(self._h, C.byref(d)))
+
+    # ---- passes
+    def initial_temporal(self, cur: DeviceGBuffer, prev: DeviceGBuffer | None, prev_res, out, uniforms, stream=None):
+        cs = cur.struct()
+        ps = prev.struct() if prev is not None else None
+        check(lib().rg_initial_temporal(self._h, C.byref(cs), C.byref(ps) if ps is not None else None,
+                                        _lib.ptr(prev_res), _lib.ptr(out), C.byref(uniforms), _stream_handle(stream)))
+
+    def spatial_biased(self, g: DeviceGBuffer, res_in, res_out, uniforms, iteration: int, stream=None):
+        gs = g.struct()
+        check(lib().rg_spatial_biased(self._h, C.byref(gs), _lib.ptr(res_in), _lib.ptr(res_out), C.byref(uniforms),
+                                      iteration, _stream_handle(stream)))
+
+    def spatial_unbiased(self, g: DeviceGBuffer, res_in, res_out, uniforms, neighbors: int = 3, pass_index: int = 0,
+                         stream=None):
+        gs = g.struct()
+        check(lib().rg_spatial_unbiased(self._h, C.byref(gs), _lib.ptr(res_in), _lib.ptr(res_out),
+                                        C.byref(uniforms), neighbors, pass_index, _stream_handle(stream)))
+
+    def shade(self, g: DeviceGBuffer, res, lighting_uniforms, out_rgba, stream=None):
+        gs = g.struct()
+        check(lib().rg_shade(self._h, C.byref(gs), _lib.ptr(res), C.byref(lighting_uniforms), _lib.ptr(out_rgba),
+                             _stream_handle(stream)))
+
+    def visibility_batch(self, p1, p2, out, stream=None):
+        n = p1.shape[0]
+        check(lib().rg_visibility_batch(self._h, _lib.ptr(p1), _lib.ptr(p2), _lib.ptr(out), n,
+                                        _stream_handle(stream)))
+
+    def trace_gbuffer(self, camera, out: DeviceGBuffer, stream=None):
+        cam = camera.to_c()
+        os_ = out.out_struct()
+        check(lib().rg_trace_gbuffer(self._h, C.byref(cam), C.byref(os_), _stream_handle(stream)))
+
+    def render_frame(self, cur: DeviceGBuffer, prev: DeviceGBuffer | None, slot: int, params, out_rgba=None,
+                     stream=None):
+        cs = cur.struct()
+        ps = (prev if prev is not None else cur).struct()
+        check(lib().rg_render_frame(self._h, C.byref(cs), C.byref(ps), slot, C.byref(params), _lib.ptr(out_rgba),
+                                    _stream_handle(stream)))
+
+    def frame_reservoirs_ptr(self, slot: int) -> int:
+        p = C.c_void_p()
+        check(lib().rg_frame_reservoirs(self._h, slot, C.byref(p)))
+        return p.value
+
+    def render_frame_host(self, g: dict, params, out_rgba: np.ndarray, stream=None):
+        h, w = g["depth"].shape
+        check(lib().rg_render_frame_host(self._h, w, h, _lib.ptr(g["albedo"]), _lib.ptr(g["normal"]),
+                                         _lib.ptr(g["material"]), _lib.ptr(g["world_pos"]), _lib.ptr(g["depth"]),
+                                         C.byref(params), _lib.ptr(out_rgba), _stream_handle(stream)))
+
+    def stats(self, reset: bool = False) -> _lib.Stats:
+        s = _lib.Stats()
+        check(lib().rg_get_stats(self._h, C.byref(s), int(reset)))
+        return s

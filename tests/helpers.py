@@ -1,0 +1,58 @@
+"""Shared helpers for the parity tests (oracle sequences, comparisons)."""
+from __future__ import annotations
+
+import numpy as np
+
+import oracle_binding as ob
+from restir_gb300 import _lib
+
+
+def new_res(n):
+    return np.zeros(n, _lib.RESERVOIR_DTYPE)
+
+
+def res_bits(a: np.ndarray) -> np.ndarray:
+    """Reservoirs as raw 32-bit words without the padding lanes."""
+    return a.view(np.uint32).reshape(-1, 16)[:, :13]
+
+
+def mismatch(a: np.ndarray, b: np.ndarray, mask=None) -> int:
+    x, y = res_bits(a), res_bits(b)
+    if mask is not None:
+        x, y = x[mask], y[mask]
+    return int(np.count_nonzero(np.any(x != y, axis=1)))
+
+
+def crop_mask(w, h, crop):
+    m = np.zeros((h, w), bool)
+    x0, y0, cw, ch = crop
+    m[y0:y0 + ch, x0:x0 + cw] = True
+    return m.reshape(-1)
+
+
+def oracle_frame(scene, frame_index, g_cur, g_prev, prev_res, crop=None):
+    """The reference's pass sequence for one frame on the oracle.  Returns
+    (reservoirs of every stage, image)."""
+    n = scene.width * scene.height
+    u = scene.uniforms(frame_index)
+    stages = []
+    r = new_res(n)
+    ob.initial_temporal(scene, g_cur, g_prev, prev_res, r, u, crop=crop)
+    stages.append(r.copy())
+    if scene.unbiased:
+        for k in range(scene.spatial_passes):
+            o = new_res(n)
+            ob.spatial_unbiased(scene, g_cur, r, o, u, scene.neighbors, k, crop=crop)
+            r = o
+            stages.append(r.copy())
+    else:
+        for j in range(scene.spatial_passes):
+            o = new_res(n)
+            ob.spatial_biased(scene, g_cur, r, o, u, 2 * j, crop=crop)
+            o2 = new_res(n)
+            ob.spatial_biased(scene, g_cur, o, o2, u, 2 * j + 1, crop=crop)
+            r = o2
+            stages.append(r.copy())
+    img = np.zeros((scene.height, scene.width, 4), np.float32)
+    ob.shade(scene, g_cur, r, scene.lighting_uniforms(frame_index), img, crop=crop)
+    return stages, img
