@@ -140,14 +140,15 @@ def cpu_sample(s, gbufs: list, crop_size: int, threads: int | None = None) -> di
         ob.oracle().or_set_threads(threads)
     W, H = s.width, s.height
     n = W * H
-    cs = min(crop_size, W, H)
-    cx, cy = (W - cs) // 2, (H - cs) // 2
+    full = crop_size <= 0 or crop_size >= max(W, H)
+    cw_, ch_ = (W, H) if full else (min(crop_size, W), min(crop_size, H))
+    cx, cy = (W - cw_) // 2, (H - ch_) // 2
     halo = int(s.radius) + 1
     n_sp = s.spatial_passes if s.unbiased else 2 * s.spatial_passes
 
     def region(grow):
         x0, y0 = max(cx - grow, 0), max(cy - grow, 0)
-        x1, y1 = min(cx + cs + grow, W), min(cy + cs + grow, H)
+        x1, y1 = min(cx + cw_ + grow, W), min(cy + ch_ + grow, H)
         return (x0, y0, x1 - x0, y1 - y0)
 
     regions = [region(halo * (n_sp - k)) for k in range(n_sp + 1)]  # [RIS, pass0, ..., pass n-1]
@@ -193,7 +194,9 @@ def cpu_sample(s, gbufs: list, crop_size: int, threads: int | None = None) -> di
     samples = s.samples_per_frame(1)
     return {"value": samples / frame_s, "frame_seconds_estimate": frame_s,
             "measured_seconds": sum(times.values()), "threads": ob.oracle().or_max_threads(),
-            "sample": (f"oracle pass sequence of frame 1 on a {cs}x{cs} crop centred in the {W}x{H} frame "
+            "sample": (f"oracle pass sequence of frame 1 over the whole {W}x{H} frame (frame 0 run first for the "
+                       f"temporal input)" if full else
+                       f"oracle pass sequence of frame 1 on a {cw_}x{ch_} crop centred in the {W}x{H} frame "
                        f"(RIS on the crop grown by {halo * n_sp}px, each spatial pass by {halo}px less), "
                        f"per-pixel cost of each pass scaled to the full frame"),
             "rays_in_sample": rays}
@@ -426,7 +429,7 @@ def main(argv=None):
     ap.add_argument("--width", type=int, default=None)
     ap.add_argument("--height", type=int, default=None)
     ap.add_argument("--frames", type=int, default=None)
-    ap.add_argument("--cpu-crop", type=int, default=192)
+    ap.add_argument("--cpu-crop", type=int, default=0, help="0: the whole frame")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args(argv)

@@ -297,6 +297,7 @@ int rg_upload_scene(rg_context *ctx, const rg_scene_desc *sc) {
     DevScene &s = ctx->scene;
     s.nodes = ctx->nodes;
     s.n_nodes = sc->n_nodes;
+    s.depth = depth < 1 ? 1 : depth;
     s.tris = ctx->tris;
     s.n_tris = sc->n_triangles;
     s.alias = ctx->alias;

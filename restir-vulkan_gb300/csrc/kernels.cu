@@ -14,6 +14,7 @@
 
 #include "rg_internal.h"
 #include "rg_math.cuh"
+#include "trace_pool.cuh"
 
 using namespace rgm;
 
@@ -25,7 +26,6 @@ cudaError_t upload_srgb_lut(const float *lut256) {
 
 namespace {
 
-constexpr int kStack = RG_MAX_TREE_DEPTH + 1;
 
 struct Texel {
     f3 albedo;
@@ -132,63 +132,24 @@ __device__ __forceinline__ void combine_res(Res &self, const Res &other, float p
 
 __device__ __forceinline__ f3 xyz(float4 v) { return mk(v.x, v.y, v.z); }
 
-// ---------------------------------------------------------------- any-hit traversal
-__device__ __forceinline__ bool tri_hit(const DevScene &s, int t, f3 o, f3 d) {
-    const GTri *tp = s.tris + t;
-    const float4 a = __ldg(&tp->a), b = __ldg(&tp->b), c = __ldg(&tp->c);
-    return ray_tri(mk(a.x, a.y, a.z), mk(a.w, b.x, b.y), mk(b.z, b.w, c.x), o, d);
-}
-
-// true when the segment o..o+d hits a triangle.  err is set if the walk
-// exceeds one visit per node (only possible for a malformed tree).
-__device__ bool trace_any(const DevScene &s, f3 o, f3 d, bool &err) {
-    if (s.n_nodes <= 0) return false;
-    int stack[kStack];
-    int top = 0;
-    int node = 0;
-    int visits = 0;
-    while (true) {
-        if (++visits > s.n_nodes) { err = true; return false; }
-        const GNode *np = s.nodes + node;
-        const float4 a = __ldg(&np->a), b = __ldg(&np->b), c = __ldg(&np->c);
-        const int4 ch = __ldg(&np->d);
-        const bool hl = ray_aabb(o, d, mk(a.x, a.y, a.z), mk(a.w, b.x, b.y));
-        const bool hr = ray_aabb(o, d, mk(b.z, b.w, c.x), mk(c.y, c.z, c.w));
-        int next = -1;
-        if (hl) {
-            if (ch.x < 0) { if (tri_hit(s, ~ch.x, o, d)) return true; }
-            else next = ch.x;
-        }
-        if (hr) {
-            if (ch.y < 0) { if (tri_hit(s, ~ch.y, o, d)) return true; }
-            else if (next < 0) next = ch.y;
-            else { if (top >= kStack) { err = true; return false; } stack[top++] = ch.y; }
-        }
-        if (next < 0) {
-            if (top == 0) return false;
-            next = stack[--top];
-        }
-        node = next;
-    }
-}
-
-__device__ __forceinline__ bool shadowed(const DevScene &s, f3 p1, f3 p2, bool &err) {
-    f3 o, d;
-    shadow_segment(p1, p2, o, d);
-    return trace_any(s, o, d, err);
-}
-
-__device__ __forceinline__ void count_rays(const DevScene &s, unsigned rays, bool err) {
-    const unsigned mask = __activemask();
-    const unsigned total = __reduce_add_sync(mask, rays);
-    const unsigned errs = __popc(__ballot_sync(mask, err));
-    if ((threadIdx.x & 31u) == (unsigned)(__ffs(mask) - 1)) {
-        if (total) atomicAdd(&s.counters[0], (unsigned long long)total);
-        if (errs) atomicAdd(&s.counters[1], (unsigned long long)errs);
-    }
+// ---------------------------------------------------------------- shadow rays
+__device__ __forceinline__ void count_block_rays(const DevScene &s, int rays, bool err) {
+    // one atomic per block for the ray count, one per erring warp
+    const unsigned errs = __ballot_sync(0xffffffffu, err);
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+    if ((tid & 31) == 0 && errs) atomicAdd(&s.counters[1], (unsigned long long)__popc(errs));
+    if (tid == 0 && rays) atomicAdd(&s.counters[0], (unsigned long long)rays);
 }
 
 // ---------------------------------------------------------------- RIS + visibility + temporal (restirOmni.glsl:86-212)
+// A block of 32x4 threads covers a 32x16 pixel tile, 4 pixels per thread:
+//   1. RIS for each pixel; the reservoir goes to `out`, the PCG state stays in
+//      registers, the visibility-reuse segment goes to the block's ray pool;
+//   2. the block traces its pool (trace_pool);
+//   3. per pixel: visibility reuse, then temporal reuse, final store.
+constexpr int kRisPpt = 4;
+constexpr int kRisTile = 128 * kRisPpt;
+
 struct InitialParams {
     DevScene s;
     GBufView cur, prev;
@@ -198,98 +159,149 @@ struct InitialParams {
     rg_restir_uniforms u;
 };
 
-__global__ void __launch_bounds__(128) k_initial_temporal(const InitialParams p) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int W = (int)p.u.screen_size[0], H = (int)p.u.screen_size[1];
-    if (x >= W || y >= H) return;
-    const size_t i = (size_t)y * (size_t)W + (size_t)x;
-    const DevScene &s = p.s;
-    Texel t;
-    load_texel(p.cur, i, t);
-    const float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
-    const f3 cam = mk(p.u.camera_pos[0], p.u.camera_pos[1], p.u.camera_pos[2]);
+__device__ __forceinline__ Res ris(const DevScene &s, const Texel &t, float albedo_lum, f3 cam, uint32_t count_c,
+                                   bool zero_normal, Pcg &rng) {
     Res r = empty_res();
-    Pcg rng = pcg_seed((uint64_t)p.u.frame, (uint64_t)((uint32_t)y * 10007u + (uint32_t)x));
-    const bool zero_normal = !(dot(t.normal, t.normal) != 0.0f);
-    if (!zero_normal) {
-        const f3 wo = view_dir(cam, t.wpos);
-        const int count = s.n_alias;
-        for (int c = 0; (uint32_t)c < p.u.initial_light_sample_count; ++c) {
-            const float r1 = rand_float(rng), r2 = rand_float(rng);
-            const int col = imin((int)((float)count * r1), count - 1);
-            float4 pos_lum, nrm;
-            float prob;
-            int32_t lidx;
-            if (s.n_point_lights != 0) {
-                const AliasLight *al = s.alias + col;
-                const float4 cc = __ldg(&al->col);
-                if (cc.x > r2) { pos_lum = __ldg(&al->own_pos); prob = cc.z; lidx = col; }
-                else { pos_lum = __ldg(&al->alias_pos); prob = cc.w; lidx = __float_as_int(cc.y); }
-                nrm = make_float4(0.f, 0.f, 0.f, 0.f);
-            } else {
-                const rg_alias_table_column cc = s.tri_alias[col];
-                int sel;
-                if (cc.prob > r2) { sel = col; prob = cc.ori_prob; }
-                else { sel = cc.alias; prob = cc.alias_ori_prob; }
-                const rg_tri_light &L = s.tri_lights[sel];
-                const float ra = rand_float(rng), rb = rand_float(rng);
-                const float sa = sqrtf(ra);  // pickPointOnTriangle, restirOmni.glsl:68-71
-                const f3 lpos = (scale(1.0f - sa, mk(L.p1[0], L.p1[1], L.p1[2])) +
-                                 scale(sa * (1.0f - rb), mk(L.p2[0], L.p2[1], L.p2[2]))) +
-                                scale(rb * sa, mk(L.p3[0], L.p3[1], L.p3[2]));
-                const f3 wi = normalize(t.wpos - lpos);
-                const f3 nn = mk(L.normal_area[0], L.normal_area[1], L.normal_area[2]);
-                prob /= fabsf(dot(wi, nn)) * L.normal_area[3];
-                pos_lum = make_float4(lpos.x, lpos.y, lpos.z, L.emission_luminance[3]);
-                nrm = make_float4(nn.x, nn.y, nn.z, 1.0f);
-                lidx = -1 - sel;
-            }
-            const float ph = eval_phat_wo(t.wpos, xyz(pos_lum), wo, t.normal, xyz(nrm), nrm.w > 0.5f, albedo_lum,
-                                          pos_lum.w, t.roughness, t.metallic);
-            add_sample(r, pos_lum, nrm, lidx, ph, prob, rng);
+    if (zero_normal) return r;
+    const f3 wo = view_dir(cam, t.wpos);
+    const int count = s.n_alias;
+    for (uint32_t c = 0; c < count_c; ++c) {
+        const float r1 = rand_float(rng), r2 = rand_float(rng);
+        const int col = imin((int)((float)count * r1), count - 1);  // restirOmni.glsl:73-83
+        float4 pos_lum, nrm;
+        float prob;
+        int32_t lidx;
+        if (s.n_point_lights != 0) {
+            const AliasLight *al = s.alias + col;
+            const float4 cc = __ldg(&al->col);
+            if (cc.x > r2) { pos_lum = __ldg(&al->own_pos); prob = cc.z; lidx = col; }
+            else { pos_lum = __ldg(&al->alias_pos); prob = cc.w; lidx = __float_as_int(cc.y); }
+            nrm = make_float4(0.f, 0.f, 0.f, 0.f);
+        } else {
+            const rg_alias_table_column cc = s.tri_alias[col];
+            int sel;
+            if (cc.prob > r2) { sel = col; prob = cc.ori_prob; }
+            else { sel = cc.alias; prob = cc.alias_ori_prob; }
+            const rg_tri_light &L = s.tri_lights[sel];
+            const float ra = rand_float(rng), rb = rand_float(rng);
+            const float sa = sqrtf(ra);  // pickPointOnTriangle, restirOmni.glsl:68-71
+            const f3 lpos = (scale(1.0f - sa, mk(L.p1[0], L.p1[1], L.p1[2])) +
+                             scale(sa * (1.0f - rb), mk(L.p2[0], L.p2[1], L.p2[2]))) +
+                            scale(rb * sa, mk(L.p3[0], L.p3[1], L.p3[2]));
+            const f3 wi = normalize(t.wpos - lpos);
+            const f3 nn = mk(L.normal_area[0], L.normal_area[1], L.normal_area[2]);
+            prob /= fabsf(dot(wi, nn)) * L.normal_area[3];
+            pos_lum = make_float4(lpos.x, lpos.y, lpos.z, L.emission_luminance[3]);
+            nrm = make_float4(nn.x, nn.y, nn.z, 1.0f);
+            lidx = -1 - sel;
         }
+        const float ph = eval_phat_wo(t.wpos, xyz(pos_lum), wo, t.normal, xyz(nrm), nrm.w > 0.5f, albedo_lum,
+                                      pos_lum.w, t.roughness, t.metallic);
+        add_sample(r, pos_lum, nrm, lidx, ph, prob, rng);
     }
-    unsigned rays = 0;
+    return r;
+}
+
+__global__ void __launch_bounds__(128) k_initial_temporal(const InitialParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    rgpool::Ray *pool = reinterpret_cast<rgpool::Ray *>(smem);
+    float4 *endp = reinterpret_cast<float4 *>(pool + kRisTile);  // sample position per pixel slot
+    uint8_t *shadow = reinterpret_cast<uint8_t *>(endp + kRisTile);
+    int *stack = reinterpret_cast<int *>(shadow + kRisTile);
+    __shared__ int s_count, s_next;
+    const int tid = threadIdx.x + threadIdx.y * 32;
+    if (tid == 0) { s_count = 0; s_next = 0; }
+    __syncthreads();
+    const DevScene &s = p.s;
+    const int W = (int)p.u.screen_size[0], H = (int)p.u.screen_size[1];
+    const int x = blockIdx.x * 32 + threadIdx.x;
+    const int y0 = blockIdx.y * (4 * kRisPpt) + threadIdx.y;
+    const f3 cam = mk(p.u.camera_pos[0], p.u.camera_pos[1], p.u.camera_pos[2]);
+    const bool vis = (p.u.flags & RG_FLAG_VISIBILITY_REUSE) != 0;
+    uint64_t rng_state[kRisPpt];
+#pragma unroll
+    for (int j = 0; j < kRisPpt; ++j) {
+        const int y = y0 + 4 * j;
+        const bool valid = x < W && y < H;
+        bool want = false;
+        f3 wpos = mk(0.f, 0.f, 0.f), lpos = wpos;
+        rng_state[j] = 0;
+        if (valid) {
+            const size_t i = (size_t)y * (size_t)W + (size_t)x;
+            Texel t;
+            load_texel(p.cur, i, t);
+            const float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
+            Pcg rng = pcg_seed((uint64_t)p.u.frame, (uint64_t)((uint32_t)y * 10007u + (uint32_t)x));
+            const bool zero_normal = !(dot(t.normal, t.normal) != 0.0f);
+            const Res r = ris(s, t, albedo_lum, cam, p.u.initial_light_sample_count, zero_normal, rng);
+            store_res(p.out, i, r);
+            rng_state[j] = rng.state;
+            // visibility reuse :147-160; a background pixel's (zero normal) sample is the
+            // zero sample, for which zeroing w and sumWeights changes nothing: no ray
+            want = vis && !zero_normal;
+            wpos = t.wpos;
+            lpos = xyz(r.pos_lum);
+        }
+        shadow[j * 128 + tid] = 0;
+        endp[j * 128 + tid] = make_float4(lpos.x, lpos.y, lpos.z, 0.0f);
+        const int slot = rgpool::append_slot(&s_count, want);
+        if (want) rgpool::put_ray(pool, slot, wpos, j * 128 + tid);
+    }
+    __syncthreads();
     bool err = false;
-    if ((p.u.flags & RG_FLAG_VISIBILITY_REUSE) && !zero_normal) {
-        ++rays;
-        if (shadowed(s, t.wpos, xyz(r.pos_lum), err)) {
+    rgpool::trace_pool(
+        s, pool, s_count, &s_next, stack, s.depth, err,
+        [&](int owner) { const float4 e = endp[owner]; return mk(e.x, e.y, e.z); },
+        [&](int owner, bool hit) { shadow[owner] = hit ? 1 : 0; });
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kRisPpt; ++j) {
+        const int y = y0 + 4 * j;
+        if (x >= W || y >= H) continue;
+        const size_t i = (size_t)y * (size_t)W + (size_t)x;
+        Res r = load_res(p.out, i);
+        if (shadow[j * 128 + tid]) {
             r.w = 0.0f;
             r.sum_w = 0.0f;
         }
-    }
-    if ((p.u.flags & RG_FLAG_TEMPORAL_REUSE) && p.has_prev) {
-        const float *m = p.u.prev_frame_projection_view;
-        float px = ((m[0] * t.wpos.x + m[4] * t.wpos.y) + m[8] * t.wpos.z) + m[12] * 1.0f;
-        float py = ((m[1] * t.wpos.x + m[5] * t.wpos.y) + m[9] * t.wpos.z) + m[13] * 1.0f;
-        const float pw = ((m[3] * t.wpos.x + m[7] * t.wpos.y) + m[11] * t.wpos.z) + m[15] * 1.0f;
-        px /= pw;
-        py /= pw;
-        px = (px + 1.0f) * 0.5f * (float)p.u.screen_size[0];
-        py = (py + 1.0f) * 0.5f * (float)p.u.screen_size[1];
-        if (px > 0.0f && py > 0.0f && px < (float)p.u.screen_size[0] && py < (float)p.u.screen_size[1]) {
-            const int fx = (int)px, fy = (int)py;
-            const size_t pi = (size_t)fy * (size_t)W + (size_t)fx;
-            const f3 dp = t.wpos - load_wpos(p.prev, pi);
-            if (dot(dp, dp) < 0.01f) {
-                const f3 da = t.albedo - load_albedo(p.prev, pi, nullptr);
-                if (dot(da, da) < 0.01f) {
-                    if (dot(t.normal, load_normal(p.prev, pi)) > 0.5f) {
-                        Res pr = load_res(p.prev_res, pi);
-                        const uint32_t cap = p.u.temporal_sample_count_multiplier * r.m;
-                        pr.m = pr.m < cap ? pr.m : cap;
-                        const float ph = eval_phat_wo(t.wpos, xyz(pr.pos_lum), view_dir(cam, t.wpos), t.normal,
-                                                      xyz(pr.nrm), pr.nrm.w > 0.5f, albedo_lum, pr.pos_lum.w,
-                                                      t.roughness, t.metallic);
-                        combine_res(r, pr, ph, rng);
+        if ((p.u.flags & RG_FLAG_TEMPORAL_REUSE) && p.has_prev) {
+            Texel t;
+            load_texel(p.cur, i, t);
+            const float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
+            Pcg rng;
+            rng.state = rng_state[j];
+            rng.inc = ((uint64_t)((uint32_t)y * 10007u + (uint32_t)x) << 1u) | 1u;
+            const float *m = p.u.prev_frame_projection_view;
+            float px = ((m[0] * t.wpos.x + m[4] * t.wpos.y) + m[8] * t.wpos.z) + m[12] * 1.0f;
+            float py = ((m[1] * t.wpos.x + m[5] * t.wpos.y) + m[9] * t.wpos.z) + m[13] * 1.0f;
+            const float pw = ((m[3] * t.wpos.x + m[7] * t.wpos.y) + m[11] * t.wpos.z) + m[15] * 1.0f;
+            px /= pw;
+            py /= pw;
+            px = (px + 1.0f) * 0.5f * (float)p.u.screen_size[0];
+            py = (py + 1.0f) * 0.5f * (float)p.u.screen_size[1];
+            if (px > 0.0f && py > 0.0f && px < (float)p.u.screen_size[0] && py < (float)p.u.screen_size[1]) {
+                const int fx = (int)px, fy = (int)py;
+                const size_t pi = (size_t)fy * (size_t)W + (size_t)fx;
+                const f3 dp = t.wpos - load_wpos(p.prev, pi);
+                if (dot(dp, dp) < 0.01f) {
+                    const f3 da = t.albedo - load_albedo(p.prev, pi, nullptr);
+                    if (dot(da, da) < 0.01f) {
+                        if (dot(t.normal, load_normal(p.prev, pi)) > 0.5f) {
+                            Res pr = load_res(p.prev_res, pi);
+                            const uint32_t cap = p.u.temporal_sample_count_multiplier * r.m;
+                            pr.m = pr.m < cap ? pr.m : cap;
+                            const float ph = eval_phat_wo(t.wpos, xyz(pr.pos_lum), view_dir(cam, t.wpos), t.normal,
+                                                          xyz(pr.nrm), pr.nrm.w > 0.5f, albedo_lum, pr.pos_lum.w,
+                                                          t.roughness, t.metallic);
+                            combine_res(r, pr, ph, rng);
+                        }
                     }
                 }
             }
         }
+        store_res(p.out, i, r);
     }
-    store_res(p.out, i, r);
-    count_rays(s, rays, err);
+    count_block_rays(s, tid == 0 ? s_count : 0, err);
 }
 
 // ---------------------------------------------------------------- biased spatial (spatialReuse.comp:30-86)
@@ -338,70 +350,124 @@ __global__ void __launch_bounds__(128) k_spatial_biased(const SpatialParams p) {
 }
 
 // ---------------------------------------------------------------- unbiased spatial (unbiasedReuse.glsl:50-185)
+// One pixel per thread, 32x4 threads per block:
+//   1. neighbour streaming (:84-124); then, for every neighbour whose
+//      hemisphere holds the chosen sample and for the pixel itself, the
+//      visibility segment goes to the block's ray pool (:132-166);
+//   2. the block traces its pool;
+//   3. the normalisation count and the final W (:168-182).
+// Shared memory: ray pool [128*(K+1)], sample position per pixel [128],
+// neighbour index and M [K][128], not-counted flags [(K+1)][128], stacks.
+// The merged reservoir is parked in `out` between steps 1 and 3.
 constexpr int kMaxNeighbors = 16;
 
+__host__ __device__ inline size_t unbiased_smem_bytes(int K, int depth) {
+    const size_t slots = (size_t)K + 1;
+    size_t b = 128 * slots * sizeof(rgpool::Ray);
+    b += 128 * sizeof(float4);
+    b += 2 * 128 * (size_t)(K > 0 ? K : 1) * sizeof(uint32_t);
+    b += (128 * slots + 15) & ~(size_t)15;
+    b += 128 * (size_t)depth * sizeof(int);
+    return b;
+}
+
 __global__ void __launch_bounds__(128) k_spatial_unbiased(const SpatialParams p) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int W = (int)p.u.screen_size[0], H = (int)p.u.screen_size[1];
-    if (x >= W || y >= H) return;
-    const DevScene &s = p.s;
-    const size_t i = (size_t)y * (size_t)W + (size_t)x;
-    Texel t;
-    load_texel(p.g, i, t);
-    const float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
-    const f3 cam = mk(p.u.camera_pos[0], p.u.camera_pos[1], p.u.camera_pos[2]);
-    const f3 wo = view_dir(cam, t.wpos);
-    Res r = load_res(p.in, i);
-    Pcg rng = pcg_seed((uint64_t)(p.u.frame * 17u + (uint32_t)p.iter), (uint64_t)((uint32_t)y * 10007u + (uint32_t)x));
+    extern __shared__ __align__(16) unsigned char smem[];
     const int K = p.num_neighbors;
-    uint32_t nidx[kMaxNeighbors];
-    uint32_t nm[kMaxNeighbors];
-    const uint32_t orig_m = r.m;
-    for (int k = 0; k < K; ++k) {
-        const float angle = rand_float(rng) * 2.0f * kPi;
-        const float radius = sqrtf(rand_float(rng)) * p.u.spatial_radius;
-        float sn, cs;
-        sincos_cw(angle, sn, cs);
-        const int nx = iclamp(x + (int)roundf(cs * radius), 0, (int)(p.u.screen_size[0] - 1u));
-        const int ny = iclamp(y + (int)roundf(sn * radius), 0, (int)(p.u.screen_size[1] - 1u));
-        const size_t ni = (size_t)ny * (size_t)W + (size_t)nx;
-        const Res rr = load_res(p.in, ni);
-        nidx[k] = (uint32_t)ni;
-        nm[k] = rr.m;
-        r.m += rr.m;
-        const float ph = eval_phat_wo(t.wpos, xyz(rr.pos_lum), wo, t.normal, xyz(rr.nrm), rr.nrm.w > 0.5f, albedo_lum,
-                                      rr.pos_lum.w, t.roughness, t.metallic);
-        const float weight = ph * rr.w * (float)rr.m;
-        if (weight > 0.0f) update_res(r, weight, rr.pos_lum, rr.nrm, rr.idx, ph, rr.w, rng);
-    }
-    const f3 lpos = xyz(r.pos_lum);
+    const int slots = K + 1;
+    rgpool::Ray *pool = reinterpret_cast<rgpool::Ray *>(smem);
+    float4 *endp = reinterpret_cast<float4 *>(pool + 128 * slots);              // [128]
+    uint32_t *nidx = reinterpret_cast<uint32_t *>(endp + 128);                   // [K][128]
+    uint32_t *nm = nidx + 128 * (K > 0 ? K : 1);                                  // [K][128]
+    uint8_t *flag = reinterpret_cast<uint8_t *>(nm + 128 * (K > 0 ? K : 1));      // [slots][128]
+    int *stack = reinterpret_cast<int *>(flag + ((128 * slots + 15) & ~15));
+    __shared__ int s_count, s_next;
+    const int tid = threadIdx.x + threadIdx.y * 32;
+    if (tid == 0) { s_count = 0; s_next = 0; }
+    __syncthreads();
+    const DevScene &s = p.s;
+    const int W = (int)p.u.screen_size[0], H = (int)p.u.screen_size[1];
+    const int x = blockIdx.x * 32 + threadIdx.x;
+    const int y = blockIdx.y * 4 + threadIdx.y;
+    const bool valid = x < W && y < H;
     const bool vis = (p.u.flags & RG_FLAG_VISIBILITY_REUSE) != 0;
-    uint32_t ns = orig_m;
-    unsigned rays = 0;
-    bool err = false;
-    for (int k = 0; k < K; ++k) {
-        const f3 nw = load_wpos(p.g, nidx[k]);
-        const f3 nn = load_normal(p.g, nidx[k]);
-        if (dot(lpos - nw, nn) < 0.0f) continue;
-        if (vis) {
-            ++rays;
-            if (shadowed(s, nw, lpos, err)) continue;
+    const size_t i = valid ? (size_t)y * (size_t)W + (size_t)x : 0;
+    f3 wpos = mk(0.f, 0.f, 0.f), lpos = wpos;
+    uint32_t orig_m = 0;
+    if (valid) {
+        Texel t;
+        load_texel(p.g, i, t);
+        wpos = t.wpos;
+        const float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
+        const f3 cam = mk(p.u.camera_pos[0], p.u.camera_pos[1], p.u.camera_pos[2]);
+        const f3 wo = view_dir(cam, t.wpos);
+        Res r = load_res(p.in, i);
+        orig_m = r.m;
+        Pcg rng = pcg_seed((uint64_t)(p.u.frame * 17u + (uint32_t)p.iter),
+                           (uint64_t)((uint32_t)y * 10007u + (uint32_t)x));
+        for (int k = 0; k < K; ++k) {
+            const float angle = rand_float(rng) * 2.0f * kPi;
+            const float radius = sqrtf(rand_float(rng)) * p.u.spatial_radius;
+            float sn, cs;
+            sincos_cw(angle, sn, cs);
+            const int nx = iclamp(x + (int)roundf(cs * radius), 0, (int)(p.u.screen_size[0] - 1u));
+            const int ny = iclamp(y + (int)roundf(sn * radius), 0, (int)(p.u.screen_size[1] - 1u));
+            const size_t ni = (size_t)ny * (size_t)W + (size_t)nx;
+            const Res rr = load_res(p.in, ni);
+            nidx[k * 128 + tid] = (uint32_t)ni;
+            nm[k * 128 + tid] = rr.m;
+            r.m += rr.m;
+            const float ph = eval_phat_wo(t.wpos, xyz(rr.pos_lum), wo, t.normal, xyz(rr.nrm), rr.nrm.w > 0.5f,
+                                          albedo_lum, rr.pos_lum.w, t.roughness, t.metallic);
+            const float weight = ph * rr.w * (float)rr.m;
+            if (weight > 0.0f) update_res(r, weight, rr.pos_lum, rr.nrm, rr.idx, ph, rr.w, rng);
         }
-        ns += nm[k];
+        lpos = xyz(r.pos_lum);
+        store_res(p.out, i, r);
     }
-    if (vis) {
-        ++rays;
-        if (shadowed(s, t.wpos, lpos, err)) ns = 0;
+    endp[tid] = make_float4(lpos.x, lpos.y, lpos.z, 0.0f);
+    for (int k = 0; k < K; ++k) {
+        bool want = false, excluded = true;
+        f3 nw = mk(0.f, 0.f, 0.f);
+        if (valid) {
+            const uint32_t ni = nidx[k * 128 + tid];
+            nw = load_wpos(p.g, ni);
+            const f3 nn = load_normal(p.g, ni);
+            excluded = dot(lpos - nw, nn) < 0.0f;
+            want = !excluded && vis;
+        }
+        flag[k * 128 + tid] = excluded ? 1 : 0;
+        const int slot = rgpool::append_slot(&s_count, want);
+        if (want) rgpool::put_ray(pool, slot, nw, k * 128 + tid);
     }
-    if (ns > 0) {
-        r.w = r.sum_w / ((float)ns * r.p_hat);
-    } else {
-        r.w = 0.0f;
-        r.sum_w = 0.0f;
+    {
+        const bool want = valid && vis;
+        flag[K * 128 + tid] = 0;
+        const int slot = rgpool::append_slot(&s_count, want);
+        if (want) rgpool::put_ray(pool, slot, wpos, K * 128 + tid);
     }
-    store_res(p.out, i, r);
-    count_rays(s, rays, err);
+    __syncthreads();
+    bool err = false;
+    rgpool::trace_pool(
+        s, pool, s_count, &s_next, stack, s.depth, err,
+        [&](int owner) { const float4 e = endp[owner & 127]; return mk(e.x, e.y, e.z); },
+        [&](int owner, bool hit) { if (hit) flag[owner] = 1; });
+    __syncthreads();
+    if (valid) {
+        uint32_t ns = orig_m;
+        for (int k = 0; k < K; ++k)
+            if (!flag[k * 128 + tid]) ns += nm[k * 128 + tid];
+        if (vis && flag[K * 128 + tid]) ns = 0;
+        Res r = load_res(p.out, i);
+        if (ns > 0) {
+            r.w = r.sum_w / ((float)ns * r.p_hat);
+        } else {
+            r.w = 0.0f;
+            r.sum_w = 0.0f;
+        }
+        store_res(p.out, i, r);
+    }
+    count_block_rays(s, tid == 0 ? s_count : 0, err);
 }
 
 // ---------------------------------------------------------------- shading (lighting.frag:43-71,103)
@@ -447,14 +513,32 @@ __global__ void __launch_bounds__(128) k_shade(const ShadeParams p) {
 }
 
 // ---------------------------------------------------------------- visibility batch (testVisibility)
+// 128 threads take a chunk of 512 segments into the pool and trace it.
+constexpr int kVisChunk = 512;
+
 __global__ void __launch_bounds__(128) k_visibility_batch(const DevScene s, const float4 *p1, const float4 *p2,
                                                           uint8_t *out, int n) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 a = __ldg(p1 + i), b = __ldg(p2 + i);
+    extern __shared__ __align__(16) unsigned char smem[];
+    rgpool::Ray *pool = reinterpret_cast<rgpool::Ray *>(smem);
+    float4 *endp = reinterpret_cast<float4 *>(pool + kVisChunk);
+    int *stack = reinterpret_cast<int *>(endp + kVisChunk);
+    __shared__ int s_next;
+    const int tid = threadIdx.x;
+    const int base = blockIdx.x * kVisChunk;
+    const int count = min(kVisChunk, n - base);
+    if (tid == 0) s_next = 0;
+    for (int k = tid; k < count; k += 128) {
+        const float4 a = __ldg(p1 + base + k), b = __ldg(p2 + base + k);
+        rgpool::put_ray(pool, k, mk(a.x, a.y, a.z), k);
+        endp[k] = b;
+    }
+    __syncthreads();
     bool err = false;
-    out[i] = shadowed(s, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), err) ? 1 : 0;
-    count_rays(s, 1u, err);
+    rgpool::trace_pool(
+        s, pool, count, &s_next, stack, s.depth, err,
+        [&](int owner) { const float4 e = endp[owner]; return mk(e.x, e.y, e.z); },
+        [&](int owner, bool hit) { out[base + owner] = hit ? 1 : 0; });
+    count_block_rays(s, tid == 0 ? count : 0, err);
 }
 
 dim3 pixel_grid(int w, int h, dim3 block) {
@@ -487,7 +571,11 @@ cudaError_t launch_initial_temporal(const DevScene &s, const GBufView &cur, cons
     p.out = out;
     p.u = u;
     const dim3 block(32, 4);
-    k_initial_temporal<<<pixel_grid((int)u.screen_size[0], (int)u.screen_size[1], block), block, 0, st>>>(p);
+    const dim3 grid((u.screen_size[0] + 31u) / 32u, (u.screen_size[1] + 4u * kRisPpt - 1u) / (4u * kRisPpt));
+    const size_t smem = kRisTile * (sizeof(rgpool::Ray) + sizeof(float4) + 1) + 128 * (size_t)s.depth * sizeof(int);
+    cudaError_t e = cudaFuncSetAttribute(k_initial_temporal, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_initial_temporal<<<grid, block, smem, st>>>(p);
     return cudaGetLastError();
 }
 
@@ -520,7 +608,10 @@ cudaError_t launch_spatial_unbiased(const DevScene &s, const GBufView &g, const 
     p.num_neighbors = num_neighbors;
     p.cos_thr = 0.0f;
     const dim3 block(32, 4);
-    k_spatial_unbiased<<<pixel_grid((int)u.screen_size[0], (int)u.screen_size[1], block), block, 0, st>>>(p);
+    const size_t smem = unbiased_smem_bytes(num_neighbors, s.depth);
+    cudaError_t e = cudaFuncSetAttribute(k_spatial_unbiased, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_spatial_unbiased<<<pixel_grid((int)u.screen_size[0], (int)u.screen_size[1], block), block, smem, st>>>(p);
     return cudaGetLastError();
 }
 
@@ -540,6 +631,9 @@ cudaError_t launch_shade(const DevScene &s, const GBufView &g, const rg_reservoi
 cudaError_t launch_visibility_batch(const DevScene &s, const float4 *p1, const float4 *p2, uint8_t *out, int n,
                                     cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_visibility_batch<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(s, p1, p2, out, n);
+    const size_t smem = kVisChunk * (sizeof(rgpool::Ray) + sizeof(float4)) + 128 * (size_t)s.depth * sizeof(int);
+    cudaError_t e = cudaFuncSetAttribute(k_visibility_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_visibility_batch<<<(unsigned)((n + kVisChunk - 1) / kVisChunk), 128, smem, st>>>(s, p1, p2, out, n);
     return cudaGetLastError();
 }

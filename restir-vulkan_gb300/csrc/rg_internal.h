@@ -35,6 +35,7 @@ struct AliasLight {
 struct DevScene {
     const GNode *nodes;
     int32_t n_nodes;
+    int32_t depth;                // validated tree depth (root = 1): traversal stack size
     const GTri *tris;
     int32_t n_tris;
     const AliasLight *alias;      // point-light scenes

@@ -1,0 +1,195 @@
+// trace_pool.cuh -- block-cooperative shadow-ray traversal.
+//
+// A block first collects its shadow segments in a shared-memory pool, then
+// every thread of the block traces rays from that pool: a thread that
+// finishes a ray immediately takes the next one (shared-memory counter), so
+// the lanes of a warp stay busy until the pool runs dry instead of idling
+// while the longest ray of their batch finishes.  Each thread's traversal
+// stack lives in shared memory, interleaved by thread so consecutive lanes
+// hit consecutive banks; its depth is the validated tree depth.
+//
+// Results equal the reference's batched stack walk
+// (src/shaders/include/softwareRaytracing.glsl:42-85): the any-hit answer is
+// an OR over every triangle whose whole box path passes the slab test, which
+// does not depend on the visiting order; every slab and triangle test uses
+// the exact arithmetic of rg_math.cuh.
+#pragma once
+#include "rg_internal.h"
+#include "rg_math.cuh"
+
+namespace rgpool {
+
+using rgm::f3;
+using rgm::mk;
+
+// 16-byte pool entry: segment start p1 and an owner tag chosen by the
+// producer; the segment end p2 comes from the caller's endpoint(owner), so
+// rays that share an end (the spatial pass: one sample per pixel) store it
+// once.  The tracer forms testVisibility's offset segment itself.
+struct Ray {
+    float4 a;  // p1.xyz, owner (int bits)
+};
+
+__device__ __forceinline__ void put_ray(Ray *pool, int slot, f3 p1, int owner) {
+    pool[slot].a = make_float4(p1.x, p1.y, p1.z, __int_as_float(owner));
+}
+
+// Warp-aggregated append to a shared counter: returns this lane's slot
+// (only meaningful where `want` is true).
+__device__ __forceinline__ int append_slot(int *counter, bool want) {
+    const unsigned mask = __ballot_sync(0xffffffffu, want);
+    if (!mask) return -1;
+    const int lane = (threadIdx.x + threadIdx.y * blockDim.x) & 31;
+    const int leader = __ffs(mask) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+// Slab test of one child box (softwareRaytracing.glsl:9-14); also returns the
+// entry distance, used only to order the walk.
+__device__ __forceinline__ bool box_hit(f3 o, f3 d, f3 bmin, f3 bmax, float &rmin_out) {
+    const float t0x = (bmin.x - o.x) / d.x, t1x = (bmax.x - o.x) / d.x;
+    const float t0y = (bmin.y - o.y) / d.y, t1y = (bmax.y - o.y) / d.y;
+    const float t0z = (bmin.z - o.z) / d.z, t1z = (bmax.z - o.z) / d.z;
+    const float rmin = rgm::gmax(rgm::gmin(t0x, t1x), rgm::gmax(rgm::gmin(t0y, t1y), rgm::gmin(t0z, t1z)));
+    const float rmax = rgm::gmin(rgm::gmax(t0x, t1x), rgm::gmin(rgm::gmax(t0y, t1y), rgm::gmax(t0z, t1z)));
+    rmin_out = rmin;
+    return rmin < 1.0f && rmax >= rmin && rmax > 0.0f;
+}
+
+// Filtered slab test.  The reference computes t = RN((b-o)/d) per slab; here
+// t~ = RN((b-o) * RN(1/d)) with 1/d precomputed per ray, so
+//   |t~ - t| <= 1.5 * 2^-23 |t|            (normal range, no overflow).
+// rmin and rmax are max/min compositions, which are monotone, and
+// min(g(x), g(y)) = g(min(x, y)) for g(t) = t +- eps|t| (also monotone), so
+// rmin~ and rmax~ lie within eps|rmin| and eps|rmax| of the exact values.  The
+// three comparisons of the reference's test are therefore decided here
+// whenever each is farther than a 2^-19 relative margin (10x the bound) from
+// its threshold, and rmin~, rmax~ are finite and at least 2^-90 in magnitude;
+// otherwise the function returns -1 and the caller repeats the test with
+// exact division.  NaN slabs (b == o and d == 0) arise at the same positions
+// in both computations and propagate the same way through min/max.
+// Returns 1 hit, 0 miss, -1 undecided.
+//
+// The fast path only runs for rays whose direction components are all
+// nonzero, finite and within [2^-100, 2^100] in magnitude (ray_inverse), so
+// no slab value is NaN or infinite and IEEE fminf/fmaxf select the same
+// values as the GLSL min/max definitions (a +-0 result fails the 2^-90 test
+// and is decided exactly).
+__device__ __forceinline__ int box_filtered(f3 o, f3 inv, f3 bmin, f3 bmax, float &rmin_out) {
+    const float t0x = (bmin.x - o.x) * inv.x, t1x = (bmax.x - o.x) * inv.x;
+    const float t0y = (bmin.y - o.y) * inv.y, t1y = (bmax.y - o.y) * inv.y;
+    const float t0z = (bmin.z - o.z) * inv.z, t1z = (bmax.z - o.z) * inv.z;
+    const float rmin = fmaxf(fminf(t0x, t1x), fmaxf(fminf(t0y, t1y), fminf(t0z, t1z)));
+    const float rmax = fminf(fmaxf(t0x, t1x), fminf(fmaxf(t0y, t1y), fmaxf(t0z, t1z)));
+    rmin_out = rmin;
+    constexpr float kEps = 1.9073486328125e-6f;     // 2^-19
+    constexpr float kTiny = 8.0779356694631609e-28f; // 2^-90
+    constexpr float kBig = 1.0e38f;
+    const float ar = fabsf(rmin), ax = fabsf(rmax);
+    if (!(ar >= kTiny && ar <= kBig && ax >= kTiny && ax <= kBig)) return -1;
+    if (rmax < 0.0f) return 0;                               // rmax > 0 fails
+    const float m1 = kEps * ar;
+    if (rmin > 1.0f + m1) return 0;                          // rmin < 1 fails
+    const float m2 = kEps * (ar + ax);
+    if (rmin - rmax > m2) return 0;                          // rmax >= rmin fails
+    if (rmin < 1.0f - m1 && rmax - rmin > m2) return 1;      // all three hold
+    return -1;
+}
+
+// Per-ray reciprocal of the direction; false when a component is zero,
+// tiny, huge or NaN, for which the ray uses exact division throughout.
+__device__ __forceinline__ bool ray_inverse(f3 d, f3 &inv) {
+    inv = mk(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    constexpr float kLo = 7.8886090522101181e-31f;  // 2^-100
+    constexpr float kHi = 1.2676506002282294e30f;   // 2^100
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    return ax >= kLo && ax <= kHi && ay >= kLo && ay <= kHi && az >= kLo && az <= kHi;
+}
+
+__device__ __forceinline__ bool tri_hit(const GTri *tris, int t, f3 o, f3 d) {
+    const GTri *tp = tris + t;
+    const float4 a = __ldg(&tp->a), b = __ldg(&tp->b), c = __ldg(&tp->c);
+    return rgm::ray_tri(mk(a.x, a.y, a.z), mk(a.w, b.x, b.y), mk(b.z, b.w, c.x), o, d);
+}
+
+// Traces pool[0..n) with all threads of the block; writes shadowed (1) /
+// unoccluded (0) through `emit(owner, shadowed)`.  `stack` points at
+// blockDim.x * depth ints of shared memory.  Sets *err on a walk longer than
+// one visit per node or a stack overflow (malformed tree; not reachable for
+// trees validated at upload).  Must be called by every thread of the block.
+template <typename Endpoint, typename Emit>
+__device__ void trace_pool(const DevScene &s, const Ray *pool, int n, int *next, int *stack, int depth, bool &err,
+                           Endpoint endpoint, Emit emit) {
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+    const int nthreads = blockDim.x * blockDim.y;
+    int *my_stack = stack + tid;
+    int cur = -1, owner = 0, node = 0, sp = 0, visits = 0;
+    f3 o = mk(0.f, 0.f, 0.f), d = mk(0.f, 0.f, 0.f), inv = o;
+    bool fast = true;
+    while (true) {
+        if (cur < 0) {
+            cur = atomicAdd(next, 1);
+            if (cur >= n) break;
+            const float4 a = pool[cur].a;
+            owner = __float_as_int(a.w);
+            rgm::shadow_segment(mk(a.x, a.y, a.z), endpoint(owner), o, d);
+            fast = ray_inverse(d, inv);
+            node = 0;
+            sp = 0;
+            visits = 0;
+            if (s.n_nodes <= 0) {  // single-triangle scene: no tree
+                emit(owner, s.n_tris > 0 && tri_hit(s.tris, 0, o, d));
+                cur = -1;
+                continue;
+            }
+        }
+        bool done = false, hit = false;
+        if (++visits > s.n_nodes) {
+            err = true;
+            done = true;
+        } else {
+            const GNode *np = s.nodes + node;
+            const float4 na = __ldg(&np->a), nb = __ldg(&np->b), nc = __ldg(&np->c);
+            const int4 ch = __ldg(&np->d);
+            float tl, tr;
+            const f3 lmin = mk(na.x, na.y, na.z), lmax = mk(na.w, nb.x, nb.y);
+            const f3 rmin = mk(nb.z, nb.w, nc.x), rmax = mk(nc.y, nc.z, nc.w);
+            int fl = fast ? box_filtered(o, inv, lmin, lmax, tl) : -1;
+            int fr = fast ? box_filtered(o, inv, rmin, rmax, tr) : -1;
+            if (fl < 0) fl = box_hit(o, d, lmin, lmax, tl) ? 1 : 0;
+            if (fr < 0) fr = box_hit(o, d, rmin, rmax, tr) ? 1 : 0;
+            const bool hl = fl != 0, hr = fr != 0;
+            if (hl && ch.x < 0 && tri_hit(s.tris, ~ch.x, o, d)) hit = true;
+            else if (hr && ch.y < 0 && tri_hit(s.tris, ~ch.y, o, d)) hit = true;
+            if (hit) {
+                done = true;
+            } else {
+                const bool il = hl && ch.x >= 0, ir = hr && ch.y >= 0;
+                if (il && ir) {
+                    const bool left_first = !(tr < tl);
+                    node = left_first ? ch.x : ch.y;
+                    if (sp >= depth) { err = true; done = true; }
+                    else { my_stack[sp * nthreads] = left_first ? ch.y : ch.x; ++sp; }
+                } else if (il) {
+                    node = ch.x;
+                } else if (ir) {
+                    node = ch.y;
+                } else if (sp > 0) {
+                    --sp;
+                    node = my_stack[sp * nthreads];
+                } else {
+                    done = true;
+                }
+            }
+        }
+        if (done) {
+            emit(owner, hit);
+            cur = -1;
+        }
+    }
+}
+
+}  // namespace rgpool
