@@ -236,6 +236,25 @@ int rg_render_frame_host(rg_context *ctx, int32_t width, int32_t height, const u
                          const uint16_t *normal, const uint16_t *material, const float *world_pos,
                          const float *depth, const rg_frame_params *params, float *rgba_out_host, void *stream);
 
+/* ---- allocation-free pass chain ----
+ * No counterpart in the reference.  Runs num_passes (1..64) unbiased spatial
+ * passes, pass index k seeding pass k exactly as rg_spatial_unbiased does,
+ * reading `in` and leaving the last pass's reservoirs in `out`; the results
+ * equal chaining rg_spatial_unbiased through a caller-provided temporary.
+ * For callers that must not allocate device memory while a frame is
+ * recorded (fixed memory budgets, frame loops where a cudaMalloc/cudaFree
+ * would stall the device, memory owned by another framework's allocator): the
+ * intermediate reservoirs live in a 16 MiB buffer built into the library,
+ * present on every GPU that loads it until the process exits.  Frames are
+ * limited to 262144 pixels (512x512); larger ones return
+ * RG_ERR_INVALID_ARGUMENT.  The first call on a device looks up that buffer's
+ * device address, so make the first call before any stream capture.  All
+ * calls share the buffer: calls whose GPU work overlaps (other streams or
+ * host threads) race and must be serialised.  Allocates nothing. */
+int rg_spatial_unbiased_chain_noalloc(rg_context *ctx, const rg_gbuffer *gbuf, const rg_reservoir *in,
+                                      rg_reservoir *out, const rg_restir_uniforms *uniforms, int32_t num_neighbors,
+                                      int32_t num_passes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -524,3 +524,16 @@ int rg_render_frame_host(rg_context *ctx, int32_t w, int32_t h, const uint8_t *a
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- internal accessors
+// For entry points defined in other translation units (noalloc.cu): the
+// per-thread error message and the uploaded scene of a context.
+int rg_internal_fail(int code, const char *msg) { return fail(code, "%s", msg); }
+
+int rg_internal_prepare(rg_context *ctx, const DevScene **scene, int *device) {
+    const int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    *scene = &ctx->scene;
+    *device = ctx->device;
+    return RG_OK;
+}

@@ -78,3 +78,7 @@ cudaError_t upload_srgb_lut(const float *lut256);
 
 // host helpers (host_bvh.cpp, host_alias.cpp, host_gbuffer.cpp)
 void srgb_lut_host(float *out256);
+
+// capi.cu: error reporting and context access for other translation units.
+int rg_internal_fail(int code, const char *msg);
+int rg_internal_prepare(rg_context *ctx, const DevScene **scene, int *device);

@@ -130,6 +130,8 @@ _SIGNATURES = {
     "rg_frame_reservoirs": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
     "rg_render_frame_host": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p, C.POINTER(FrameParams), C.c_void_p, C.c_void_p]),
+    "rg_spatial_unbiased_chain_noalloc": (C.c_int, [C.c_void_p, C.POINTER(GBuffer), C.c_void_p, C.c_void_p,
+                                                    C.POINTER(RestirUniforms), C.c_int32, C.c_int32, C.c_void_p]),
 }
 
 EXPORTED = tuple(_SIGNATURES)
