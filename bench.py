@@ -202,6 +202,20 @@ def cpu_sample(s, gbufs: list, crop_size: int, threads: int | None = None) -> di
             "rays_in_sample": rays}
 
 
+# ------------------------------------------------------------------ ranks
+def aggregate_ranks(total_ms: float, samples: float, rays: float, dist, device: str = "cuda"):
+    """Whole-job figures over replicas: the slowest rank's time and the sum
+    of the samples and rays every rank processed (no data is exchanged)."""
+    if dist is None:
+        return float(total_ms), float(samples), float(rays)
+    import torch
+    t = torch.tensor([float(total_ms)], dtype=torch.float64, device=device)
+    u = torch.tensor([float(samples), float(rays)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t[0]), float(u[0]), float(u[1])
+
+
 # ------------------------------------------------------------------ GPU arm
 def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
     import torch
@@ -295,16 +309,7 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
             a = prev_ev if i == 0 else evs[k][i - 1]
             per_kind.setdefault(kind, []).append(a.elapsed_time(evs[k][i]))
     # first pass of step 0 starts at `start`; every later launch directly follows its predecessor
-    max_ms, units = total_ms, samples
-    if dist:
-        t = torch.tensor([total_ms, float(samples), float(st.rays_traced)], dtype=torch.float64, device="cuda")
-        tm = t.clone()
-        dist.all_reduce(tm[:1], op=dist.ReduceOp.MAX)
-        dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
-        max_ms, units = float(tm[0]), float(t[1])
-        rays_total = float(t[2])
-    else:
-        rays_total = float(st.rays_traced)
+    max_ms, units, rays_total = aggregate_ranks(total_ms, samples, st.rays_traced, dist, "cuda")
     if rank != 0:
         return None
     value = units / (max_ms / 1000.0)
