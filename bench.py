@@ -344,6 +344,11 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
                    "parallelism": f"replicas x{world}"},
         "mrays_per_s": mrays,
         "rays_per_step": rays_total / args.steps / world,
+        "traversal": {"node_visits_per_ray": round(st.node_visits / max(st.rays_traced, 1), 2),
+                      "triangle_tests_per_ray": round(st.triangle_tests / max(st.rays_traced, 1), 2),
+                      "tree_bytes_per_ray": round((64 * st.node_visits + 48 * st.triangle_tests)
+                                                  / max(st.rays_traced, 1), 1),
+                      "note": "a node visit fetches 64 B (both child boxes), a triangle test 48 B"},
         "passes_ms_mean": {k: round(sum(v) / len(v), 4) for k, v in per_kind.items()},
         "roofline": roofline,
         "gpu_launches": len(kinds) * args.steps,

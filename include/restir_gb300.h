@@ -176,6 +176,8 @@ typedef struct rg_frame_params {
 typedef struct rg_stats {
     uint64_t rays_traced;            /* shadow segments traced since the last reset */
     uint64_t traversal_errors;       /* traversals that hit the iteration limit */
+    uint64_t node_visits;            /* tree nodes visited by those segments */
+    uint64_t triangle_tests;         /* triangle tests made by those segments */
 } rg_stats;
 
 /* ---- context ---- */

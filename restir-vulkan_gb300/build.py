@@ -34,9 +34,9 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
-def _compile(src: str, verbose: bool) -> Path:
-    obj = BUILD / (src + ".o")
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(CSRC / src), "-o", str(obj)]
+def _compile(src: str, verbose: bool, build_dir: Path, extra: list) -> Path:
+    obj = build_dir / (src + ".o")
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", str(CSRC / src), "-o", str(obj)]
     if verbose:
         cmd += ["-Xptxas", "-v"]
     res = subprocess.run(cmd, capture_output=True, text=True)
@@ -47,22 +47,28 @@ def _compile(src: str, verbose: bool) -> Path:
     return obj
 
 
-def build(force: bool = False, verbose: bool = False) -> Path:
+def build(force: bool = False, verbose: bool = False, out: Path | None = None, extra_flags: list | None = None) -> Path:
+    """Compiles and links the library; `out` and `extra_flags` (e.g. -D tuning
+    constants) build an alternative copy elsewhere."""
+    out = Path(out) if out else OUT
+    extra = list(extra_flags or [])
     deps = [CSRC / s for s in SOURCES] + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh"))
     deps.append(HERE.parent / "include" / "restir_gb300.h")
-    if not force and OUT.exists() and all(OUT.stat().st_mtime >= d.stat().st_mtime for d in deps):
-        return OUT
-    BUILD.mkdir(exist_ok=True)
+    if not force and not extra and out.exists() and all(out.stat().st_mtime >= d.stat().st_mtime for d in deps):
+        return out
+    build_dir = BUILD if out == OUT else out.parent / "_build"
+    build_dir.mkdir(parents=True, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
-    tmp = OUT.with_suffix(".so.tmp")
+        objs = list(ex.map(lambda s: _compile(s, verbose, build_dir, extra), SOURCES))
+    OUT_ = out
+    tmp = OUT_.with_suffix(".so.tmp")
     cmd = [nvcc(), *ARCH, "-shared", "-Xcompiler", "-fopenmp", "-o", str(tmp), *map(str, objs), "-lcudart_static",
            "-lrt", "-lpthread", "-ldl"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
-    os.replace(tmp, OUT)
-    return OUT
+    os.replace(tmp, OUT_)
+    return OUT_
 
 
 if __name__ == "__main__":

@@ -149,8 +149,8 @@ int rg_create(int32_t device, rg_context **out) {
     float lut[256];
     srgb_lut_host(lut);
     e = upload_srgb_lut(lut);
-    if (e == cudaSuccess) e = dev_alloc(&ctx->counters, 2);
-    if (e == cudaSuccess) e = cudaMemset(ctx->counters, 0, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = dev_alloc(&ctx->counters, 4);
+    if (e == cudaSuccess) e = cudaMemset(ctx->counters, 0, 4 * sizeof(unsigned long long));
     if (e != cudaSuccess) {
         dev_free(ctx->counters);
         delete ctx;
@@ -174,11 +174,13 @@ int rg_get_stats(rg_context *ctx, rg_stats *out, int32_t reset) {
     int rc = check_ctx(ctx, false);
     if (rc) return rc;
     if (!out) return fail(RG_ERR_INVALID_ARGUMENT, "null stats");
-    unsigned long long c[2];
+    unsigned long long c[4];
     RG_CUDA(cudaDeviceSynchronize(), "rg_get_stats");
     RG_CUDA(cudaMemcpy(c, ctx->counters, sizeof(c), cudaMemcpyDeviceToHost), "rg_get_stats");
     out->rays_traced = c[0];
     out->traversal_errors = c[1];
+    out->node_visits = c[2];
+    out->triangle_tests = c[3];
     if (reset) RG_CUDA(cudaMemset(ctx->counters, 0, sizeof(c)), "rg_get_stats");
     return RG_OK;
 }

@@ -133,11 +133,19 @@ __device__ __forceinline__ void combine_res(Res &self, const Res &other, float p
 __device__ __forceinline__ f3 xyz(float4 v) { return mk(v.x, v.y, v.z); }
 
 // ---------------------------------------------------------------- shadow rays
-__device__ __forceinline__ void count_block_rays(const DevScene &s, int rays, bool err) {
-    // one atomic per block for the ray count, one per erring warp
-    const unsigned errs = __ballot_sync(0xffffffffu, err);
+// Adds a block's ray count (passed by one thread) and its lanes' traversal
+// counters to the context's counters: one atomic per warp and counter.
+__device__ __forceinline__ void count_block_rays(const DevScene &s, int rays, const rgpool::TraceStats &ts) {
+    constexpr unsigned kFull = 0xffffffffu;
+    const unsigned errs = __popc(__ballot_sync(kFull, ts.err));
+    const unsigned visits = __reduce_add_sync(kFull, ts.visits);
+    const unsigned tris = __reduce_add_sync(kFull, ts.tri_tests);
     const int tid = threadIdx.x + threadIdx.y * blockDim.x;
-    if ((tid & 31) == 0 && errs) atomicAdd(&s.counters[1], (unsigned long long)__popc(errs));
+    if ((tid & 31) == 0) {
+        if (errs) atomicAdd(&s.counters[1], (unsigned long long)errs);
+        if (visits) atomicAdd(&s.counters[2], (unsigned long long)visits);
+        if (tris) atomicAdd(&s.counters[3], (unsigned long long)tris);
+    }
     if (tid == 0 && rays) atomicAdd(&s.counters[0], (unsigned long long)rays);
 }
 
@@ -147,6 +155,12 @@ __device__ __forceinline__ void count_block_rays(const DevScene &s, int rays, bo
 //      registers, the visibility-reuse segment goes to the block's ray pool;
 //   2. the block traces its pool (trace_pool);
 //   3. per pixel: visibility reuse, then temporal reuse, final store.
+// Shared-memory carveout hint (percent of the unified L1/shared storage) for
+// the ray-tracing kernels; -1 leaves the driver's choice.
+#ifndef RG_SMEM_CARVEOUT
+#define RG_SMEM_CARVEOUT -1
+#endif
+
 constexpr int kRisPpt = 4;
 constexpr int kRisTile = 128 * kRisPpt;
 
@@ -202,7 +216,10 @@ __device__ __forceinline__ Res ris(const DevScene &s, const Texel &t, float albe
     return r;
 }
 
-__global__ void __launch_bounds__(128) k_initial_temporal(const InitialParams p) {
+#ifndef RG_RIS_MIN_BLOCKS
+#define RG_RIS_MIN_BLOCKS 8
+#endif
+__global__ void __launch_bounds__(128, RG_RIS_MIN_BLOCKS) k_initial_temporal(const InitialParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     rgpool::Ray *pool = reinterpret_cast<rgpool::Ray *>(smem);
     float4 *endp = reinterpret_cast<float4 *>(pool + kRisTile);  // sample position per pixel slot
@@ -248,9 +265,9 @@ __global__ void __launch_bounds__(128) k_initial_temporal(const InitialParams p)
         if (want) rgpool::put_ray(pool, slot, wpos, j * 128 + tid);
     }
     __syncthreads();
-    bool err = false;
+    rgpool::TraceStats ts;
     rgpool::trace_pool(
-        s, pool, s_count, &s_next, stack, s.depth, err,
+        s, pool, s_count, &s_next, stack, s.depth, ts,
         [&](int owner) { const float4 e = endp[owner]; return mk(e.x, e.y, e.z); },
         [&](int owner, bool hit) { shadow[owner] = hit ? 1 : 0; });
     __syncthreads();
@@ -301,7 +318,7 @@ __global__ void __launch_bounds__(128) k_initial_temporal(const InitialParams p)
         }
         store_res(p.out, i, r);
     }
-    count_block_rays(s, tid == 0 ? s_count : 0, err);
+    count_block_rays(s, tid == 0 ? s_count : 0, ts);
 }
 
 // ---------------------------------------------------------------- biased spatial (spatialReuse.comp:30-86)
@@ -371,7 +388,10 @@ __host__ __device__ inline size_t unbiased_smem_bytes(int K, int depth) {
     return b;
 }
 
-__global__ void __launch_bounds__(128) k_spatial_unbiased(const SpatialParams p) {
+#ifndef RG_UNBIASED_MIN_BLOCKS
+#define RG_UNBIASED_MIN_BLOCKS 8
+#endif
+__global__ void __launch_bounds__(128, RG_UNBIASED_MIN_BLOCKS) k_spatial_unbiased(const SpatialParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int K = p.num_neighbors;
     const int slots = K + 1;
@@ -447,9 +467,9 @@ __global__ void __launch_bounds__(128) k_spatial_unbiased(const SpatialParams p)
         if (want) rgpool::put_ray(pool, slot, wpos, K * 128 + tid);
     }
     __syncthreads();
-    bool err = false;
+    rgpool::TraceStats ts;
     rgpool::trace_pool(
-        s, pool, s_count, &s_next, stack, s.depth, err,
+        s, pool, s_count, &s_next, stack, s.depth, ts,
         [&](int owner) { const float4 e = endp[owner & 127]; return mk(e.x, e.y, e.z); },
         [&](int owner, bool hit) { if (hit) flag[owner] = 1; });
     __syncthreads();
@@ -467,7 +487,7 @@ __global__ void __launch_bounds__(128) k_spatial_unbiased(const SpatialParams p)
         }
         store_res(p.out, i, r);
     }
-    count_block_rays(s, tid == 0 ? s_count : 0, err);
+    count_block_rays(s, tid == 0 ? s_count : 0, ts);
 }
 
 // ---------------------------------------------------------------- shading (lighting.frag:43-71,103)
@@ -533,12 +553,12 @@ __global__ void __launch_bounds__(128) k_visibility_batch(const DevScene s, cons
         endp[k] = b;
     }
     __syncthreads();
-    bool err = false;
+    rgpool::TraceStats ts;
     rgpool::trace_pool(
-        s, pool, count, &s_next, stack, s.depth, err,
+        s, pool, count, &s_next, stack, s.depth, ts,
         [&](int owner) { const float4 e = endp[owner]; return mk(e.x, e.y, e.z); },
         [&](int owner, bool hit) { out[base + owner] = hit ? 1 : 0; });
-    count_block_rays(s, tid == 0 ? count : 0, err);
+    count_block_rays(s, tid == 0 ? count : 0, ts);
 }
 
 dim3 pixel_grid(int w, int h, dim3 block) {
@@ -572,7 +592,7 @@ cudaError_t launch_initial_temporal(const DevScene &s, const GBufView &cur, cons
     p.u = u;
     const dim3 block(32, 4);
     const dim3 grid((u.screen_size[0] + 31u) / 32u, (u.screen_size[1] + 4u * kRisPpt - 1u) / (4u * kRisPpt));
-    const size_t smem = kRisTile * (sizeof(rgpool::Ray) + sizeof(float4) + 1) + 128 * (size_t)s.depth * sizeof(int);
+    const size_t smem = kRisTile * (sizeof(rgpool::Ray) + sizeof(float4) + 1) + 128 * (size_t)(RG_STACK_LOCAL ? 0 : s.depth) * sizeof(int);
     cudaError_t e = cudaFuncSetAttribute(k_initial_temporal, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k_initial_temporal<<<grid, block, smem, st>>>(p);
@@ -608,9 +628,13 @@ cudaError_t launch_spatial_unbiased(const DevScene &s, const GBufView &g, const 
     p.num_neighbors = num_neighbors;
     p.cos_thr = 0.0f;
     const dim3 block(32, 4);
-    const size_t smem = unbiased_smem_bytes(num_neighbors, s.depth);
+    const size_t smem = unbiased_smem_bytes(num_neighbors, RG_STACK_LOCAL ? 0 : s.depth);
     cudaError_t e = cudaFuncSetAttribute(k_spatial_unbiased, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    if (RG_SMEM_CARVEOUT >= 0) {
+        e = cudaFuncSetAttribute(k_spatial_unbiased, cudaFuncAttributePreferredSharedMemoryCarveout, RG_SMEM_CARVEOUT);
+        if (e != cudaSuccess) return e;
+    }
     k_spatial_unbiased<<<pixel_grid((int)u.screen_size[0], (int)u.screen_size[1], block), block, smem, st>>>(p);
     return cudaGetLastError();
 }
@@ -631,7 +655,7 @@ cudaError_t launch_shade(const DevScene &s, const GBufView &g, const rg_reservoi
 cudaError_t launch_visibility_batch(const DevScene &s, const float4 *p1, const float4 *p2, uint8_t *out, int n,
                                     cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    const size_t smem = kVisChunk * (sizeof(rgpool::Ray) + sizeof(float4)) + 128 * (size_t)s.depth * sizeof(int);
+    const size_t smem = kVisChunk * (sizeof(rgpool::Ray) + sizeof(float4)) + 128 * (size_t)(RG_STACK_LOCAL ? 0 : s.depth) * sizeof(int);
     cudaError_t e = cudaFuncSetAttribute(k_visibility_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k_visibility_batch<<<(unsigned)((n + kVisChunk - 1) / kVisChunk), 128, smem, st>>>(s, p1, p2, out, n);

@@ -115,79 +115,164 @@ __device__ __forceinline__ bool tri_hit(const GTri *tris, int t, f3 o, f3 d) {
     return rgm::ray_tri(mk(a.x, a.y, a.z), mk(a.w, b.x, b.y), mk(b.z, b.w, c.x), o, d);
 }
 
-// Traces pool[0..n) with all threads of the block; writes shadowed (1) /
+// Lanes of a warp share one loop and each pass through it does one warp-wide
+// step: refill idle lanes with new segments (once at least RG_FETCH_MIN of
+// them are idle, or the whole warp is), test deferred triangles (once at
+// least RG_LEAF_MIN lanes hold some, or no lane can walk on), or visit one
+// tree node per walking lane.  A node whose hit children are leaves parks
+// them (two slots) instead of testing them at once, so triangle tests and
+// ray set-up run with many lanes active rather than one or two.
+#ifndef RG_FETCH_MIN
+#define RG_FETCH_MIN 4
+#endif
+#ifndef RG_LEAF_MIN
+#define RG_LEAF_MIN 4
+#endif
+
+// RG_STACK_LOCAL: keep each lane's traversal stack in local memory (cached
+// in L1 only while in use) instead of a reserved slice of shared memory.
+#ifndef RG_STACK_LOCAL
+#define RG_STACK_LOCAL 1
+#endif
+
+// Per-lane traversal counters, reduced per warp into the context's counters.
+struct TraceStats {
+    bool err = false;        // walk exceeded one visit per node or the stack (malformed tree)
+    unsigned visits = 0;     // tree nodes visited
+    unsigned tri_tests = 0;  // triangle tests
+};
+
+// Traces pool[0..n) with all threads of the block; reports shadowed (1) /
 // unoccluded (0) through `emit(owner, shadowed)`.  `stack` points at
-// blockDim.x * depth ints of shared memory.  Sets *err on a walk longer than
-// one visit per node or a stack overflow (malformed tree; not reachable for
-// trees validated at upload).  Must be called by every thread of the block.
+// blockDim.x * blockDim.y * depth ints of shared memory.  Sets ts.err on a
+// walk longer than one visit per node or a stack overflow (malformed tree;
+// not reachable for trees validated at upload).  Every thread of the block
+// must call it, and the block size must be a multiple of 32.
 template <typename Endpoint, typename Emit>
-__device__ void trace_pool(const DevScene &s, const Ray *pool, int n, int *next, int *stack, int depth, bool &err,
-                           Endpoint endpoint, Emit emit) {
+__device__ void trace_pool(const DevScene &s, const Ray *pool, int n, int *next, int *stack, int depth,
+                           TraceStats &ts, Endpoint endpoint, Emit emit) {
+    constexpr unsigned kFull = 0xffffffffu;
     const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+#if RG_STACK_LOCAL
+    int local_stack[RG_MAX_TREE_DEPTH + 1];
+    int *my_stack = local_stack;
+    const int nthreads = 1;
+    (void)stack;
+#else
     const int nthreads = blockDim.x * blockDim.y;
     int *my_stack = stack + tid;
-    int cur = -1, owner = 0, node = 0, sp = 0, visits = 0;
-    f3 o = mk(0.f, 0.f, 0.f), d = mk(0.f, 0.f, 0.f), inv = o;
+#endif
+    int cur = -1;          // pool index of this lane's segment, -1: none
+    bool retired = false;  // the pool has no segment left for this lane
+    int owner = 0, node = 0, sp = 0, visits = 0;
+    int leaf0 = -1, leaf1 = -1;  // parked triangle tests
+    bool walked = false;         // tree walk finished, only parked triangles remain
+    f3 o = mk(0.f, 0.f, 0.f), d = o, inv = o;
     bool fast = true;
     while (true) {
-        if (cur < 0) {
-            cur = atomicAdd(next, 1);
-            if (cur >= n) break;
-            const float4 a = pool[cur].a;
-            owner = __float_as_int(a.w);
-            rgm::shadow_segment(mk(a.x, a.y, a.z), endpoint(owner), o, d);
-            fast = ray_inverse(d, inv);
-            node = 0;
-            sp = 0;
-            visits = 0;
-            if (s.n_nodes <= 0) {  // single-triangle scene: no tree
-                emit(owner, s.n_tris > 0 && tri_hit(s.tris, 0, o, d));
+        // 1. refill idle lanes, several at a time
+        const bool idle = !retired && cur < 0;
+        const unsigned m_idle = __ballot_sync(kFull, idle);
+        const unsigned m_busy = __ballot_sync(kFull, cur >= 0);
+        if (m_idle != 0u && (__popc(m_idle) >= RG_FETCH_MIN || m_busy == 0u)) {
+            if (idle) {
+                const int k = atomicAdd(next, 1);
+                if (k >= n) {
+                    retired = true;
+                } else {
+                    cur = k;
+                    const float4 a = pool[k].a;
+                    owner = __float_as_int(a.w);
+                    rgm::shadow_segment(mk(a.x, a.y, a.z), endpoint(owner), o, d);
+                    fast = ray_inverse(d, inv);
+                    node = 0;
+                    sp = 0;
+                    visits = 0;
+                    leaf0 = leaf1 = -1;
+                    walked = false;
+                    if (s.n_nodes <= 0) {  // single-triangle scene: no tree
+                        leaf0 = s.n_tris > 0 ? 0 : -1;
+                        walked = true;
+                        if (leaf0 < 0) { emit(owner, false); cur = -1; }
+                    }
+                }
+            }
+        }
+        if (__all_sync(kFull, retired)) break;
+        // 2. parked triangle tests
+        const bool has_leaf = cur >= 0 && leaf0 >= 0;
+        const unsigned m_leaf = __ballot_sync(kFull, has_leaf);
+        const unsigned m_walk = __ballot_sync(kFull, cur >= 0 && leaf0 < 0 && !walked);
+        if (m_leaf != 0u && (__popc(m_leaf) >= RG_LEAF_MIN || m_walk == 0u)) {
+            if (has_leaf) {
+                bool hit = tri_hit(s.tris, leaf0, o, d);
+                ++ts.tri_tests;
+                if (!hit && leaf1 >= 0) {
+                    hit = tri_hit(s.tris, leaf1, o, d);
+                    ++ts.tri_tests;
+                }
+                leaf0 = leaf1 = -1;
+                if (hit || walked) {
+                    emit(owner, hit);
+                    cur = -1;
+                }
+            }
+            continue;
+        }
+        // 3. one node per walking lane
+        if (cur >= 0 && leaf0 < 0 && !walked) {
+            ++ts.visits;
+            if (++visits > s.n_nodes) {
+                ts.err = true;
+                emit(owner, false);
                 cur = -1;
                 continue;
             }
-        }
-        bool done = false, hit = false;
-        if (++visits > s.n_nodes) {
-            err = true;
-            done = true;
-        } else {
             const GNode *np = s.nodes + node;
             const float4 na = __ldg(&np->a), nb = __ldg(&np->b), nc = __ldg(&np->c);
             const int4 ch = __ldg(&np->d);
             float tl, tr;
             const f3 lmin = mk(na.x, na.y, na.z), lmax = mk(na.w, nb.x, nb.y);
             const f3 rmin = mk(nb.z, nb.w, nc.x), rmax = mk(nc.y, nc.z, nc.w);
+            // both filtered tests first (independent, so they overlap), then
+            // the rare exact retests
             int fl = fast ? box_filtered(o, inv, lmin, lmax, tl) : -1;
             int fr = fast ? box_filtered(o, inv, rmin, rmax, tr) : -1;
             if (fl < 0) fl = box_hit(o, d, lmin, lmax, tl) ? 1 : 0;
             if (fr < 0) fr = box_hit(o, d, rmin, rmax, tr) ? 1 : 0;
             const bool hl = fl != 0, hr = fr != 0;
-            if (hl && ch.x < 0 && tri_hit(s.tris, ~ch.x, o, d)) hit = true;
-            else if (hr && ch.y < 0 && tri_hit(s.tris, ~ch.y, o, d)) hit = true;
-            if (hit) {
-                done = true;
+            if (hl && ch.x < 0) leaf0 = ~ch.x;
+            if (hr && ch.y < 0) {
+                if (leaf0 < 0) leaf0 = ~ch.y;
+                else leaf1 = ~ch.y;
+            }
+            const bool il = hl && ch.x >= 0, ir = hr && ch.y >= 0;
+            if (il && ir) {
+                const bool left_first = !(tr < tl);
+                node = left_first ? ch.x : ch.y;
+                if (sp >= depth) {
+                    ts.err = true;
+                    emit(owner, false);
+                    cur = -1;
+                    leaf0 = leaf1 = -1;
+                    continue;
+                }
+                my_stack[sp * nthreads] = left_first ? ch.y : ch.x;
+                ++sp;
+            } else if (il) {
+                node = ch.x;
+            } else if (ir) {
+                node = ch.y;
+            } else if (sp > 0) {
+                --sp;
+                node = my_stack[sp * nthreads];
             } else {
-                const bool il = hl && ch.x >= 0, ir = hr && ch.y >= 0;
-                if (il && ir) {
-                    const bool left_first = !(tr < tl);
-                    node = left_first ? ch.x : ch.y;
-                    if (sp >= depth) { err = true; done = true; }
-                    else { my_stack[sp * nthreads] = left_first ? ch.y : ch.x; ++sp; }
-                } else if (il) {
-                    node = ch.x;
-                } else if (ir) {
-                    node = ch.y;
-                } else if (sp > 0) {
-                    --sp;
-                    node = my_stack[sp * nthreads];
-                } else {
-                    done = true;
+                walked = true;
+                if (leaf0 < 0) {
+                    emit(owner, false);
+                    cur = -1;
                 }
             }
-        }
-        if (done) {
-            emit(owner, hit);
-            cur = -1;
         }
     }
 }

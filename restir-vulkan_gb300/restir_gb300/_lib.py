@@ -8,12 +8,15 @@ fallback implementation.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
 import numpy as np
 
 PKG_ROOT = Path(__file__).resolve().parent.parent
-LIB_PATH = PKG_ROOT / "librestir_gb300.so"
+# RESTIR_GB300_LIB selects another build of the library (e.g. one compiled
+# with different tuning constants); the default is the in-tree build.
+LIB_PATH = Path(os.environ.get("RESTIR_GB300_LIB", str(PKG_ROOT / "librestir_gb300.so")))
 
 RG_OK = 0
 RG_FLAG_VISIBILITY_REUSE = 1
@@ -75,7 +78,8 @@ class FrameParams(C.Structure):
 
 
 class Stats(C.Structure):
-    _fields_ = [("rays_traced", C.c_uint64), ("traversal_errors", C.c_uint64)]
+    _fields_ = [("rays_traced", C.c_uint64), ("traversal_errors", C.c_uint64), ("node_visits", C.c_uint64),
+                ("triangle_tests", C.c_uint64)]
 
 
 assert C.sizeof(Reservoir) == 64 and C.sizeof(AabbTreeNode) == 80
