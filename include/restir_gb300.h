@@ -59,6 +59,11 @@ extern "C" {
 
 #define RG_FLAG_VISIBILITY_REUSE 1 /* RESTIR_VISIBILITY_REUSE_FLAG, restirStructs.glsl:37 */
 #define RG_FLAG_TEMPORAL_REUSE 2   /* RESTIR_TEMPORAL_REUSE_FLAG, restirStructs.glsl:38 */
+/* Extension (not in the reference, off by default): after the RIS candidate
+ * loop set W = sumWeights / (M * pHat), the standard RIS weight, instead of
+ * keeping the value stored when the sample was selected
+ * (reservoir.glsl:33-40 never refreshes it), which biases RIS upwards. */
+#define RG_FLAG_FINAL_RIS_WEIGHT 256
 
 /* Deepest BVH the traversal accepts: its stack holds depth+1 entries. */
 #define RG_MAX_TREE_DEPTH 63

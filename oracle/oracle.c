@@ -574,6 +574,8 @@ int or_initial_temporal(const or_scene *sc, const or_gbuffer *cur, const or_gbuf
                                          t.roughness, t.metallic);
                     add_sample(&res, lpos, ln, llum, lidx, ph, prob, &rng);
                 }
+                if ((u->flags & OR_FLAG_FINAL_RIS_WEIGHT) && res.sum_weights > 0.0f)
+                    res.w = res.sum_weights / ((float)res.m * res.p_hat);
             }
             /* visibility reuse :147-160 -- a background pixel's (zero normal) sample is
              * undefined in the reference; here it is the zero sample, for which zeroing

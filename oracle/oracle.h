@@ -80,6 +80,7 @@ typedef struct {             /* LightingPassUniforms: 96 bytes */
 
 #define OR_FLAG_VISIBILITY 1
 #define OR_FLAG_TEMPORAL 2
+#define OR_FLAG_FINAL_RIS_WEIGHT 256 /* extension: W = sumWeights / (M * pHat) after RIS */
 
 typedef struct {
     const or_node *nodes; int32_t n_nodes;

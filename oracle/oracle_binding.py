@@ -89,9 +89,12 @@ def P(a):
 
 def scene_struct(scene) -> tuple[Scene, list]:
     """Oracle view of a restir_gb300 Scene (keeps the arrays alive)."""
-    keep = [scene.nodes, scene.triangles, scene.point_lights, scene.alias]
+    tl = getattr(scene, "tri_lights", None)
+    has_tri = tl is not None and len(tl) > 0
+    keep = [scene.nodes, scene.triangles, scene.point_lights, scene.alias, tl]
     s = Scene(scene.nodes.ctypes.data, len(scene.nodes), scene.triangles.ctypes.data, len(scene.triangles),
-              scene.point_lights.ctypes.data, len(scene.point_lights), None, 0, scene.alias.ctypes.data,
+              scene.point_lights.ctypes.data if len(scene.point_lights) else None, len(scene.point_lights),
+              tl.ctypes.data if has_tri else None, len(tl) if has_tri else 0, scene.alias.ctypes.data,
               len(scene.alias))
     return s, keep
 

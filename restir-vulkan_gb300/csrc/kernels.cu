@@ -174,7 +174,7 @@ struct InitialParams {
 };
 
 __device__ __forceinline__ Res ris(const DevScene &s, const Texel &t, float albedo_lum, f3 cam, uint32_t count_c,
-                                   bool zero_normal, Pcg &rng) {
+                                   bool zero_normal, int flags, Pcg &rng) {
     Res r = empty_res();
     if (zero_normal) return r;
     const f3 wo = view_dir(cam, t.wpos);
@@ -213,6 +213,7 @@ __device__ __forceinline__ Res ris(const DevScene &s, const Texel &t, float albe
                                       pos_lum.w, t.roughness, t.metallic);
         add_sample(r, pos_lum, nrm, lidx, ph, prob, rng);
     }
+    if ((flags & RG_FLAG_FINAL_RIS_WEIGHT) && r.sum_w > 0.0f) r.w = r.sum_w / ((float)r.m * r.p_hat);
     return r;
 }
 
@@ -250,7 +251,7 @@ __global__ void __launch_bounds__(128, RG_RIS_MIN_BLOCKS) k_initial_temporal(con
             const float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
             Pcg rng = pcg_seed((uint64_t)p.u.frame, (uint64_t)((uint32_t)y * 10007u + (uint32_t)x));
             const bool zero_normal = !(dot(t.normal, t.normal) != 0.0f);
-            const Res r = ris(s, t, albedo_lum, cam, p.u.initial_light_sample_count, zero_normal, rng);
+            const Res r = ris(s, t, albedo_lum, cam, p.u.initial_light_sample_count, zero_normal, p.u.flags, rng);
             store_res(p.out, i, r);
             rng_state[j] = rng.state;
             // visibility reuse :147-160; a background pixel's (zero normal) sample is the

@@ -21,6 +21,7 @@ LIB_PATH = Path(os.environ.get("RESTIR_GB300_LIB", str(PKG_ROOT / "librestir_gb3
 RG_OK = 0
 RG_FLAG_VISIBILITY_REUSE = 1
 RG_FLAG_TEMPORAL_REUSE = 2
+RG_FLAG_FINAL_RIS_WEIGHT = 256
 RG_MAX_TREE_DEPTH = 63
 
 F4 = C.c_float * 4

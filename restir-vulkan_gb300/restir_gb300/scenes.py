@@ -55,6 +55,7 @@ class Scene:
     normal_threshold: float = 25.0
     source_pdf: str = "power"
     tree_depth: int = 0
+    tri_lights: np.ndarray | None = None  # TRI_LIGHT_DTYPE; used when point_lights is empty
     extra: dict = field(default_factory=dict)
 
     @property
@@ -67,10 +68,11 @@ class Scene:
         d.n_nodes = len(self.nodes)
         d.triangles = self.triangles.ctypes.data
         d.n_triangles = len(self.triangles)
-        d.point_lights = self.point_lights.ctypes.data
+        d.point_lights = self.point_lights.ctypes.data if len(self.point_lights) else None
         d.n_point_lights = len(self.point_lights)
-        d.tri_lights = None
-        d.n_tri_lights = 0
+        has_tri = self.tri_lights is not None and len(self.tri_lights) > 0
+        d.tri_lights = self.tri_lights.ctypes.data if has_tri else None
+        d.n_tri_lights = len(self.tri_lights) if has_tri else 0
         d.alias_table = self.alias.ctypes.data
         d.n_alias = len(self.alias)
         d.materials = self.materials.ctypes.data
@@ -328,6 +330,63 @@ def config3(seed: int = 3, width: int = 1920, height: int = 1080, grid=(64, 32, 
     cams = camera_path(rng, frames, width / height)
     return _finish("config3", tri_xyz, mats, lights, width, height, cams, uniform_pdf=False, candidates=32,
                    unbiased=True, spatial_passes=3, neighbors=5, radius=30.0, temporal=True, temporal_mult=20)
+
+
+def make_tri_lights(tri_xyz: np.ndarray, emission_rgb: np.ndarray) -> np.ndarray:
+    """triLight records as the reference collects them (src/misc.cpp:380-414):
+    normal = cross(p2-p1, p3-p1), area = |normal|, normal /= area, area *= 0.5."""
+    f = np.float32
+    t = tri_xyz.reshape(-1, 3, 3).astype(f)
+    n = np.cross(t[:, 1] - t[:, 0], t[:, 2] - t[:, 0]).astype(f)
+    area = np.sqrt((n * n).sum(1, dtype=f)).astype(f)
+    n = (n / area[:, None]).astype(f)
+    area = (area * f(0.5)).astype(f)
+    out = np.zeros(len(t), _lib.TRI_LIGHT_DTYPE)
+    for k, name in enumerate(("p1", "p2", "p3")):
+        out[name][:, :3] = t[:, k]
+        out[name][:, 3] = 1.0
+    e = emission_rgb.astype(f)
+    out["emission_lum"][:, :3] = e
+    out["emission_lum"][:, 3] = luminance_f32(e[:, 0], e[:, 1], e[:, 2])
+    out["normal_area"][:, :3] = n
+    out["normal_area"][:, 3] = area
+    return out
+
+
+def config1_triangle_lights(seed: int = 11, width: int = 128, height: int = 128, n_quads: int = 12) -> Scene:
+    """Config 1's room and cubes lit by emissive quads under the ceiling instead
+    of point lights: exercises triangle-light sampling (pickPointOnTriangle,
+    restirOmni.glsl:68-71,123-133), the alias table by luminance x area, and
+    negative light indices in shading (lighting.frag:56-58)."""
+    base = config1(seed=seed, width=width, height=height)
+    rng = np.random.default_rng(seed + 1000)
+    quads, emis = [], []
+    for _ in range(n_quads):
+        cx, cz = rng.uniform(0.15, 0.85, 2)
+        h = rng.uniform(0.02, 0.06)
+        y = 0.97
+        a, b, c, d = ([cx - h, y, cz - h], [cx + h, y, cz - h], [cx + h, y, cz + h], [cx - h, y, cz + h])
+        quads.append(np.array([a + b + c, a + c + d], np.float32))  # facing down
+        e = np.exp(rng.uniform(np.log(2.0), np.log(40.0), 3))
+        emis.append(np.repeat(e[None], 2, 0))
+    quad_xyz = np.concatenate(quads).astype(np.float32)
+    tri_xyz = np.concatenate([base.tri_xyz, quad_xyz]).astype(np.float32)
+    emis = np.concatenate(emis)
+    tl = make_tri_lights(quad_xyz, emis)
+    n_geo = len(base.tri_xyz)
+    mats = np.concatenate([base.materials, make_materials(np.clip(emis, 0, 1), np.ones(len(quad_xyz)),
+                                                          np.zeros(len(quad_xyz)))])
+    mats["albedo"][n_geo:, 3] = 255  # emissive flag (gBuffer.frag:73-79)
+    nodes, tris, depth = build_bvh(tri_xyz)
+    alias = np.zeros(len(tl), _lib.ALIAS_DTYPE)
+    _lib.check(_lib.lib().rg_build_alias_table(None, 0, tl.ctypes.data, len(tl), alias.ctypes.data))
+    # looking up from below the middle of the room, so the emitters are in view
+    cams = [CameraModel(position=np.array([0.5, 0.35, 0.2], np.float32),
+                        look_at=np.array([0.5, 0.9, 0.6], np.float32), aspect=width / height)]
+    return Scene(name="config1_triangle_lights", tri_xyz=tri_xyz, nodes=nodes, triangles=tris, materials=mats,
+                 point_lights=np.zeros(0, _lib.POINT_LIGHT_DTYPE), alias=alias, width=width, height=height,
+                 cameras=cams, tree_depth=depth, candidates=32, unbiased=False, spatial_passes=1,
+                 neighbors=5, radius=30.0, temporal=False, tri_lights=tl, source_pdf="power")
 
 
 CONFIGS = {"config1": config1, "config2": config2, "config3": config3}

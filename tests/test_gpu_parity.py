@@ -203,3 +203,49 @@ def test_render_frame_host_matches_device(ctx, cfg2_small, cuda):
         imgs_host.append(h)
     for a, b in zip(imgs_dev, imgs_host):
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_triangle_light_scene_bit_exact(ctx, cuda):
+    """Emissive-triangle lights: pickPointOnTriangle, the |cos| x area pdf, the
+    luminance x area alias table, negative light indices in shading and the
+    emissive passthrough (restirOmni.glsl:68-71,123-133; lighting.frag:56-71)."""
+    from restir_gb300 import scenes
+    from restir_gb300.passes import DeviceGBuffer, reservoirs, reservoirs_to_numpy
+    s = scenes.config1_triangle_lights()
+    g = scenes.trace_gbuffer_host(s, 0)
+    assert (g["albedo"][..., 3] == 255).any()
+    ctx.upload_scene(s)
+    dg = DeviceGBuffer.from_host(g)
+    n = s.width * s.height
+    stages, img = oracle_frame(s, 0, g, None, None)
+    u = s.uniforms(0)
+    r0, r1, r2 = reservoirs(n), reservoirs(n), reservoirs(n)
+    ctx.initial_temporal(dg, None, None, r0, u)
+    assert mismatch(reservoirs_to_numpy(r0), stages[0]) == 0
+    ctx.spatial_biased(dg, r0, r1, u, 0)
+    ctx.spatial_biased(dg, r1, r2, u, 1)
+    got = reservoirs_to_numpy(r2)
+    assert mismatch(got, stages[-1]) == 0
+    assert (got["light_index"] < 0).mean() > 0.5
+    out = cuda.zeros((s.height, s.width, 4), dtype=cuda.float32, device="cuda")
+    ctx.shade(dg, r2, s.lighting_uniforms(0), out)
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), img.view(np.uint32))
+
+
+def test_final_ris_weight_flag_bit_exact(ctx, cfg1, cuda):
+    from restir_gb300 import _lib
+    from restir_gb300.passes import reservoirs, reservoirs_to_numpy
+    s, g = cfg1
+    dg = _dev(ctx, s, g)
+    n = s.width * s.height
+    u = s.uniforms(0)
+    u.flags |= _lib.RG_FLAG_FINAL_RIS_WEIGHT
+    exp = new_res(n)
+    ob.initial_temporal(s, g, None, None, exp, u)
+    r = reservoirs(n)
+    ctx.initial_temporal(dg, None, None, r, u)
+    got = reservoirs_to_numpy(r)
+    assert mismatch(got, exp) == 0
+    ref_mode = new_res(n)
+    ob.initial_temporal(s, g, None, None, ref_mode, s.uniforms(0))
+    assert mismatch(got, ref_mode) > 0  # the flag changes W
