@@ -183,6 +183,7 @@ typedef struct rg_stats {
     uint64_t traversal_errors;       /* traversals that hit the iteration limit */
     uint64_t node_visits;            /* tree nodes visited by those segments */
     uint64_t triangle_tests;         /* triangle tests made by those segments */
+    uint64_t mma_timeouts;           /* tensor-core launches whose bounded completion wait ran out */
 } rg_stats;
 
 /* ---- context ---- */
@@ -242,6 +243,16 @@ int rg_frame_reservoirs(rg_context *ctx, int32_t frame_slot, const rg_reservoir 
 int rg_render_frame_host(rg_context *ctx, int32_t width, int32_t height, const uint8_t *albedo,
                          const uint16_t *normal, const uint16_t *material, const float *world_pos,
                          const float *depth, const rg_frame_params *params, float *rgba_out_host, void *stream);
+
+/* ---- tensor-core GEMM (used by the learned proposal's training) ----
+ * D = alpha * A . B^T, or D += alpha * A . B^T with accumulate != 0 (always
+ * atomic when k_splits > 1).  A is m x k and B is n x k, read from device
+ * memory with the given element strides of (row, k), as bf16 or, with
+ * *_fp32 != 0, as float rounded to bf16; accumulation is FP32 in tensor
+ * memory (tcgen05); D is row-major float with leading dimension ldd. */
+int rg_gemm_bf16(rg_context *ctx, const void *a, int32_t a_fp32, int64_t a_row_stride, int64_t a_k_stride, int32_t m,
+                 const void *b, int32_t b_fp32, int64_t b_row_stride, int64_t b_k_stride, int32_t n, int32_t k,
+                 float *d, int64_t ldd, int32_t accumulate, float alpha, int32_t k_splits, void *stream);
 
 /* ---- allocation-free pass chain ----
  * No counterpart in the reference.  Runs num_passes (1..64) unbiased spatial

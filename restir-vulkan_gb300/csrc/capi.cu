@@ -76,6 +76,7 @@ struct rg_context {
     rg_alias_table_column *tri_alias = nullptr;
     rg_material *materials = nullptr;
     unsigned long long *counters = nullptr;
+    int *mma_timeouts = nullptr;
     // frame driver
     int fw = 0, fh = 0;
     rg_reservoir *res[2] = {nullptr, nullptr};
@@ -151,8 +152,11 @@ int rg_create(int32_t device, rg_context **out) {
     e = upload_srgb_lut(lut);
     if (e == cudaSuccess) e = dev_alloc(&ctx->counters, 4);
     if (e == cudaSuccess) e = cudaMemset(ctx->counters, 0, 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = dev_alloc(&ctx->mma_timeouts, 1);
+    if (e == cudaSuccess) e = cudaMemset(ctx->mma_timeouts, 0, sizeof(int));
     if (e != cudaSuccess) {
         dev_free(ctx->counters);
+        dev_free(ctx->mma_timeouts);
         delete ctx;
         return cuda_fail(e, "rg_create");
     }
@@ -166,6 +170,7 @@ int rg_destroy(rg_context *ctx) {
     ctx->release_scene();
     ctx->release_frame();
     dev_free(ctx->counters);
+    dev_free(ctx->mma_timeouts);
     delete ctx;
     return RG_OK;
 }
@@ -181,6 +186,10 @@ int rg_get_stats(rg_context *ctx, rg_stats *out, int32_t reset) {
     out->traversal_errors = c[1];
     out->node_visits = c[2];
     out->triangle_tests = c[3];
+    int to = 0;
+    RG_CUDA(cudaMemcpy(&to, ctx->mma_timeouts, sizeof(int), cudaMemcpyDeviceToHost), "rg_get_stats");
+    out->mma_timeouts = (uint64_t)to;
+    if (reset) RG_CUDA(cudaMemset(ctx->mma_timeouts, 0, sizeof(int)), "rg_get_stats");
     if (reset) RG_CUDA(cudaMemset(ctx->counters, 0, sizeof(c)), "rg_get_stats");
     return RG_OK;
 }
@@ -312,6 +321,7 @@ int rg_upload_scene(rg_context *ctx, const rg_scene_desc *sc) {
     s.materials = ctx->materials;
     s.n_materials = sc->n_materials;
     s.counters = ctx->counters;
+    s.mma_timeouts = ctx->mma_timeouts;
     ctx->has_scene = true;
     return RG_OK;
 }
@@ -537,5 +547,19 @@ int rg_internal_prepare(rg_context *ctx, const DevScene **scene, int *device) {
     if (rc) return rc;
     *scene = &ctx->scene;
     *device = ctx->device;
+    return RG_OK;
+}
+
+extern "C" int rg_gemm_bf16(rg_context *ctx, const void *a, int32_t a_fp32, int64_t a_row_stride, int64_t a_k_stride,
+                            int32_t m, const void *b, int32_t b_fp32, int64_t b_row_stride, int64_t b_k_stride,
+                            int32_t n, int32_t k, float *d, int64_t ldd, int32_t accumulate, float alpha,
+                            int32_t k_splits, void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (!a || !b || !d || m <= 0 || n <= 0 || k <= 0 || ldd < n)
+        return fail(RG_ERR_INVALID_ARGUMENT, "rg_gemm_bf16: bad arguments");
+    RG_CUDA(launch_gemm_tc(a, a_fp32, a_row_stride, a_k_stride, m, b, b_fp32, b_row_stride, b_k_stride, n, k, d, ldd,
+                           accumulate, alpha, k_splits, ctx->mma_timeouts, (cudaStream_t)stream),
+            "k_gemm_tc");
     return RG_OK;
 }

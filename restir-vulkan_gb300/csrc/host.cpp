@@ -346,3 +346,95 @@ int host_trace_gbuffer(const float *nodes16, int32_t n_nodes, const float *tris1
     }
     return RG_OK;
 }
+
+// ---------------------------------------------------------------- light clusters
+// Seeded k-means (Lloyd) over light positions for the learned proposal:
+// initial centres are the lights at the first k positions of a seeded
+// Fisher-Yates shuffle (SplitMix64), assignment to the nearest centre (ties
+// to the smaller index, distances in double), centres moved to their
+// members' mean; a centre that loses all members stays where it was.
+namespace {
+inline uint64_t splitmix64(uint64_t &s) {
+    uint64_t z = (s += 0x9e3779b97f4a7c15ULL);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+}  // namespace
+
+int host_kmeans(const float *pos4, int32_t n, int32_t k, int32_t iterations, uint64_t seed, int32_t *cluster_of,
+                float *centers3) {
+    if (n <= 0 || k <= 0 || k > n) return RG_ERR_INVALID_ARGUMENT;
+    std::vector<int32_t> perm((size_t)n);
+    for (int32_t i = 0; i < n; ++i) perm[(size_t)i] = i;
+    uint64_t st = seed;
+    for (int32_t i = n - 1; i > 0; --i) {
+        const int32_t j = (int32_t)(splitmix64(st) % (uint64_t)(i + 1));
+        std::swap(perm[(size_t)i], perm[(size_t)j]);
+    }
+    std::vector<double> c((size_t)k * 3);
+    for (int32_t j = 0; j < k; ++j)
+        for (int d = 0; d < 3; ++d) c[(size_t)j * 3 + d] = pos4[(size_t)perm[(size_t)j] * 4 + d];
+    for (int it = 0; it <= iterations; ++it) {
+#pragma omp parallel for schedule(static)
+        for (int32_t i = 0; i < n; ++i) {
+            const double x = pos4[(size_t)i * 4], y = pos4[(size_t)i * 4 + 1], z = pos4[(size_t)i * 4 + 2];
+            double best = 1e300;
+            int32_t bj = 0;
+            for (int32_t j = 0; j < k; ++j) {
+                const double dx = x - c[(size_t)j * 3], dy = y - c[(size_t)j * 3 + 1], dz = z - c[(size_t)j * 3 + 2];
+                const double dd = dx * dx + dy * dy + dz * dz;
+                if (dd < best) { best = dd; bj = j; }
+            }
+            cluster_of[i] = bj;
+        }
+        if (it == iterations) break;
+        std::vector<double> sum((size_t)k * 3, 0.0);
+        std::vector<int64_t> cnt((size_t)k, 0);
+        for (int32_t i = 0; i < n; ++i) {
+            const int32_t j = cluster_of[i];
+            for (int d = 0; d < 3; ++d) sum[(size_t)j * 3 + d] += pos4[(size_t)i * 4 + d];
+            ++cnt[(size_t)j];
+        }
+        for (int32_t j = 0; j < k; ++j)
+            if (cnt[(size_t)j] > 0)
+                for (int d = 0; d < 3; ++d) c[(size_t)j * 3 + d] = sum[(size_t)j * 3 + d] / (double)cnt[(size_t)j];
+    }
+    if (centers3)
+        for (size_t i = 0; i < c.size(); ++i) centers3[i] = (float)c[i];
+    return RG_OK;
+}
+
+// Lights grouped by cluster (stable by light index), with one Vose alias
+// table per cluster over its members' luminance, laid out in grouped order:
+//   order[pos]        light at grouped position pos
+//   offset[c]         first grouped position of cluster c (offset[k] = n)
+//   col[pos]          {prob, alias grouped position, p(light|cluster) of the
+//                      column's own light, p of the alias's light}
+//   within[light]     p(light | its cluster)
+int host_cluster_tables(const rg_point_light *pl, int32_t n, const int32_t *cluster_of, int32_t k, int32_t *order,
+                        int32_t *offset, rg_alias_table_column *col, float *within) {
+    std::vector<int32_t> cnt((size_t)k + 1, 0);
+    for (int32_t i = 0; i < n; ++i) {
+        if (cluster_of[i] < 0 || cluster_of[i] >= k) return RG_ERR_INVALID_ARGUMENT;
+        ++cnt[(size_t)cluster_of[i] + 1];
+    }
+    offset[0] = 0;
+    for (int32_t c = 0; c < k; ++c) offset[c + 1] = offset[c] + cnt[(size_t)c + 1];
+    std::vector<int32_t> fill(offset, offset + k);
+    for (int32_t i = 0; i < n; ++i) order[fill[(size_t)cluster_of[i]]++] = i;
+    for (int32_t c = 0; c < k; ++c) {
+        const int32_t b = offset[c], e = offset[c + 1], m = e - b;
+        if (m <= 0) continue;
+        std::vector<rg_point_light> sub((size_t)m);
+        for (int32_t j = 0; j < m; ++j) sub[(size_t)j] = pl[order[b + j]];
+        std::vector<rg_alias_table_column> t((size_t)m);
+        host_build_alias_table(sub.data(), m, nullptr, 0, t.data());
+        for (int32_t j = 0; j < m; ++j) {
+            col[b + j] = t[(size_t)j];
+            col[b + j].alias = b + t[(size_t)j].alias;
+            within[order[b + j]] = t[(size_t)j].ori_prob;
+        }
+    }
+    return RG_OK;
+}

@@ -15,3 +15,7 @@ void srgb_lut_host(float *out256);
 int host_trace_gbuffer(const float *nodes16, int32_t n_nodes, const float *tris12, int32_t n_tris,
                        const rg_material *mats, int32_t n_mats, const rg_camera &cam, int32_t w, int32_t h,
                        uint8_t *albedo, uint16_t *normal, uint16_t *material, float *world_pos, float *depth);
+int host_kmeans(const float *pos4, int32_t n, int32_t k, int32_t iterations, uint64_t seed, int32_t *cluster_of,
+                float *centers3);
+int host_cluster_tables(const rg_point_light *pl, int32_t n, const int32_t *cluster_of, int32_t k, int32_t *order,
+                        int32_t *offset, rg_alias_table_column *col, float *within);

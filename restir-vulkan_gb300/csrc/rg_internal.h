@@ -47,7 +47,8 @@ struct DevScene {
     int32_t n_tri_lights;
     const rg_material *materials;
     int32_t n_materials;
-    unsigned long long *counters; // [0] rays traced, [1] traversal errors
+    unsigned long long *counters; // [0] rays traced, [1] traversal errors, [2] node visits, [3] triangle tests
+    int *mma_timeouts;            // tensor-core kernels whose bounded mbarrier wait ran out
 };
 
 struct GBufView {
@@ -75,6 +76,9 @@ cudaError_t launch_visibility_batch(const DevScene &s, const float4 *p1, const f
                                     cudaStream_t st);
 cudaError_t launch_trace_gbuffer(const DevScene &s, const rg_camera &cam, const rg_gbuffer_out &out, cudaStream_t st);
 cudaError_t upload_srgb_lut(const float *lut256);
+cudaError_t launch_gemm_tc(const void *a, int a_fp32, int64_t a_rs, int64_t a_ks, int m, const void *b, int b_fp32,
+                           int64_t b_rs, int64_t b_ks, int n, int k, float *d, int64_t ldd, int accumulate,
+                           float alpha, int splits, int *err, cudaStream_t st);
 
 // host helpers (host_bvh.cpp, host_alias.cpp, host_gbuffer.cpp)
 void srgb_lut_host(float *out256);

@@ -1,0 +1,134 @@
+// umma.cuh -- 5th-generation tensor-core (tcgen05) primitives for sm_103a,
+// written as inline PTX: shared-memory operand descriptors, the instruction
+// descriptor of kind::f16 (BF16 x BF16 -> FP32), tensor-memory (TMEM)
+// allocation, MMA issue, completion through an mbarrier, and TMEM loads.
+//
+// Operand layout in shared memory: the canonical K-major layout without
+// swizzling.  A matrix of R rows x K bf16 values is stored as 8x8 "core
+// matrices" (8 rows x 16 bytes, 128 contiguous bytes); the core matrix
+// holding rows 8i..8i+7 and k = 8j..8j+7 starts at
+//     i * SBO + j * LBO,  LBO = 128 bytes,  SBO = (K / 8) * 128 bytes,
+// and row r of it sits at r * 16 bytes.  One MMA consumes K = 16 (two core
+// matrices along K), so consecutive K-steps advance both descriptors'
+// start addresses by 2 * LBO = 256 bytes.
+#pragma once
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace umma {
+
+// Byte offset of element (r, k) of an R x K tile in the layout above.
+__host__ __device__ __forceinline__ uint32_t kmajor_offset(int r, int k, int K) {
+    return (uint32_t)((r >> 3) * (K >> 3) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor (tcgen05): start address, leading and
+// stride byte offsets (all >> 4), descriptor version 1 at bits 46-47,
+// base offset 0, relative LBO, layout type 0 (no swizzle).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo_bytes, uint32_t sbo_bytes) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo_bytes >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo_bytes >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1u << 46;
+    return d;
+}
+
+// Instruction descriptor, kind::f16: D = FP32 (bits 4-5 = 1), A = B = BF16
+// (bits 7-9 = 1, bits 10-12 = 1), both K-major (bits 15, 16 = 0),
+// N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+__host__ __device__ __forceinline__ uint32_t idesc_bf16_f32(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+// ---- tensor memory
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst_smem, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(dst_smem)),
+                 "r"(ncols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols));
+}
+
+// ---- MMA: D[tmem] (+)= A[smem] x B[smem]^T, issued by one thread
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                         bool accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"((uint32_t)accumulate));
+}
+// Arrive (once) on the mbarrier when all MMAs issued so far by this thread complete.
+__device__ __forceinline__ void mma_commit(uint64_t *mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_addr(mbar)));
+}
+
+// ---- fences
+__device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;"); }
+__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;"); }
+// Generic-proxy shared-memory writes become visible to the tensor core.
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// ---- mbarrier
+__device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(mbar)), "r"(count));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// Waits for the phase with parity `parity` to complete; gives up after
+// `max_polls` polls and returns false (the caller records an error).
+__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, uint32_t max_polls) {
+    const uint32_t a = smem_addr(mbar);
+    for (uint32_t i = 0; i < max_polls; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// ---- TMEM -> registers: warp w of the warpgroup reads lanes 32w..32w+31,
+// 32 consecutive 32-bit columns starting at `col`; thread t gets row 32w+t.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr_base, int warp, int col, float (&v)[32]) {
+    const uint32_t a = taddr_base + ((uint32_t)(warp * 32) << 16) + (uint32_t)col;
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(a));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Issues the K/16 MMAs of one K-chunk: A tile (M rows) and B tile (N rows)
+// in the layout above with K columns each.
+__device__ __forceinline__ void mma_chunk(uint32_t d_tmem, const void *a_tile, const void *b_tile, int K, int M, int N,
+                                          bool accumulate_first) {
+    const uint32_t sbo = (uint32_t)(K >> 3) * 128u;
+    const uint32_t a0 = smem_addr(a_tile), b0 = smem_addr(b_tile);
+    const uint32_t idesc = idesc_bf16_f32(M, N);
+    for (int ks = 0; ks < K / 16; ++ks) {
+        const uint64_t ad = smem_desc(a0 + (uint32_t)ks * 256u, 128u, sbo);
+        const uint64_t bd = smem_desc(b0 + (uint32_t)ks * 256u, 128u, sbo);
+        mma_bf16(d_tmem, ad, bd, idesc, accumulate_first || ks > 0);
+    }
+}
+
+}  // namespace umma

@@ -80,7 +80,7 @@ class FrameParams(C.Structure):
 
 class Stats(C.Structure):
     _fields_ = [("rays_traced", C.c_uint64), ("traversal_errors", C.c_uint64), ("node_visits", C.c_uint64),
-                ("triangle_tests", C.c_uint64)]
+                ("triangle_tests", C.c_uint64), ("mma_timeouts", C.c_uint64)]
 
 
 assert C.sizeof(Reservoir) == 64 and C.sizeof(AabbTreeNode) == 80
@@ -135,6 +135,9 @@ _SIGNATURES = {
     "rg_frame_reservoirs": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
     "rg_render_frame_host": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p, C.POINTER(FrameParams), C.c_void_p, C.c_void_p]),
+    "rg_gemm_bf16": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_int32, C.c_void_p,
+                               C.c_int32, C.c_int64, C.c_int64, C.c_int32, C.c_int32, C.c_void_p, C.c_int64,
+                               C.c_int32, C.c_float, C.c_int32, C.c_void_p]),
     "rg_spatial_unbiased_chain_noalloc": (C.c_int, [C.c_void_p, C.POINTER(GBuffer), C.c_void_p, C.c_void_p,
                                                     C.POINTER(RestirUniforms), C.c_int32, C.c_int32, C.c_void_p]),
 }
