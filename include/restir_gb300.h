@@ -64,6 +64,13 @@ extern "C" {
  * keeping the value stored when the sample was selected
  * (reservoir.glsl:33-40 never refreshes it), which biases RIS upwards. */
 #define RG_FLAG_FINAL_RIS_WEIGHT 256
+/* Extensions of the learned light-cluster proposal (no reference counterpart):
+ * LEARNED_PROPOSAL draws the initial RIS candidates from the context's
+ * proposal (rg_proposal_create) instead of the alias table; in
+ * rg_render_frame it also runs the proposal's inference for the frame, and
+ * LEARNED_TRAIN adds one training step on the frame's final reservoirs. */
+#define RG_FLAG_LEARNED_PROPOSAL 512
+#define RG_FLAG_LEARNED_TRAIN 1024
 
 /* Deepest BVH the traversal accepts: its stack holds depth+1 entries. */
 #define RG_MAX_TREE_DEPTH 63
@@ -272,6 +279,73 @@ int rg_gemm_bf16(rg_context *ctx, const void *a, int32_t a_fp32, int64_t a_row_s
 int rg_spatial_unbiased_chain_noalloc(rg_context *ctx, const rg_gbuffer *gbuf, const rg_reservoir *in,
                                       rg_reservoir *out, const rg_restir_uniforms *uniforms, int32_t num_neighbors,
                                       int32_t num_passes, void *stream);
+
+/* ---- learned light-cluster proposal ----
+ * No counterpart in the reference: it replaces the source pdf of the initial
+ * RIS candidates (restirOmni.glsl:73-83).  Per pixel an MLP (9 features:
+ * position in the normalisation box, normal, direction to the camera ->
+ * 3 x 64 ReLU -> one logit per light cluster; bf16 weights and activations,
+ * FP32 accumulation on the tensor cores) gives q(cluster | pixel); a candidate
+ * is a cluster c ~ q with a light l ~ p(l | c) from the cluster's alias table
+ * over luminance with probability `mix`, else a light drawn uniformly, and its
+ * source pdf is the mixture  mix * q(c(l)) * p(l | c(l)) + (1 - mix) / N.
+ * The network is trained online by Adam on the clusters of the lights that the
+ * final reservoirs hold (softmax cross-entropy).  Point-light scenes only. */
+typedef struct rg_proposal_config {
+    int32_t clusters;      /* multiple of 128, <= number of lights */
+    float mix;             /* probability of the learned branch, in (0, 1) */
+    float learning_rate;   /* Adam step size */
+    int32_t batch;         /* training pixels per frame */
+    float box_min[3];      /* feature normalisation box (scene bounds) */
+    float box_max[3];
+    uint64_t seed;         /* weight initialisation */
+} rg_proposal_config;
+
+/* One learned candidate: key >= 0 is a light drawn uniformly, key < 0 the
+ * cluster -1-key drawn from q; q = q(that cluster | pixel). */
+typedef struct rg_proposal_candidate {
+    int32_t key;
+    float q;
+} rg_proposal_candidate;
+
+/* Seeded k-means (Lloyd, `iterations` rounds, first centres a seeded shuffle)
+ * of the point lights' positions into k clusters; host only. */
+int rg_cluster_lights(const rg_point_light *lights, int32_t n, int32_t k, int32_t iterations, uint64_t seed,
+                      int32_t *cluster_of, float *centers_xyz);
+/* Parameters of the network for `clusters` clusters, packed FP32 in this
+ * order, matrices row-major with one row per input: W1 16x64 (rows 9..15 are
+ * zero), b1, W2 64x64, b2, W3 64x64, b3, W4 64xC, b4. */
+int64_t rg_proposal_param_count(int32_t clusters);
+/* Creates (or replaces) the proposal of a context whose uploaded scene has
+ * these n point lights; cluster_of[i] is the cluster of light i.  Initial
+ * weights are seeded; b4 starts at log(cluster luminance), so that the
+ * untrained proposal is close to the luminance-proportional one. */
+int rg_proposal_create(rg_context *ctx, const rg_proposal_config *config, const rg_point_light *lights, int32_t n,
+                       const int32_t *cluster_of);
+int rg_proposal_destroy(rg_context *ctx);
+/* Host copies of the FP32 parameters; set also resets Adam. */
+int rg_proposal_set_params(rg_context *ctx, const float *params, int64_t n);
+int rg_proposal_get_params(rg_context *ctx, float *params, int64_t n);
+/* Inference over every pixel for uniforms->frame: fills the candidate buffer
+ * (initial_light_sample_count <= 32 candidates per pixel) used by
+ * rg_initial_temporal with RG_FLAG_LEARNED_PROPOSAL. */
+int rg_proposal_infer(rg_context *ctx, const rg_gbuffer *gbuf, const rg_restir_uniforms *uniforms, void *stream);
+/* Device buffers of the last inference: candidates [pixels x 32] and per-pixel
+ * {log-sum-exp, most probable cluster (int bits), its probability, 0}. */
+int rg_proposal_buffers(rg_context *ctx, const rg_proposal_candidate **candidates, const float **row_stats);
+/* Gradient of the mean cross-entropy over n rows (pixel rows[i] of gbuf with
+ * target cluster targets[i], -1 = no target, counted in the mean with zero
+ * loss) w.r.t. the packed parameters, into grad (device, param_count floats);
+ * *loss_sum (host, may be null) receives the summed loss.  No update. */
+int rg_proposal_gradients(rg_context *ctx, const rg_gbuffer *gbuf, const float camera_pos[3], const int32_t *rows,
+                          const int32_t *targets, int32_t n, float *grad, double *loss_sum, void *stream);
+/* One Adam step on `batch` pixels of the frame (a strided sweep whose offset
+ * changes with uniforms->frame), targets from final_reservoirs. */
+int rg_proposal_train(rg_context *ctx, const rg_gbuffer *gbuf, const rg_restir_uniforms *uniforms,
+                      const rg_reservoir *final_reservoirs, void *stream);
+/* Mean loss over the rows with a target, and their number, of the last
+ * training step (synchronises). */
+int rg_proposal_last_loss(rg_context *ctx, double *mean_loss, int64_t *rows_with_target);
 
 #ifdef __cplusplus
 }

@@ -519,7 +519,19 @@ static int crop_ok(const int32_t *crop, int W, int H, int *x0, int *y0, int *cw,
 int or_initial_temporal(const or_scene *sc, const or_gbuffer *cur, const or_gbuffer *prev,
                         const or_reservoir *prev_res, or_reservoir *out, const or_uniforms *u,
                         const int32_t *crop, or_stats *st) {
+    return or_initial_temporal_learned(sc, cur, prev, prev_res, out, u, NULL, crop, st);
+}
+
+/* With l != NULL (point lights only), candidate i of pixel p is l->cand[p*32+i]
+ * of the learned proposal: key < 0 names a cluster whose light is drawn from
+ * the cluster's alias table with r1, r2; key >= 0 is a light; the source pdf
+ * is mix * q * p(light | cluster) + uniform_pdf.  Everything else is the
+ * reference's pass. */
+int or_initial_temporal_learned(const or_scene *sc, const or_gbuffer *cur, const or_gbuffer *prev,
+                                const or_reservoir *prev_res, or_reservoir *out, const or_uniforms *u,
+                                const or_learned *l, const int32_t *crop, or_stats *st) {
     srgb_init();
+    if (l && sc->n_point_lights == 0) return -3;
     int W = (int)u->size[0], H = (int)u->size[1];
     int x0, y0, cw, ch;
     if (W != cur->width || H != cur->height) return -1;
@@ -546,7 +558,24 @@ int or_initial_temporal(const or_scene *sc, const or_gbuffer *cur, const or_gbuf
                 for (int i = 0; (uint32_t)i < u->initial_light_sample_count; ++i) {
                     int sel; float prob;
                     float r1 = rand_float(&rng), r2 = rand_float(&rng);
-                    alias_sample(sc->alias, sc->n_alias, r1, r2, &sel, &prob);
+                    if (l) {
+                        const or_candidate cd = l->cand[((size_t)y * (size_t)W + (size_t)x) * 32 + (size_t)i];
+                        float pl;
+                        if (cd.key < 0) {
+                            const int32_t cl = -1 - cd.key;
+                            const int32_t b = l->offset[cl], m = l->offset[cl + 1] - b;
+                            const int32_t pos = b + imin((int)((float)m * r1), m - 1);
+                            const or_alias *c = &l->col[pos];
+                            if (c->prob > r2) { sel = l->order[pos]; pl = c->ori_prob; }
+                            else { sel = l->order[c->alias]; pl = c->alias_ori_prob; }
+                        } else {
+                            sel = cd.key;
+                            pl = l->within[sel];
+                        }
+                        prob = l->mix * cd.q * pl + l->uniform_pdf;
+                    } else {
+                        alias_sample(sc->alias, sc->n_alias, r1, r2, &sel, &prob);
+                    }
                     v3 lpos; or_f4 ln; float llum; int32_t lidx;
                     if (use_point) {
                         const or_point_light *L = &sc->point_lights[sel];
@@ -930,4 +959,300 @@ void or_set_threads(int32_t n) {
 #else
     (void)n;
 #endif
+}
+
+/* ------------------------------------------------------------------ learned light-cluster proposal
+ * No reference counterpart: the CPU statement of the product's learned
+ * proposal (network, sampling rule and training loss), used to check its
+ * tensor-core kernels.  Layout of the packed parameters: W1 16x64, b1, W2
+ * 64x64, b2, W3 64x64, b3, W4 64xC, b4 (matrices row-major, one row per
+ * input).  Forward: h = bf16(relu(W^T h_prev + b)) per hidden layer with bf16
+ * weights, z = W4^T h3 + b4, sums accumulated in double here (FP32 on the
+ * tensor cores). */
+#define MLP_IN 16
+#define MLP_IN_USED 9
+#define MLP_H 64
+#define MLP_CAND 32
+#define MLP_SEED_MUL 0x9E3779B97F4A7C15ULL
+#define MLP_SEED_ADD 0x2545F4914F6CDD1DULL
+
+/* round to nearest even on the upper 16 bits of the binary32 pattern */
+float or_bf16_round(float x) {
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    if ((u & 0x7f800000u) == 0x7f800000u) {
+        if (u & 0x007fffffu) u |= 0x00400000u;  /* quiet NaN */
+        u &= 0xffff0000u;
+    } else {
+        u += 0x7fffu + ((u >> 16) & 1u);
+        u &= 0xffff0000u;
+    }
+    float r;
+    memcpy(&r, &u, 4);
+    return r;
+}
+
+typedef struct { size_t w1, b1, w2, b2, w3, b3, w4, b4, total; } mlp_layout;
+static mlp_layout mlp_layout_of(int32_t c) {
+    mlp_layout L;
+    size_t o = 0;
+    L.w1 = o; o += (size_t)MLP_IN * MLP_H;
+    L.b1 = o; o += MLP_H;
+    L.w2 = o; o += (size_t)MLP_H * MLP_H;
+    L.b2 = o; o += MLP_H;
+    L.w3 = o; o += (size_t)MLP_H * MLP_H;
+    L.b3 = o; o += MLP_H;
+    L.w4 = o; o += (size_t)MLP_H * c;
+    L.b4 = o; o += (size_t)c;
+    L.total = o;
+    return L;
+}
+int64_t or_mlp_param_count(int32_t clusters) { return (int64_t)mlp_layout_of(clusters).total; }
+
+void or_mlp_features(const or_mlp *m, const or_gbuffer *g, const float cam[3], int32_t px, float x[16]) {
+    const float *p = g->world_pos + 4 * (size_t)px;
+    const uint16_t *nb = g->normal + 4 * (size_t)px;
+    const v3 wpos = V(p[0], p[1], p[2]);
+    const v3 n = V(or_half_to_float(nb[0]), or_half_to_float(nb[1]), or_half_to_float(nb[2]));
+    const v3 v = vnormalize(vsub(V(cam[0], cam[1], cam[2]), wpos));
+    float t[16] = {0};
+    t[0] = (wpos.x - m->box_center[0]) * m->box_inv_half[0];
+    t[1] = (wpos.y - m->box_center[1]) * m->box_inv_half[1];
+    t[2] = (wpos.z - m->box_center[2]) * m->box_inv_half[2];
+    t[3] = n.x; t[4] = n.y; t[5] = n.z;
+    t[6] = v.x; t[7] = v.y; t[8] = v.z;
+    for (int i = 0; i < MLP_IN; ++i) x[i] = (i < MLP_IN_USED && isfinite(t[i])) ? or_bf16_round(t[i]) : 0.0f;
+}
+
+/* weights as double: bf16-rounded (emulate) or exact */
+static void mlp_weights(const or_mlp *m, const double *p64, int emulate, double *w) {
+    const mlp_layout L = mlp_layout_of(m->clusters);
+    for (size_t i = 0; i < L.total; ++i) {
+        double v = p64 ? p64[i] : (double)m->params[i];
+        const int is_weight = (i < L.b1) || (i >= L.w2 && i < L.b2) || (i >= L.w3 && i < L.b3) ||
+                              (i >= L.w4 && i < L.b4);
+        if (emulate && is_weight) v = (double)or_bf16_round((float)v);
+        w[i] = v;
+    }
+}
+
+/* forward of one row; h* as double (bf16 values when emulating); z with -inf for empty clusters */
+static void mlp_forward_row(const or_mlp *m, const double *w, int emulate, const float *x, double *h1, double *h2,
+                            double *h3, double *z) {
+    const mlp_layout L = mlp_layout_of(m->clusters);
+    const double *layer_w[3] = {w + L.w1, w + L.w2, w + L.w3};
+    const double *layer_b[3] = {w + L.b1, w + L.b2, w + L.b3};
+    double xin[MLP_H];
+    double *outs[3] = {h1, h2, h3};
+    for (int i = 0; i < MLP_IN; ++i) xin[i] = x[i];
+    int nin = MLP_IN;
+    const double *in = xin;
+    for (int l = 0; l < 3; ++l) {
+        for (int j = 0; j < MLP_H; ++j) {
+            double acc = 0.0;
+            for (int k = 0; k < nin; ++k) acc += in[k] * layer_w[l][(size_t)k * MLP_H + j];
+            double v = acc + layer_b[l][j];
+            v = v > 0.0 ? v : 0.0;
+            outs[l][j] = emulate ? (double)or_bf16_round((float)v) : v;
+        }
+        in = outs[l];
+        nin = MLP_H;
+    }
+    for (int c = 0; c < m->clusters; ++c) {
+        if (!m->cluster_valid[c]) { z[c] = -INFINITY; continue; }
+        double acc = 0.0;
+        for (int k = 0; k < MLP_H; ++k) acc += h3[k] * w[L.w4 + (size_t)k * m->clusters + c];
+        z[c] = acc + w[L.b4 + c];
+    }
+}
+
+static double mlp_lse(const double *z, int32_t c, int32_t *amax) {
+    double mx = -INFINITY;
+    int32_t a = 0;
+    for (int32_t i = 0; i < c; ++i)
+        if (z[i] > mx) { mx = z[i]; a = i; }
+    double s = 0.0;
+    for (int32_t i = 0; i < c; ++i) s += exp(z[i] - mx);
+    if (amax) *amax = a;
+    return mx + log(s);
+}
+
+void or_mlp_row_stats(const or_mlp *m, const or_gbuffer *g, const float cam[3], int32_t n, const int32_t *rows,
+                      double *lse, int32_t *amax, double *z_out) {
+    const mlp_layout L = mlp_layout_of(m->clusters);
+    double *w = (double *)malloc(L.total * sizeof(double));
+    mlp_weights(m, NULL, 1, w);
+#pragma omp parallel
+    {
+        double *z = (double *)malloc((size_t)m->clusters * sizeof(double));
+        double h1[MLP_H], h2[MLP_H], h3[MLP_H];
+        float x[MLP_IN];
+#pragma omp for schedule(dynamic, 16)
+        for (int32_t r = 0; r < n; ++r) {
+            or_mlp_features(m, g, cam, rows ? rows[r] : r, x);
+            mlp_forward_row(m, w, 1, x, h1, h2, h3, z);
+            lse[r] = mlp_lse(z, m->clusters, amax ? amax + r : NULL);
+            if (z_out) memcpy(z_out + (size_t)r * m->clusters, z, (size_t)m->clusters * sizeof(double));
+        }
+        free(z);
+    }
+    free(w);
+}
+
+/* The proposal's candidates of pixel rows[r] (keys/q: [n x n_cand]): the
+ * same branch draws as the product (PCG stream frame*MUL+ADD, pixel), then the
+ * learned-branch uniforms placed on the double-precision softmax CDF
+ * (a uniform at or beyond the total takes the most probable cluster). */
+void or_mlp_sample(const or_mlp *m, const or_gbuffer *g, const float cam[3], uint32_t frame, int32_t n_cand,
+                   int32_t n, const int32_t *rows, int32_t *keys, float *qs) {
+    const mlp_layout L = mlp_layout_of(m->clusters);
+    double *w = (double *)malloc(L.total * sizeof(double));
+    mlp_weights(m, NULL, 1, w);
+#pragma omp parallel
+    {
+        double *z = (double *)malloc((size_t)m->clusters * sizeof(double));
+        double h1[MLP_H], h2[MLP_H], h3[MLP_H];
+        float x[MLP_IN];
+#pragma omp for schedule(dynamic, 16)
+        for (int32_t r = 0; r < n; ++r) {
+            const int32_t px = rows ? rows[r] : r;
+            or_mlp_features(m, g, cam, px, x);
+            mlp_forward_row(m, w, 1, x, h1, h2, h3, z);
+            int32_t amax = 0;
+            const double lse = mlp_lse(z, m->clusters, &amax);
+            pcg_t rng = pcg_seed((uint64_t)frame * MLP_SEED_MUL + MLP_SEED_ADD, (uint64_t)px);
+            for (int32_t j = 0; j < n_cand; ++j) {
+                const float u0 = rand_float(&rng);
+                const float u1 = rand_float(&rng);
+                int32_t key;
+                double q;
+                if (u0 < m->mix) {
+                    double cum = 0.0;
+                    key = -1 - amax;
+                    q = exp(z[amax] - lse);
+                    for (int32_t c = 0; c < m->clusters; ++c) {
+                        const double pr = exp(z[c] - lse);
+                        cum += pr;
+                        if ((double)u1 < cum) { key = -1 - c; q = pr; break; }
+                    }
+                } else {
+                    const int32_t l = imin((int)((float)m->n_lights * u1), m->n_lights - 1);
+                    key = l;
+                    q = exp(z[m->cluster_of[l]] - lse);
+                }
+                keys[(size_t)r * n_cand + j] = key;
+                qs[(size_t)r * n_cand + j] = (float)q;
+            }
+        }
+        free(z);
+    }
+    free(w);
+}
+
+/* Summed cross-entropy over the rows with a target (target -1: no loss) and
+ * its gradient divided by n, i.e. the gradient of the mean over all n rows.
+ * emulate = 1 rounds to bf16 where the product does (weights, activations,
+ * the logit gradient and the hidden pre-activation gradients entering the
+ * weight products); emulate = 0 is plain double arithmetic (params64, when
+ * given, replaces the FP32 parameters). */
+double or_mlp_loss_grad(const or_mlp *m, const double *params64, const or_gbuffer *g, const float cam[3], int32_t n,
+                        const int32_t *rows, const int32_t *target, int32_t emulate, double *grad) {
+    const mlp_layout L = mlp_layout_of(m->clusters);
+    const int32_t C = m->clusters;
+    double *w = (double *)malloc(L.total * sizeof(double));
+    mlp_weights(m, params64, emulate, w);
+    memset(grad, 0, L.total * sizeof(double));
+    double loss = 0.0;
+    const double inv_n = 1.0 / (double)n;
+    double *z = (double *)malloc((size_t)C * sizeof(double));
+    double *dz = (double *)malloc((size_t)C * sizeof(double));
+    for (int32_t r = 0; r < n; ++r) {
+        const int32_t t = target[r];
+        if (t < 0) continue;
+        float x[MLP_IN];
+        double h1[MLP_H], h2[MLP_H], h3[MLP_H];
+        or_mlp_features(m, g, cam, rows[r], x);
+        mlp_forward_row(m, w, emulate, x, h1, h2, h3, z);
+        const double lse = mlp_lse(z, C, NULL);
+        loss += lse - z[t];
+        for (int32_t c = 0; c < C; ++c) {
+            double d = (exp(z[c] - lse) - (c == t ? 1.0 : 0.0)) * inv_n;
+            if (emulate) d = (double)or_bf16_round((float)d);
+            dz[c] = d;
+        }
+        double dh3[MLP_H], da3[MLP_H], da2[MLP_H], da1[MLP_H];
+        for (int k = 0; k < MLP_H; ++k) {
+            double acc = 0.0;
+            const double *wr = w + L.w4 + (size_t)k * C;
+            double *gr = grad + L.w4 + (size_t)k * C;
+            for (int32_t c = 0; c < C; ++c) {
+                acc += dz[c] * wr[c];
+                gr[c] += h3[k] * dz[c];
+            }
+            dh3[k] = acc;
+        }
+        for (int32_t c = 0; c < C; ++c) grad[L.b4 + c] += dz[c];
+        for (int k = 0; k < MLP_H; ++k) da3[k] = h3[k] > 0.0 ? dh3[k] : 0.0;
+        for (int i = 0; i < MLP_H; ++i) {
+            double acc = 0.0;
+            for (int k = 0; k < MLP_H; ++k) acc += w[L.w3 + (size_t)i * MLP_H + k] * da3[k];
+            da2[i] = h2[i] > 0.0 ? acc : 0.0;
+        }
+        for (int i = 0; i < MLP_H; ++i) {
+            double acc = 0.0;
+            for (int k = 0; k < MLP_H; ++k) acc += w[L.w2 + (size_t)i * MLP_H + k] * da2[k];
+            da1[i] = h1[i] > 0.0 ? acc : 0.0;
+        }
+        for (int j = 0; j < MLP_H; ++j) {
+            const double r3 = emulate ? (double)or_bf16_round((float)da3[j]) : da3[j];
+            const double r2 = emulate ? (double)or_bf16_round((float)da2[j]) : da2[j];
+            const double r1 = emulate ? (double)or_bf16_round((float)da1[j]) : da1[j];
+            for (int i = 0; i < MLP_H; ++i) {
+                grad[L.w3 + (size_t)i * MLP_H + j] += h2[i] * r3;
+                grad[L.w2 + (size_t)i * MLP_H + j] += h1[i] * r2;
+            }
+            for (int i = 0; i < MLP_IN; ++i) grad[L.w1 + (size_t)i * MLP_H + j] += (double)x[i] * r1;
+            grad[L.b3 + j] += da3[j];
+            grad[L.b2 + j] += da2[j];
+            grad[L.b1 + j] += da1[j];
+        }
+    }
+    free(z);
+    free(dz);
+    free(w);
+    return loss;
+}
+
+/* Lights grouped by cluster (stable by index) with one alias table per cluster
+ * over its members (createAliasTable, src/misc.cpp:418-497, on the subset):
+ * order[pos] light at grouped position pos, offset[c] first position of
+ * cluster c (offset[k] = n), col[pos] the column with its alias as a grouped
+ * position, within[light] p(light | its cluster). */
+int or_cluster_tables(const or_point_light *pl, int32_t n, const int32_t *cluster_of, int32_t k, int32_t *order,
+                      int32_t *offset, or_alias *col, float *within) {
+    int32_t *cnt = (int32_t *)calloc((size_t)k + 1, sizeof(int32_t));
+    for (int32_t i = 0; i < n; ++i) {
+        if (cluster_of[i] < 0 || cluster_of[i] >= k) { free(cnt); return -1; }
+        ++cnt[cluster_of[i] + 1];
+    }
+    offset[0] = 0;
+    for (int32_t c = 0; c < k; ++c) offset[c + 1] = offset[c] + cnt[c + 1];
+    int32_t *fill = (int32_t *)malloc((size_t)k * sizeof(int32_t));
+    memcpy(fill, offset, (size_t)k * sizeof(int32_t));
+    for (int32_t i = 0; i < n; ++i) order[fill[cluster_of[i]]++] = i;
+    or_point_light *sub = (or_point_light *)malloc((size_t)n * sizeof(or_point_light));
+    for (int32_t c = 0; c < k; ++c) {
+        const int32_t b = offset[c], m = offset[c + 1] - b;
+        if (m <= 0) continue;
+        for (int32_t j = 0; j < m; ++j) sub[j] = pl[order[b + j]];
+        or_build_alias_table(sub, m, NULL, 0, col + b);
+        for (int32_t j = 0; j < m; ++j) {
+            col[b + j].alias += b;
+            within[order[b + j]] = col[b + j].ori_prob;
+        }
+    }
+    free(sub);
+    free(fill);
+    free(cnt);
+    return 0;
 }

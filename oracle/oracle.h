@@ -127,6 +127,17 @@ void or_alias_sample_batch(const or_alias *table, int32_t count, int32_t n, cons
 void or_build_alias_table(const or_point_light *pl, int32_t n_pl, const or_tri_light *tl, int32_t n_tl, or_alias *out);
 
 /* ---- passes; crop = {x0, y0, w, h} or NULL for the full frame; out is full-frame sized ---- */
+typedef struct { int32_t key; float q; } or_candidate;     /* learned candidate (see or_mlp below) */
+typedef struct {
+    const or_candidate *cand;   /* [pixels x 32] */
+    const int32_t *order, *offset;
+    const or_alias *col;        /* per grouped position, alias = grouped position */
+    const float *within;
+    float mix, uniform_pdf;
+} or_learned;
+int or_initial_temporal_learned(const or_scene *scene, const or_gbuffer *cur, const or_gbuffer *prev,
+                                const or_reservoir *prev_res, or_reservoir *out, const or_uniforms *u,
+                                const or_learned *learned, const int32_t *crop, or_stats *stats);
 int or_initial_temporal(const or_scene *scene, const or_gbuffer *cur, const or_gbuffer *prev,
                         const or_reservoir *prev_res, or_reservoir *out, const or_uniforms *u,
                         const int32_t *crop, or_stats *stats);
@@ -138,6 +149,29 @@ int or_shade(const or_scene *scene, const or_gbuffer *g, const or_reservoir *res
              float *rgba_out, const int32_t *crop);
 int or_brute_force_fp64(const or_scene *scene, const or_gbuffer *g, const float *camera_pos3,
                         double *rgb_out, const int32_t *crop);
+
+/* ---- learned light-cluster proposal (no reference counterpart; see oracle.c) ---- */
+typedef struct {
+    int32_t clusters;
+    float mix;                   /* probability of the learned branch */
+    int32_t n_lights;
+    float box_center[3], box_inv_half[3];
+    const float *params;         /* packed FP32 parameters */
+    const uint8_t *cluster_valid;/* 1: the cluster has lights */
+    const int32_t *cluster_of;   /* cluster of each light */
+} or_mlp;
+float or_bf16_round(float x);
+int or_cluster_tables(const or_point_light *pl, int32_t n, const int32_t *cluster_of, int32_t k, int32_t *order,
+                      int32_t *offset, or_alias *col, float *within);
+int64_t or_mlp_param_count(int32_t clusters);
+void or_mlp_features(const or_mlp *m, const or_gbuffer *g, const float cam[3], int32_t px, float x[16]);
+/* rows == NULL: row r is pixel r; z_out (optional) receives [n x clusters] logits */
+void or_mlp_row_stats(const or_mlp *m, const or_gbuffer *g, const float cam[3], int32_t n, const int32_t *rows,
+                      double *lse, int32_t *amax, double *z_out);
+void or_mlp_sample(const or_mlp *m, const or_gbuffer *g, const float cam[3], uint32_t frame, int32_t n_cand,
+                   int32_t n, const int32_t *rows, int32_t *keys, float *qs);
+double or_mlp_loss_grad(const or_mlp *m, const double *params64, const or_gbuffer *g, const float cam[3], int32_t n,
+                        const int32_t *rows, const int32_t *target, int32_t emulate, double *grad);
 
 int or_max_threads(void);
 void or_set_threads(int32_t n);

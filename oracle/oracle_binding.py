@@ -156,3 +156,106 @@ def brute_force(scene, g, camera_pos3, crop=None):
     cam = np.asarray(camera_pos3, np.float32)
     check(oracle().or_brute_force_fp64(C.byref(s), C.byref(gg), P(cam), P(out), crop_arg(crop)), "brute_force")
     return out
+
+
+# ---------------------------------------------------------------- learned proposal
+class Mlp(C.Structure):
+    _fields_ = [("clusters", C.c_int32), ("mix", C.c_float), ("n_lights", C.c_int32),
+                ("box_center", C.c_float * 3), ("box_inv_half", C.c_float * 3), ("params", C.c_void_p),
+                ("cluster_valid", C.c_void_p), ("cluster_of", C.c_void_p)]
+
+
+class OracleMlp:
+    """The oracle's statement of the learned proposal for given FP32 parameters,
+    clusters and normalisation box (the same float arithmetic as the product's
+    box centre and inverse half-extent)."""
+
+    def __init__(self, params, cluster_of, clusters, mix=0.9, box_min=(0, 0, 0), box_max=(1, 1, 1)):
+        self.params = np.ascontiguousarray(params, np.float32)
+        self.cluster_of = np.ascontiguousarray(cluster_of, np.int32)
+        self.clusters = clusters
+        self.valid = np.zeros(clusters, np.uint8)
+        self.valid[np.unique(self.cluster_of)] = 1
+        bmin, bmax = np.asarray(box_min, np.float32), np.asarray(box_max, np.float32)
+        center = np.float32(0.5) * (bmin + bmax)
+        inv_half = np.float32(2.0) / (bmax - bmin)
+        self.s = Mlp(clusters, mix, len(self.cluster_of), (C.c_float * 3)(*center), (C.c_float * 3)(*inv_half),
+                     self.params.ctypes.data, self.valid.ctypes.data, self.cluster_of.ctypes.data)
+        o = oracle()
+        o.or_mlp_loss_grad.restype = C.c_double
+        o.or_bf16_round.restype = C.c_float
+        o.or_bf16_round.argtypes = [C.c_float]
+
+    def set_params(self, params):
+        self.params = np.ascontiguousarray(params, np.float32)
+        self.s.params = self.params.ctypes.data
+
+    def row_stats(self, g, cam, rows=None, logits=False):
+        gg = gbuffer_struct(g)
+        n = len(rows) if rows is not None else g["depth"].size
+        rows_a = None if rows is None else np.ascontiguousarray(rows, np.int32)
+        lse = np.zeros(n, np.float64)
+        amax = np.zeros(n, np.int32)
+        z = np.zeros((n, self.clusters), np.float64) if logits else None
+        cam_a = np.asarray(cam, np.float32)
+        oracle().or_mlp_row_stats(C.byref(self.s), C.byref(gg), P(cam_a), C.c_int32(n), P(rows_a), P(lse), P(amax),
+                                  P(z))
+        return (lse, amax, z) if logits else (lse, amax)
+
+    def sample(self, g, cam, frame, n_cand, rows):
+        gg = gbuffer_struct(g)
+        rows_a = np.ascontiguousarray(rows, np.int32)
+        n = len(rows_a)
+        keys = np.zeros((n, n_cand), np.int32)
+        qs = np.zeros((n, n_cand), np.float32)
+        cam_a = np.asarray(cam, np.float32)
+        oracle().or_mlp_sample(C.byref(self.s), C.byref(gg), P(cam_a), C.c_uint32(frame), C.c_int32(n_cand),
+                               C.c_int32(n), P(rows_a), P(keys), P(qs))
+        return keys, qs
+
+    def loss_grad(self, g, cam, rows, targets, emulate=True, params64=None):
+        gg = gbuffer_struct(g)
+        rows_a = np.ascontiguousarray(rows, np.int32)
+        tg = np.ascontiguousarray(targets, np.int32)
+        grad = np.zeros(len(self.params), np.float64)
+        p64 = None if params64 is None else np.ascontiguousarray(params64, np.float64)
+        cam_a = np.asarray(cam, np.float32)
+        loss = oracle().or_mlp_loss_grad(C.byref(self.s), P(p64), C.byref(gg), P(cam_a), C.c_int32(len(rows_a)),
+                                         P(rows_a), P(tg), C.c_int32(1 if emulate else 0), P(grad))
+        return loss, grad
+
+
+class Learned(C.Structure):
+    _fields_ = [("cand", C.c_void_p), ("order", C.c_void_p), ("offset", C.c_void_p), ("col", C.c_void_p),
+                ("within", C.c_void_p), ("mix", C.c_float), ("uniform_pdf", C.c_float)]
+
+
+def cluster_tables(point_lights, cluster_of, clusters):
+    """(order, offset, col, within) of the oracle's per-cluster alias tables."""
+    n = len(point_lights)
+    order = np.zeros(n, np.int32)
+    offset = np.zeros(clusters + 1, np.int32)
+    col = np.zeros(n, np.dtype([("prob", "<f4"), ("alias", "<i4"), ("ori_prob", "<f4"), ("alias_ori_prob", "<f4")]))
+    within = np.zeros(n, np.float32)
+    co = np.ascontiguousarray(cluster_of, np.int32)
+    check(oracle().or_cluster_tables(P(point_lights), C.c_int32(n), P(co), C.c_int32(clusters), P(order), P(offset),
+                                     P(col), P(within)), "cluster_tables")
+    return order, offset, col, within
+
+
+def initial_temporal_learned(scene, g_cur, g_prev, prev_res, out, uniforms, candidates, cluster_of, clusters,
+                             mix=0.9, crop=None, stats=None):
+    """The pass with the learned proposal's candidates (structured array with
+    fields key, q; 32 per pixel) as the candidate source."""
+    s, keep = scene_struct(scene)
+    gc = gbuffer_struct(g_cur)
+    gp = gbuffer_struct(g_prev) if g_prev is not None else None
+    order, offset, col, within = cluster_tables(scene.point_lights, cluster_of, clusters)
+    cand = np.ascontiguousarray(candidates)
+    upd = np.float32(np.float32(1.0) - np.float32(mix)) / np.float32(len(scene.point_lights))
+    lrn = Learned(cand.ctypes.data, order.ctypes.data, offset.ctypes.data, col.ctypes.data, within.ctypes.data,
+                  mix, float(upd))
+    check(oracle().or_initial_temporal_learned(C.byref(s), C.byref(gc), C.byref(gp) if gp else None, P(prev_res),
+                                               P(out), C.byref(uniforms), C.byref(lrn), crop_arg(crop),
+                                               C.byref(stats) if stats else None),
+          "initial_temporal_learned")

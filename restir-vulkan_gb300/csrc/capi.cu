@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "host_internal.h"
+#include "mlp.cuh"
 #include "rg_internal.h"
 
 namespace {
@@ -77,6 +78,7 @@ struct rg_context {
     rg_material *materials = nullptr;
     unsigned long long *counters = nullptr;
     int *mma_timeouts = nullptr;
+    ProposalState *proposal = nullptr;  // learned proposal (proposal.cu), tied to the uploaded lights
     // frame driver
     int fw = 0, fh = 0;
     rg_reservoir *res[2] = {nullptr, nullptr};
@@ -86,6 +88,8 @@ struct rg_context {
     bool gslot_valid[2] = {false, false};
 
     void release_scene() {
+        proposal_release(proposal);
+        proposal = nullptr;
         dev_free(nodes); dev_free(tris); dev_free(alias); dev_free(pl_color); dev_free(tri_lights);
         dev_free(tri_alias); dev_free(materials);
         has_scene = false;
@@ -330,6 +334,11 @@ int rg_initial_temporal(rg_context *ctx, const rg_gbuffer *cur, const rg_gbuffer
                         const rg_reservoir *prev_res, rg_reservoir *out, const rg_restir_uniforms *u, void *stream) {
     int rc = check_ctx(ctx, true);
     if (rc) return rc;
+    mlp::LearnedRis learned{};
+    if (u && (u->flags & RG_FLAG_LEARNED_PROPOSAL) &&
+        (rc = proposal_learned_ris(ctx->proposal, (int)u->screen_size[0], (int)u->screen_size[1], u->frame,
+                                   u->initial_light_sample_count, &learned)))
+        return rc;
     if (!u) return fail(RG_ERR_INVALID_ARGUMENT, "null uniforms");
     if ((rc = check_size(u->screen_size[0], u->screen_size[1]))) return rc;
     if ((rc = check_gbuffer(cur, u->screen_size[0], u->screen_size[1], "current G-buffer"))) return rc;
@@ -343,7 +352,7 @@ int rg_initial_temporal(rg_context *ctx, const rg_gbuffer *cur, const rg_gbuffer
     }
     const GBufView cv = make_view(cur);
     RG_CUDA(launch_initial_temporal(ctx->scene, cv, temporal ? &pv : nullptr, temporal ? prev_res : nullptr, out, *u,
-                                    (cudaStream_t)stream),
+                                    learned.cand ? &learned : nullptr, (cudaStream_t)stream),
             "k_initial_temporal");
     return RG_OK;
 }
@@ -451,6 +460,7 @@ int rg_render_frame(rg_context *ctx, const rg_gbuffer *cur, const rg_gbuffer *pr
     if ((rc = ensure_frame_buffers(ctx, (int)u.screen_size[0], (int)u.screen_size[1], st))) return rc;
     rg_reservoir *cur_res = ctx->res[slot], *prev_res = ctx->res[1 - slot];
     const int passes = fp->spatial_iterations < 0 ? 0 : fp->spatial_iterations;
+    if ((u.flags & RG_FLAG_LEARNED_PROPOSAL) && (rc = rg_proposal_infer(ctx, cur, &u, stream))) return rc;
     // src/app.h:212-262 and :297-334
     if (fp->unbiased) {
         // RIS -> temporary, then `passes` unbiased passes ending in the frame buffer.
@@ -478,7 +488,9 @@ int rg_render_frame(rg_context *ctx, const rg_gbuffer *cur, const rg_gbuffer *pr
     lu.debug_mode = 0;
     lu.gamma = fp->gamma > 0.0f ? fp->gamma : 1.0f;
     float *img = rgba_out ? rgba_out : reinterpret_cast<float *>(ctx->image);
-    return rg_shade(ctx, cur, cur_res, &lu, img, stream);
+    if ((rc = rg_shade(ctx, cur, cur_res, &lu, img, stream))) return rc;
+    if ((u.flags & RG_FLAG_LEARNED_TRAIN) && (rc = rg_proposal_train(ctx, cur, &u, cur_res, stream))) return rc;
+    return RG_OK;
 }
 
 int rg_frame_reservoirs(rg_context *ctx, int32_t slot, const rg_reservoir **out) {
@@ -541,6 +553,11 @@ int rg_render_frame_host(rg_context *ctx, int32_t w, int32_t h, const uint8_t *a
 // For entry points defined in other translation units (noalloc.cu): the
 // per-thread error message and the uploaded scene of a context.
 int rg_internal_fail(int code, const char *msg) { return fail(code, "%s", msg); }
+
+ProposalState **rg_internal_proposal(rg_context *ctx) {
+    cudaSetDevice(ctx->device);
+    return &ctx->proposal;
+}
 
 int rg_internal_prepare(rg_context *ctx, const DevScene **scene, int *device) {
     const int rc = check_ctx(ctx, true);

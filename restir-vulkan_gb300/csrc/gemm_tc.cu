@@ -46,6 +46,25 @@ __device__ __forceinline__ __nv_bfloat16 fetch(const Operand &o, int r, int k, i
     return static_cast<const __nv_bfloat16 *>(o.ptr)[idx];
 }
 
+// Stages rows [row0, row0 + R) x k [kc, kc + 64) of an operand into a
+// K-major tile.  Consecutive threads walk k when k is the contiguous index of
+// the source, rows otherwise, so that global reads coalesce either way.
+__device__ __forceinline__ void stage(const Operand &o, unsigned char *tile, int R, int row0, int kc, int kmax) {
+    if (o.rs == 1 && o.ks != 1) {
+        for (int e = threadIdx.x; e < R * kChunkK; e += blockDim.x) {
+            const int k = e / R, r = e % R;
+            *reinterpret_cast<__nv_bfloat16 *>(tile + umma::kmajor_offset(r, k, kChunkK)) =
+                fetch(o, row0 + r, kc + k, kmax);
+        }
+    } else {
+        for (int e = threadIdx.x; e < R * kChunkK; e += blockDim.x) {
+            const int r = e / kChunkK, k = e % kChunkK;
+            *reinterpret_cast<__nv_bfloat16 *>(tile + umma::kmajor_offset(r, k, kChunkK)) =
+                fetch(o, row0 + r, kc + k, kmax);
+        }
+    }
+}
+
 template <int NT>
 __global__ void __launch_bounds__(128) k_gemm_tc(const GemmParams p) {
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -67,16 +86,8 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const GemmParams p) {
     bool ok = true;
     bool any = false;
     for (int kc = k_begin; kc < k_end; kc += kChunkK) {
-        for (int e = tid; e < kTileM * kChunkK; e += 128) {
-            const int r = e / kChunkK, k = e % kChunkK;
-            *reinterpret_cast<__nv_bfloat16 *>(reinterpret_cast<unsigned char *>(a_tile) +
-                                               umma::kmajor_offset(r, k, kChunkK)) = fetch(p.a, m0 + r, kc + k, k_end);
-        }
-        for (int e = tid; e < NT * kChunkK; e += 128) {
-            const int r = e / kChunkK, k = e % kChunkK;
-            *reinterpret_cast<__nv_bfloat16 *>(reinterpret_cast<unsigned char *>(b_tile) +
-                                               umma::kmajor_offset(r, k, kChunkK)) = fetch(p.b, n0 + r, kc + k, k_end);
-        }
+        stage(p.a, reinterpret_cast<unsigned char *>(a_tile), kTileM, m0, kc, k_end);
+        stage(p.b, reinterpret_cast<unsigned char *>(b_tile), NT, n0, kc, k_end);
         umma::fence_proxy_async();
         __syncthreads();
         if (tid == 0) {
@@ -85,12 +96,17 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const GemmParams p) {
             umma::mma_commit(&mbar);
         }
         any = true;
-        ok = umma::mbar_wait(&mbar, phase, kMaxPolls) && ok;
-        phase ^= 1u;
+        const bool w = umma::mbar_wait(&mbar, phase, kMaxPolls);
         umma::fence_after_sync();
-        __syncthreads();
+        // block-uniform, so that every thread leaves the loop at the same barrier
+        ok = __syncthreads_and(w) != 0;
+        if (!ok) {
+            if (tid == 0) umma::mbar_wait(&mbar, phase, kMaxPolls);  // bounded: the MMA still in flight
+            break;
+        }
+        phase ^= 1u;
     }
-    if (!ok) atomicAdd(p.err, 1);
+    if (!ok && tid == 0) atomicAdd(p.err, 1);
     if (any && ok) {
         const int row = m0 + warp * 32 + lane;
         for (int c = 0; c < NT; c += 32) {

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "mlp.cuh"
 #include "rg_internal.h"
 #include "rg_math.cuh"
 #include "trace_pool.cuh"
@@ -171,10 +172,17 @@ struct InitialParams {
     const rg_reservoir *prev_res;
     rg_reservoir *out;
     rg_restir_uniforms u;
+    mlp::LearnedRis learned;  // learned.cand == nullptr: the plain alias-table proposal
 };
 
+// Initial RIS (restirOmni.glsl:86-145).  With the learned proposal, candidate
+// c of the pixel comes from its candidate slot: a cluster drawn from q(.|x)
+// (the light within it from the cluster's alias table with r1, r2) or a light
+// drawn uniformly; either way the source pdf is the mixture density
+// mix * q(cluster) * p(light | cluster) + (1 - mix) / N.  The RIS stream keeps
+// the shape of the plain path (two uniforms per candidate).
 __device__ __forceinline__ Res ris(const DevScene &s, const Texel &t, float albedo_lum, f3 cam, uint32_t count_c,
-                                   bool zero_normal, int flags, Pcg &rng) {
+                                   bool zero_normal, int flags, const mlp::LearnedRis &lr, size_t px, Pcg &rng) {
     Res r = empty_res();
     if (zero_normal) return r;
     const f3 wo = view_dir(cam, t.wpos);
@@ -185,7 +193,30 @@ __device__ __forceinline__ Res ris(const DevScene &s, const Texel &t, float albe
         float4 pos_lum, nrm;
         float prob;
         int32_t lidx;
-        if (s.n_point_lights != 0) {
+        if (lr.cand) {
+            const mlp::Candidate cd = lr.cand[px * mlp::kCand + c];
+            float pl;
+            if (cd.key < 0) {
+                const int cl = -1 - cd.key;
+                const int b = __ldg(lr.offset + cl), m = __ldg(lr.offset + cl + 1) - b;
+                if (m > 0) {
+                    const mlp::LearnedCol *lc = lr.lcol + b + imin((int)((float)m * r1), m - 1);
+                    const float4 cc = __ldg(&lc->col);
+                    if (cc.x > r2) { pos_lum = __ldg(&lc->own_pos); pl = cc.w; lidx = __float_as_int(cc.y); }
+                    else { pos_lum = __ldg(&lc->alias_pos); lidx = __float_as_int(cc.z); pl = __ldg(lr.within + lidx); }
+                } else {  // an empty cluster (only from non-finite logits): light 0 with weight 0
+                    lidx = 0;
+                    pos_lum = __ldg(&s.alias[0].own_pos);
+                    pl = 0.0f;
+                }
+            } else {
+                lidx = cd.key;
+                pos_lum = __ldg(&s.alias[lidx].own_pos);
+                pl = __ldg(lr.within + lidx);
+            }
+            prob = lr.mix * cd.q * pl + lr.uniform_pdf;
+            nrm = make_float4(0.f, 0.f, 0.f, 0.f);
+        } else if (s.n_point_lights != 0) {
             const AliasLight *al = s.alias + col;
             const float4 cc = __ldg(&al->col);
             if (cc.x > r2) { pos_lum = __ldg(&al->own_pos); prob = cc.z; lidx = col; }
@@ -251,7 +282,8 @@ __global__ void __launch_bounds__(128, RG_RIS_MIN_BLOCKS) k_initial_temporal(con
             const float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
             Pcg rng = pcg_seed((uint64_t)p.u.frame, (uint64_t)((uint32_t)y * 10007u + (uint32_t)x));
             const bool zero_normal = !(dot(t.normal, t.normal) != 0.0f);
-            const Res r = ris(s, t, albedo_lum, cam, p.u.initial_light_sample_count, zero_normal, p.u.flags, rng);
+            const Res r = ris(s, t, albedo_lum, cam, p.u.initial_light_sample_count, zero_normal, p.u.flags,
+                              p.learned, i, rng);
             store_res(p.out, i, r);
             rng_state[j] = rng.state;
             // visibility reuse :147-160; a background pixel's (zero normal) sample is the
@@ -582,8 +614,9 @@ GBufView make_view(const rg_gbuffer *g) {
 
 cudaError_t launch_initial_temporal(const DevScene &s, const GBufView &cur, const GBufView *prev,
                                     const rg_reservoir *prev_res, rg_reservoir *out, const rg_restir_uniforms &u,
-                                    cudaStream_t st) {
+                                    const mlp::LearnedRis *learned, cudaStream_t st) {
     InitialParams p;
+    p.learned = learned ? *learned : mlp::LearnedRis{};
     p.s = s;
     p.cur = cur;
     p.has_prev = prev != nullptr && prev_res != nullptr;

@@ -1,0 +1,621 @@
+// mlp.cu -- kernels of the learned light-cluster proposal (network in mlp.cuh).
+//
+// The forward pass of a 128-pixel tile is one CTA on the tcgen05 tensor cores:
+// features -> x tile (shared memory, bf16) -> three 64-wide layers (MMA into
+// tensor memory, bias + ReLU + bf16 epilogue back into shared memory) -> the
+// cluster logit layer in chunks of 128 clusters, double-buffered in tensor
+// memory so that the MMA of chunk c+1 runs under the epilogue of chunk c.
+// Weight tiles arrive by cp.async from bf16 images that are already in the MMA
+// operand layout.  Logits never leave the SM.  Three epilogues:
+//   kLse     log-sum-exp, arg-max and its probability per row;
+//   kSample  the proposal's candidates: each row walks its softmax CDF once,
+//            with its sorted uniforms and the clusters of its uniform-branch
+//            lights (the walk skips 32-column pieces that hold neither);
+//   kGrad    d(loss)/d(logits) = (softmax - onehot) / n as bf16 rows, and the
+//            cross-entropy loss, for training.
+// Every wait on the tensor core is bounded; a CTA whose wait runs out records
+// an error, waits (bounded) for its last MMA, frees its tensor memory and
+// leaves.  At most two CTAs share an SM: each holds 256 tensor-memory columns
+// and asks for at least 80 KB of shared memory.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "mlp.cuh"
+#include "rg_math.cuh"
+#include "umma.cuh"
+
+using namespace rgm;
+
+namespace {
+
+constexpr int kRows = 128;                 // rows (pixels) per CTA
+constexpr int kChunkN = mlp::kChunkN;      // clusters per logit MMA chunk
+constexpr uint32_t kMaxPolls = 1u << 26;   // bounded mbarrier waits
+constexpr int kTmemCols = 256;
+
+// shared-memory map (bytes)
+constexpr int kOffX = 0;                               // x tile, 128 x 16 bf16
+constexpr int kOffH = kOffX + kRows * mlp::kIn * 2;    // h tile, 128 x 64 bf16
+constexpr int kOffW1 = kOffH + kRows * mlp::kH * 2;    // W1^T image, 64 x 16
+constexpr int kOffW2 = kOffW1 + mlp::kH * mlp::kIn * 2;
+constexpr int kOffW3 = kOffW2 + mlp::kH * mlp::kH * 2;
+constexpr int kOffB = kOffW3 + mlp::kH * mlp::kH * 2;  // two chunk tiles, 128 x 64
+constexpr int kChunkBytes = kChunkN * mlp::kH * 2;
+constexpr int kOffBias = kOffB + 2 * kChunkBytes;      // b1 | b2 | b3
+constexpr int kOffRow = kOffBias + 3 * mlp::kH * 4;    // per-row arrays (kSample)
+constexpr int kRowBytes = mlp::kCand * kRows * (4 + 1 + 4);
+constexpr int kSmemMin = 80 * 1024;                    // caps residency at two CTAs per SM
+constexpr int kWeightImgBytes = (mlp::kH * mlp::kIn + 2 * mlp::kH * mlp::kH) * 2;
+
+enum { kLse = 0, kSample = 1, kGrad = 2 };
+
+__device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(umma::smem_addr(smem_dst)), "l"(gsrc)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+__device__ __forceinline__ void copy_bytes(unsigned char *dst, const unsigned char *src, int bytes) {
+    for (int o = threadIdx.x * 16; o < bytes; o += blockDim.x * 16) cp_async16(dst + o, src + o);
+}
+
+struct FusedParams {
+    mlp::ProposalDev pd;
+    GBufView g;
+    float cam[3];
+    const int32_t *rows;       // pixel of each row; nullptr: row = pixel
+    int n;
+    float4 *stat;              // per row: lse, arg-max cluster (int bits), its probability, 0
+    // training (kLse with save != 0, kGrad)
+    int save;
+    __nv_bfloat16 *x, *h1, *h2, *h3;  // [n x 16], [n x 64] x 3
+    const int32_t *target;     // cluster per row, -1: no target
+    __nv_bfloat16 *dz;         // [n x C]
+    float inv_n;
+    float *loss_sum;
+    // sampling
+    mlp::Candidate *cand;      // [n x kCand]
+    uint32_t frame;
+    int n_cand;
+    int *err;
+};
+
+// Features of one pixel (mlp.cuh), each rounded to bf16; non-finite values
+// (a pixel at the camera position) become 0.
+__device__ __forceinline__ void features(const FusedParams &p, size_t px, float x[mlp::kIn]) {
+    const float4 wp = __ldg(p.g.wpos + px);
+    const uint2 nb = __ldg(p.g.normal + px);
+    const f3 wpos = mk(wp.x, wp.y, wp.z);
+    const f3 n = mk(half_bits_to_float((uint16_t)(nb.x & 0xffffu)), half_bits_to_float((uint16_t)(nb.x >> 16)),
+                    half_bits_to_float((uint16_t)(nb.y & 0xffffu)));
+    const f3 v = normalize(mk(p.cam[0], p.cam[1], p.cam[2]) - wpos);
+    x[0] = (wpos.x - p.pd.box_center.x) * p.pd.box_inv_half.x;
+    x[1] = (wpos.y - p.pd.box_center.y) * p.pd.box_inv_half.y;
+    x[2] = (wpos.z - p.pd.box_center.z) * p.pd.box_inv_half.z;
+    x[3] = n.x; x[4] = n.y; x[5] = n.z;
+    x[6] = v.x; x[7] = v.y; x[8] = v.z;
+#pragma unroll
+    for (int i = 0; i < mlp::kIn; ++i) {
+        const float t = i < mlp::kInUsed ? x[i] : 0.0f;
+        x[i] = isfinite(t) ? bf16r(t) : 0.0f;
+    }
+}
+
+// Writes 8 consecutive bf16 values (k = k0..k0+7) of row r into a K-major tile.
+__device__ __forceinline__ void put8(unsigned char *tile, int r, int k0, int K, const float *v) {
+    __align__(16) __nv_bfloat16 b[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) b[i] = __float2bfloat16_rn(v[i]);
+    *reinterpret_cast<uint4 *>(tile + umma::kmajor_offset(r, k0, K)) = *reinterpret_cast<const uint4 *>(b);
+}
+__device__ __forceinline__ void store8(__nv_bfloat16 *dst, const float *v) {
+    __align__(16) __nv_bfloat16 b[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) b[i] = __float2bfloat16_rn(v[i]);
+    *reinterpret_cast<uint4 *>(dst) = *reinterpret_cast<const uint4 *>(b);
+}
+
+// Bounded wait for an MMA commit; warp-uniform result.
+__device__ __forceinline__ bool mma_wait(uint64_t *mbar, uint32_t parity) {
+    bool w = umma::mbar_wait(mbar, parity, kMaxPolls);
+    umma::fence_after_sync();
+    return __all_sync(0xffffffffu, w);
+}
+
+template <int kMode>
+__global__ void __launch_bounds__(128, 1) k_mlp_fused(const FusedParams p) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint64_t mbar_layer, mbar_chunk[2];
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int row = blockIdx.x * kRows + tid;
+    const bool valid = row < p.n;
+    const size_t px = valid ? (p.rows ? (size_t)p.rows[row] : (size_t)row) : 0;
+    const int nch = p.pd.c / kChunkN;
+    const mlp::Layout L(p.pd.c);
+    unsigned char *xtile = smem + kOffX, *htile = smem + kOffH;
+    unsigned char *btile[2] = {smem + kOffB, smem + kOffB + kChunkBytes};
+    float *bias = reinterpret_cast<float *>(smem + kOffBias);
+    const unsigned char *w4img = reinterpret_cast<const unsigned char *>(p.pd.w4t);
+
+    // weights and the first two logit chunks start moving
+    copy_bytes(smem + kOffW1, reinterpret_cast<const unsigned char *>(p.pd.w123img), kWeightImgBytes);
+    copy_bytes(btile[0], w4img, kChunkBytes);
+    cp_async_commit();
+    if (nch > 1) copy_bytes(btile[1], w4img + kChunkBytes, kChunkBytes);
+    cp_async_commit();
+    for (int i = tid; i < 3 * mlp::kH; i += blockDim.x) {
+        const size_t b = i < mlp::kH ? L.b1 : i < 2 * mlp::kH ? L.b2 : L.b3;
+        bias[i] = p.pd.params[b + (size_t)(i % mlp::kH)];
+    }
+    if (warp == 0) umma::tmem_alloc(&tmem_base, kTmemCols);
+    if (tid == 0) {
+        umma::mbar_init(&mbar_layer, 1);
+        umma::mbar_init(&mbar_chunk[0], 1);
+        umma::mbar_init(&mbar_chunk[1], 1);
+    }
+    {
+        float x[mlp::kIn];
+        if (valid) {
+            features(p, px, x);
+        } else {
+#pragma unroll
+            for (int i = 0; i < mlp::kIn; ++i) x[i] = 0.0f;
+        }
+        put8(xtile, tid, 0, mlp::kIn, x);
+        put8(xtile, tid, 8, mlp::kIn, x + 8);
+        if (kMode == kLse && p.save && valid) {
+            store8(p.x + (size_t)row * mlp::kIn, x);
+            store8(p.x + (size_t)row * mlp::kIn + 8, x + 8);
+        }
+    }
+
+    // kSample: the row's branches and uniforms from a PCG stream of its own
+    float *u_val = reinterpret_cast<float *>(smem + kOffRow);          // [kCand][128]
+    uint8_t *u_slot = reinterpret_cast<uint8_t *>(u_val + mlp::kCand * kRows);
+    int32_t *lk = reinterpret_cast<int32_t *>(u_slot + mlp::kCand * kRows);  // cluster << 5 | slot
+    int n_u = 0, n_lk = 0;
+    if (kMode == kSample && valid) {
+        Pcg rng = pcg_seed((uint64_t)p.frame * mlp::kSeedMul + mlp::kSeedAdd, (uint64_t)px);
+        mlp::Candidate *out = p.cand + (size_t)row * mlp::kCand;
+        for (int j = 0; j < p.n_cand; ++j) {
+            const float u0 = rand_float(rng);
+            const float u1 = rand_float(rng);
+            if (u0 < p.pd.mix) {
+                int k = n_u++;
+                while (k > 0 && u_val[(k - 1) * kRows + tid] > u1) {
+                    u_val[k * kRows + tid] = u_val[(k - 1) * kRows + tid];
+                    u_slot[k * kRows + tid] = u_slot[(k - 1) * kRows + tid];
+                    --k;
+                }
+                u_val[k * kRows + tid] = u1;
+                u_slot[k * kRows + tid] = (uint8_t)j;
+            } else {
+                const int l = imin((int)((float)p.pd.n_lights * u1), p.pd.n_lights - 1);
+                const int32_t key = (p.pd.cluster_of[l] << 5) | j;
+                out[j] = mlp::Candidate{l, 0.0f};
+                int k = n_lk++;
+                while (k > 0 && lk[(k - 1) * kRows + tid] > key) {
+                    lk[k * kRows + tid] = lk[(k - 1) * kRows + tid];
+                    --k;
+                }
+                lk[k * kRows + tid] = key;
+            }
+        }
+    }
+
+    cp_async_wait_one();
+    umma::fence_proxy_async();
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tmem_base;
+    bool ok = true;
+    int issued = 0;          // logit chunks whose MMA was issued
+    int layer_commits = 0;
+
+    // ---- hidden layers: MMA into columns 64*l, epilogue into the h tile
+    const unsigned char *wimg[3] = {smem + kOffW1, smem + kOffW2, smem + kOffW3};
+    __nv_bfloat16 *hsave[3] = {p.h1, p.h2, p.h3};
+    for (int l = 0; l < 3 && ok; ++l) {
+        if (tid == 0) {
+            umma::mma_chunk(tmem + (uint32_t)(64 * l), l == 0 ? xtile : htile, wimg[l], l == 0 ? mlp::kIn : mlp::kH,
+                            kRows, mlp::kH, false);
+            umma::mma_commit(&mbar_layer);
+        }
+        ++layer_commits;
+        const bool w = mma_wait(&mbar_layer, (uint32_t)(l & 1));
+        if (w) {
+            float v[64];
+            umma::tmem_ld32(tmem + (uint32_t)(64 * l), warp, 0, *reinterpret_cast<float(*)[32]>(v));
+            umma::tmem_ld32(tmem + (uint32_t)(64 * l), warp, 32, *reinterpret_cast<float(*)[32]>(v + 32));
+#pragma unroll
+            for (int j = 0; j < 64; ++j) v[j] = bf16r(fmaxf(v[j] + bias[64 * l + j], 0.0f));
+#pragma unroll
+            for (int j = 0; j < 64; j += 8) put8(htile, tid, j, mlp::kH, v + j);
+            if (kMode == kLse && p.save && valid) {
+#pragma unroll
+                for (int j = 0; j < 64; j += 8) store8(hsave[l] + (size_t)row * mlp::kH + j, v + j);
+            }
+        }
+        umma::fence_proxy_async();
+        umma::fence_before_sync();
+        ok = __syncthreads_and(w) != 0;
+        umma::fence_after_sync();
+    }
+
+    // ---- logit chunks
+    float m = -INFINITY, s = 0.0f;  // kLse: running max and sum
+    int amax = 0;
+    float lse = 0.0f, cum = 0.0f;   // kSample / kGrad
+    int iu = 0, ik = 0;
+    float next_u = INFINITY;  // no uniform left (cum never exceeds it, even when it overflows)
+    int next_lk = p.pd.c;
+    int target = -1;
+    float zt = 0.0f;
+    if (kMode != kLse && valid) {
+        lse = p.stat[row].x;
+        if (kMode == kSample) {
+            if (n_u > 0) next_u = u_val[tid];
+            if (n_lk > 0) next_lk = lk[tid] >> 5;
+        } else {
+            target = p.target[row];
+        }
+    }
+    if (ok) {
+        if (tid == 0) {
+            umma::mma_chunk(tmem, htile, btile[0], mlp::kH, kRows, kChunkN, false);
+            umma::mma_commit(&mbar_chunk[0]);
+        }
+        issued = 1;
+    }
+    // `ok` changes only at block barriers (uniform); `ok_warp` records this
+    // warp's waits and joins `ok` at the next barrier, so every warp passes
+    // the same sequence of barriers whatever fails.
+    bool ok_warp = true;
+    for (int c = 0; c < nch; ++c) {
+        if (!ok) break;
+        if (c + 1 < nch) {
+            cp_async_wait_all();
+            umma::fence_proxy_async();
+            umma::fence_before_sync();
+            ok = __syncthreads_and(ok_warp) != 0;
+            umma::fence_after_sync();
+            if (!ok) break;
+            if (tid == 0) {
+                umma::mma_chunk(tmem + (uint32_t)(((c + 1) & 1) * kChunkN), htile, btile[(c + 1) & 1], mlp::kH, kRows,
+                                kChunkN, false);
+                umma::mma_commit(&mbar_chunk[(c + 1) & 1]);
+            }
+            issued = c + 2;
+        }
+        const bool w = mma_wait(&mbar_chunk[c & 1], (uint32_t)((c >> 1) & 1));
+        ok_warp = ok_warp && w;
+        if (!w) continue;
+        if (c + 2 < nch) {
+            copy_bytes(btile[c & 1], w4img + (size_t)(c + 2) * kChunkBytes, kChunkBytes);
+            cp_async_commit();
+        }
+        const uint32_t half = tmem + (uint32_t)((c & 1) * kChunkN);
+        for (int piece = 0; piece < kChunkN / 32; ++piece) {
+            float v[32];
+            umma::tmem_ld32(half, warp, piece * 32, v);
+            const int col0 = c * kChunkN + piece * 32;
+            const float4 *be = reinterpret_cast<const float4 *>(p.pd.b4e + col0);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const float4 b = __ldg(be + q);
+                v[4 * q] += b.x; v[4 * q + 1] += b.y; v[4 * q + 2] += b.z; v[4 * q + 3] += b.w;
+            }
+            if (kMode == kLse) {
+                float mp = v[0];
+#pragma unroll
+                for (int i = 1; i < 32; ++i) mp = fmaxf(mp, v[i]);
+                if (mp == -INFINITY) continue;
+                float sp = 0.0f;
+#pragma unroll
+                for (int i = 0; i < 32; ++i) sp += __expf(v[i] - mp);
+                if (mp > m) {
+                    s = (m == -INFINITY) ? sp : s * __expf(m - mp) + sp;
+                    m = mp;
+#pragma unroll
+                    for (int i = 31; i >= 0; --i)
+                        if (v[i] == mp) amax = col0 + i;
+                } else {
+                    s += sp * __expf(mp - m);
+                }
+            } else if (kMode == kSample) {
+                if (!valid) continue;
+                float pr[32], psum = 0.0f;
+#pragma unroll
+                for (int i = 0; i < 32; ++i) {
+                    pr[i] = __expf(v[i] - lse);
+                    psum += pr[i];
+                }
+                if (next_u < cum + psum || next_lk < col0 + 32) {
+                    mlp::Candidate *out = p.cand + (size_t)row * mlp::kCand;
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) {
+                        cum += pr[i];
+                        while (next_u < cum) {
+                            out[u_slot[iu * kRows + tid]] = mlp::Candidate{-1 - (col0 + i), pr[i]};
+                            ++iu;
+                            next_u = iu < n_u ? u_val[iu * kRows + tid] : INFINITY;
+                        }
+                        while (next_lk == col0 + i) {
+                            out[lk[ik * kRows + tid] & 31].q = pr[i];
+                            ++ik;
+                            next_lk = ik < n_lk ? lk[ik * kRows + tid] >> 5 : p.pd.c;
+                        }
+                    }
+                } else {
+                    cum += psum;
+                }
+            } else {  // kGrad
+                float d[32];
+#pragma unroll
+                for (int i = 0; i < 32; ++i) {
+                    const float pr = __expf(v[i] - lse);
+                    const bool hit = (col0 + i) == target;
+                    if (hit) zt = v[i];
+                    d[i] = target < 0 ? 0.0f : (pr - (hit ? 1.0f : 0.0f)) * p.inv_n;
+                }
+                if (valid) {
+                    __nv_bfloat16 *dst = p.dz + (size_t)row * p.pd.c + col0;
+#pragma unroll
+                    for (int q = 0; q < 32; q += 8) store8(dst + q, d + q);
+                }
+            }
+        }
+        umma::fence_before_sync();
+    }
+    ok = __syncthreads_and(ok && ok_warp) != 0;
+    if (!ok) {
+        if (tid == 0) {
+            atomicAdd(p.err, 1);
+            if (issued > 0)
+                umma::mbar_wait(&mbar_chunk[(issued - 1) & 1], (uint32_t)(((issued - 1) >> 1) & 1), kMaxPolls);
+            else if (layer_commits > 0)
+                umma::mbar_wait(&mbar_layer, (uint32_t)((layer_commits - 1) & 1), kMaxPolls);
+        }
+        cp_async_wait_all();
+    } else if (valid) {
+        if (kMode == kLse) {
+            const float lse_row = m + __logf(s);
+            p.stat[row] = make_float4(lse_row, __int_as_float(amax), __expf(m - lse_row), 0.0f);
+        } else if (kMode == kSample) {
+            // a uniform beyond the rounded CDF total: the most probable cluster
+            const float4 st = p.stat[row];
+            mlp::Candidate *out = p.cand + (size_t)row * mlp::kCand;
+            for (; iu < n_u; ++iu) out[u_slot[iu * kRows + tid]] = mlp::Candidate{-1 - __float_as_int(st.y), st.z};
+        }
+    }
+    if (kMode == kGrad && ok) {
+        float l = (valid && target >= 0) ? lse - zt : 0.0f;
+        for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+        if ((tid & 31) == 0 && l != 0.0f) atomicAdd(p.loss_sum, l);
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, kTmemCols);
+}
+
+// ---------------------------------------------------------------- training helpers
+// Column sums of a row-major [n x c] matrix (bf16 or FP32), added into out[c].
+template <typename T>
+__global__ void k_colsum(const T *a, int n, int c, float *out) {
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= c) return;
+    const int r0 = blockIdx.y * 512, r1 = min(n, r0 + 512);
+    float s = 0.0f;
+    for (int r = r0; r < r1; ++r) {
+        if constexpr (sizeof(T) == 2) s += __bfloat162float(a[(size_t)r * c + col]);
+        else s += a[(size_t)r * c + col];
+    }
+    atomicAdd(out + col, s);
+}
+
+struct BackParams {
+    const __nv_bfloat16 *w123;
+    const __nv_bfloat16 *h1, *h2, *h3;
+    const float *dh3;
+    float *da1, *da2, *da3;
+    int n;
+};
+
+// dh3 -> da3 -> dh2 -> da2 -> dh1 -> da1, one row per thread, FP32 with the
+// bf16 weights of the forward pass.
+__global__ void __launch_bounds__(128) k_mlp_backward_rows(const BackParams p) {
+    __shared__ float w[2 * mlp::kH * mlp::kH];
+    for (int i = threadIdx.x; i < 2 * mlp::kH * mlp::kH; i += blockDim.x)
+        w[i] = __bfloat162float(p.w123[mlp::kIn * mlp::kH + i]);
+    __syncthreads();
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= p.n) return;
+    const float *w2 = w, *w3 = w + mlp::kH * mlp::kH;
+    float da[mlp::kH], db[mlp::kH];
+    for (int j = 0; j < mlp::kH; ++j) {
+        const size_t i = (size_t)r * mlp::kH + j;
+        da[j] = __bfloat162float(p.h3[i]) > 0.0f ? p.dh3[i] : 0.0f;
+        p.da3[i] = da[j];
+    }
+    for (int i = 0; i < mlp::kH; ++i) {  // dh2_i = sum_k W3[i][k] da3_k
+        float acc = 0.0f;
+#pragma unroll 16
+        for (int k = 0; k < mlp::kH; ++k) acc += w3[i * mlp::kH + k] * da[k];
+        db[i] = __bfloat162float(p.h2[(size_t)r * mlp::kH + i]) > 0.0f ? acc : 0.0f;
+        p.da2[(size_t)r * mlp::kH + i] = db[i];
+    }
+    for (int i = 0; i < mlp::kH; ++i) {
+        float acc = 0.0f;
+#pragma unroll 16
+        for (int k = 0; k < mlp::kH; ++k) acc += w2[i * mlp::kH + k] * db[k];
+        p.da1[(size_t)r * mlp::kH + i] = __bfloat162float(p.h1[(size_t)r * mlp::kH + i]) > 0.0f ? acc : 0.0f;
+    }
+}
+
+__global__ void k_adam(float *w, const float *g, float *m, float *v, size_t n, float lr, float b1, float b2,
+                       float eps, float c1, float c2, size_t w1_pad_begin, size_t w1_pad_end) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || (i >= w1_pad_begin && i < w1_pad_end)) return;  // padded inputs stay zero
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * (gi * gi);
+    m[i] = mi;
+    v[i] = vi;
+    w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+// bf16 images of the weights: W1^T | W2^T | W3^T in the MMA operand layout
+// (w123img), W4^T in 128-cluster chunk tiles (w4t), W1 | W2 | W3 row-major
+// (w123), W4 row-major (w4), and b4 with -inf for clusters without lights.
+__global__ void k_refresh(const float *params, int c, const uint8_t *valid, __nv_bfloat16 *w123img,
+                          __nv_bfloat16 *w4t, __nv_bfloat16 *w123, __nv_bfloat16 *w4, float *b4e) {
+    const mlp::Layout L(c);
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t n1 = (size_t)mlp::kIn * mlp::kH, n2 = (size_t)mlp::kH * mlp::kH;
+    unsigned char *img = reinterpret_cast<unsigned char *>(w123img);
+    if (i < n1) {  // W1[k][n]
+        const int k = (int)(i / mlp::kH), nn = (int)(i % mlp::kH);
+        const __nv_bfloat16 b = __float2bfloat16_rn(params[L.w1 + i]);
+        w123[i] = b;
+        *reinterpret_cast<__nv_bfloat16 *>(img + umma::kmajor_offset(nn, k, mlp::kIn)) = b;
+    } else if (i < n1 + 2 * n2) {
+        const size_t j = i - n1;
+        const int layer = (int)(j / n2);
+        const size_t e = j % n2;
+        const int k = (int)(e / mlp::kH), nn = (int)(e % mlp::kH);
+        const __nv_bfloat16 b = __float2bfloat16_rn(params[(layer == 0 ? L.w2 : L.w3) + e]);
+        w123[i] = b;
+        *reinterpret_cast<__nv_bfloat16 *>(img + n1 * 2 + (size_t)layer * n2 * 2 +
+                                           umma::kmajor_offset(nn, k, mlp::kH)) = b;
+    } else if (i < n1 + 2 * n2 + (size_t)mlp::kH * c) {
+        const size_t e = i - n1 - 2 * n2;  // W4[k][cl]
+        const int k = (int)(e / (size_t)c), cl = (int)(e % (size_t)c);
+        const __nv_bfloat16 b = __float2bfloat16_rn(params[L.w4 + e]);
+        w4[e] = b;
+        unsigned char *tile = reinterpret_cast<unsigned char *>(w4t) + (size_t)(cl / kChunkN) * kChunkBytes;
+        *reinterpret_cast<__nv_bfloat16 *>(tile + umma::kmajor_offset(cl % kChunkN, k, mlp::kH)) = b;
+    } else if (i < n1 + 2 * n2 + (size_t)(mlp::kH + 1) * c) {
+        const size_t cl = i - n1 - 2 * n2 - (size_t)mlp::kH * c;
+        b4e[cl] = valid[cl] ? params[L.b4 + cl] : -INFINITY;
+    }
+}
+
+// Training target of each row: the cluster of its final reservoir's light,
+// or -1 (no light kept).
+__global__ void k_targets(const rg_reservoir *res, const int32_t *rows, int n, const int32_t *cluster_of,
+                          int n_lights, int32_t *target, int *count) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const float4 c = __ldg(reinterpret_cast<const float4 *>(res + rows[r]) + 2);
+    const int idx = __float_as_int(c.x);
+    int t = -1;
+    if (c.w > 0.0f && idx >= 0 && idx < n_lights) t = cluster_of[idx];
+    target[r] = t;
+    if (t >= 0) atomicAdd(count, 1);
+}
+
+// Training rows of one frame: a strided sweep over the pixels.
+__global__ void k_batch_rows(int32_t *rows, int n, uint32_t pixels, uint32_t offset, uint32_t stride) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    rows[r] = (int32_t)(((uint64_t)r * stride + offset) % pixels);
+}
+
+template <int kMode>
+cudaError_t launch_fused(const FusedParams &p, cudaStream_t st) {
+    if (p.pd.c % kChunkN != 0 || p.pd.c < kChunkN) return cudaErrorInvalidValue;
+    int smem = kOffRow + (kMode == kSample ? kRowBytes : 0);
+    if (smem < kSmemMin) smem = kSmemMin;
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_fused<kMode>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    if (p.n > 0) k_mlp_fused<kMode><<<(p.n + kRows - 1) / kRows, kRows, smem, st>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- launchers (mlp.cuh)
+namespace mlp {
+
+size_t weight_image_bytes() { return (size_t)kWeightImgBytes; }
+
+cudaError_t forward_lse(const ProposalDev &pd, const GBufView &g, const float cam[3], const int32_t *rows, int n,
+                        float4 *stat, const TrainBuffers *save, int *err, cudaStream_t st) {
+    FusedParams p{};
+    p.pd = pd; p.g = g; p.cam[0] = cam[0]; p.cam[1] = cam[1]; p.cam[2] = cam[2];
+    p.rows = rows; p.n = n; p.stat = stat; p.err = err;
+    if (save) { p.save = 1; p.x = save->x; p.h1 = save->h1; p.h2 = save->h2; p.h3 = save->h3; }
+    return launch_fused<kLse>(p, st);
+}
+
+cudaError_t forward_sample(const ProposalDev &pd, const GBufView &g, const float cam[3], int n, const float4 *stat,
+                           uint32_t frame, int n_cand, Candidate *cand, int *err, cudaStream_t st) {
+    if (n_cand < 1 || n_cand > kCand) return cudaErrorInvalidValue;
+    FusedParams p{};
+    p.pd = pd; p.g = g; p.cam[0] = cam[0]; p.cam[1] = cam[1]; p.cam[2] = cam[2];
+    p.n = n; p.stat = const_cast<float4 *>(stat); p.frame = frame; p.n_cand = n_cand; p.cand = cand; p.err = err;
+    return launch_fused<kSample>(p, st);
+}
+
+cudaError_t forward_grad(const ProposalDev &pd, const GBufView &g, const float cam[3], const int32_t *rows, int n,
+                         const float4 *stat, const int32_t *target, float inv_n, __nv_bfloat16 *dz, float *loss_sum,
+                         int *err, cudaStream_t st) {
+    FusedParams p{};
+    p.pd = pd; p.g = g; p.cam[0] = cam[0]; p.cam[1] = cam[1]; p.cam[2] = cam[2];
+    p.rows = rows; p.n = n; p.stat = const_cast<float4 *>(stat); p.target = target; p.inv_n = inv_n; p.dz = dz;
+    p.loss_sum = loss_sum; p.err = err;
+    return launch_fused<kGrad>(p, st);
+}
+
+cudaError_t colsum_bf16(const __nv_bfloat16 *a, int n, int c, float *out, cudaStream_t st) {
+    if (n > 0) k_colsum<__nv_bfloat16><<<dim3((c + 127) / 128, (n + 511) / 512), 128, 0, st>>>(a, n, c, out);
+    return cudaGetLastError();
+}
+cudaError_t colsum_f32(const float *a, int n, int c, float *out, cudaStream_t st) {
+    if (n > 0) k_colsum<float><<<dim3((c + 127) / 128, (n + 511) / 512), 128, 0, st>>>(a, n, c, out);
+    return cudaGetLastError();
+}
+
+cudaError_t backward_rows(const __nv_bfloat16 *w123, const TrainBuffers &t, const float *dh3, float *da1, float *da2,
+                          float *da3, int n, cudaStream_t st) {
+    BackParams p{w123, t.h1, t.h2, t.h3, dh3, da1, da2, da3, n};
+    if (n > 0) k_mlp_backward_rows<<<(n + 127) / 128, 128, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t adam(float *w, const float *g, float *m, float *v, size_t n, float lr, int step, int c, cudaStream_t st) {
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
+    const Layout L(c);
+    k_adam<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(w, g, m, v, n, lr, b1, b2, 1e-8f, c1, c2,
+                                                         L.w1 + (size_t)kInUsed * kH, L.w1 + (size_t)kIn * kH);
+    return cudaGetLastError();
+}
+
+cudaError_t refresh(const float *params, int c, const uint8_t *valid, __nv_bfloat16 *w123img, __nv_bfloat16 *w4t,
+                    __nv_bfloat16 *w123, __nv_bfloat16 *w4, float *b4e, cudaStream_t st) {
+    const size_t n = (size_t)kIn * kH + 2 * (size_t)kH * kH + (size_t)(kH + 1) * c;
+    k_refresh<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(params, c, valid, w123img, w4t, w123, w4, b4e);
+    return cudaGetLastError();
+}
+
+cudaError_t targets(const rg_reservoir *res, const int32_t *rows, int n, const int32_t *cluster_of, int n_lights,
+                    int32_t *target, int *count, cudaStream_t st) {
+    if (n > 0) k_targets<<<(n + 127) / 128, 128, 0, st>>>(res, rows, n, cluster_of, n_lights, target, count);
+    return cudaGetLastError();
+}
+
+cudaError_t batch_rows(int32_t *rows, int n, uint32_t pixels, uint32_t offset, uint32_t stride, cudaStream_t st) {
+    if (n > 0) k_batch_rows<<<(n + 127) / 128, 128, 0, st>>>(rows, n, pixels, offset, stride);
+    return cudaGetLastError();
+}
+
+}  // namespace mlp

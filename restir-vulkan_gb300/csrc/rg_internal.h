@@ -63,9 +63,10 @@ struct GBufView {
 GBufView make_view(const rg_gbuffer *g);
 
 // launchers (kernels.cu); return cudaGetLastError()
+namespace mlp { struct LearnedRis; }
 cudaError_t launch_initial_temporal(const DevScene &s, const GBufView &cur, const GBufView *prev,
                                     const rg_reservoir *prev_res, rg_reservoir *out, const rg_restir_uniforms &u,
-                                    cudaStream_t st);
+                                    const mlp::LearnedRis *learned, cudaStream_t st);
 cudaError_t launch_spatial_biased(const DevScene &s, const GBufView &g, const rg_reservoir *in, rg_reservoir *out,
                                   const rg_restir_uniforms &u, int iter, cudaStream_t st);
 cudaError_t launch_spatial_unbiased(const DevScene &s, const GBufView &g, const rg_reservoir *in, rg_reservoir *out,
@@ -86,3 +87,11 @@ void srgb_lut_host(float *out256);
 // capi.cu: error reporting and context access for other translation units.
 int rg_internal_fail(int code, const char *msg);
 int rg_internal_prepare(rg_context *ctx, const DevScene **scene, int *device);
+
+// proposal.cu: the learned proposal attached to a context.
+struct ProposalState;
+ProposalState **rg_internal_proposal(rg_context *ctx);
+void proposal_release(ProposalState *ps);
+// Learned RIS inputs for a frame of w x h with `count` candidates, or an
+// RG_ERR_* code when the context's candidates do not match that frame.
+int proposal_learned_ris(ProposalState *ps, int w, int h, uint32_t frame, uint32_t count, mlp::LearnedRis *out);

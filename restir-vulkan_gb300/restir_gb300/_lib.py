@@ -22,6 +22,8 @@ RG_OK = 0
 RG_FLAG_VISIBILITY_REUSE = 1
 RG_FLAG_TEMPORAL_REUSE = 2
 RG_FLAG_FINAL_RIS_WEIGHT = 256
+RG_FLAG_LEARNED_PROPOSAL = 512
+RG_FLAG_LEARNED_TRAIN = 1024
 RG_MAX_TREE_DEPTH = 63
 
 F4 = C.c_float * 4
@@ -83,6 +85,12 @@ class Stats(C.Structure):
                 ("triangle_tests", C.c_uint64), ("mma_timeouts", C.c_uint64)]
 
 
+class ProposalConfig(C.Structure):
+    _fields_ = [("clusters", C.c_int32), ("mix", C.c_float), ("learning_rate", C.c_float), ("batch", C.c_int32),
+                ("box_min", C.c_float * 3), ("box_max", C.c_float * 3), ("seed", C.c_uint64)]
+
+
+assert C.sizeof(ProposalConfig) == 48
 assert C.sizeof(Reservoir) == 64 and C.sizeof(AabbTreeNode) == 80
 assert C.sizeof(RestirUniforms) == 128 and C.sizeof(LightingUniforms) == 96
 
@@ -96,6 +104,7 @@ POINT_LIGHT_DTYPE = np.dtype([("pos", "<f4", 4), ("color_lum", "<f4", 4)])
 TRI_LIGHT_DTYPE = np.dtype([("p1", "<f4", 4), ("p2", "<f4", 4), ("p3", "<f4", 4), ("emission_lum", "<f4", 4),
                             ("normal_area", "<f4", 4)])
 ALIAS_DTYPE = np.dtype([("prob", "<f4"), ("alias", "<i4"), ("ori_prob", "<f4"), ("alias_ori_prob", "<f4")])
+CANDIDATE_DTYPE = np.dtype([("key", "<i4"), ("q", "<f4")])
 MATERIAL_DTYPE = np.dtype([("albedo", "u1", 4), ("roughness", "<u2"), ("metallic", "<u2")])
 assert RESERVOIR_DTYPE.itemsize == 64 and NODE_DTYPE.itemsize == 80 and TRI_DTYPE.itemsize == 48
 assert POINT_LIGHT_DTYPE.itemsize == 32 and TRI_LIGHT_DTYPE.itemsize == 80 and ALIAS_DTYPE.itemsize == 16
@@ -140,6 +149,20 @@ _SIGNATURES = {
                                C.c_int32, C.c_float, C.c_int32, C.c_void_p]),
     "rg_spatial_unbiased_chain_noalloc": (C.c_int, [C.c_void_p, C.POINTER(GBuffer), C.c_void_p, C.c_void_p,
                                                     C.POINTER(RestirUniforms), C.c_int32, C.c_int32, C.c_void_p]),
+    "rg_cluster_lights": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_void_p,
+                                    C.c_void_p]),
+    "rg_proposal_param_count": (C.c_int64, [C.c_int32]),
+    "rg_proposal_create": (C.c_int, [C.c_void_p, C.POINTER(ProposalConfig), C.c_void_p, C.c_int32, C.c_void_p]),
+    "rg_proposal_destroy": (C.c_int, [C.c_void_p]),
+    "rg_proposal_set_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
+    "rg_proposal_get_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
+    "rg_proposal_infer": (C.c_int, [C.c_void_p, C.POINTER(GBuffer), C.POINTER(RestirUniforms), C.c_void_p]),
+    "rg_proposal_buffers": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+    "rg_proposal_gradients": (C.c_int, [C.c_void_p, C.POINTER(GBuffer), C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_int32, C.c_void_p, C.POINTER(C.c_double), C.c_void_p]),
+    "rg_proposal_train": (C.c_int, [C.c_void_p, C.POINTER(GBuffer), C.POINTER(RestirUniforms), C.c_void_p,
+                                    C.c_void_p]),
+    "rg_proposal_last_loss": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
 }
 
 EXPORTED = tuple(_SIGNATURES)

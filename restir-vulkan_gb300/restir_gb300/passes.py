@@ -188,3 +188,70 @@ class Context:
         s = _lib.Stats()
         check(lib().rg_get_stats(self._h, C.byref(s), int(reset)))
         return s
+
+    # ---- learned light-cluster proposal
+    def create_proposal(self, cluster_of: np.ndarray, clusters: int, *, mix: float = 0.9,
+                        learning_rate: float = 1e-3, batch: int = 65536, box_min=(0.0, 0.0, 0.0),
+                        box_max=(1.0, 1.0, 1.0), seed: int = 1):
+        pl = self.scene.point_lights
+        cfg = _lib.ProposalConfig(clusters, mix, learning_rate, batch, (C.c_float * 3)(*box_min),
+                                  (C.c_float * 3)(*box_max), seed)
+        co = np.ascontiguousarray(cluster_of, np.int32)
+        check(lib().rg_proposal_create(self._h, C.byref(cfg), _lib.ptr(pl), len(pl), _lib.ptr(co)))
+        self.proposal_clusters = clusters
+
+    def proposal_params(self) -> np.ndarray:
+        n = lib().rg_proposal_param_count(self.proposal_clusters)
+        out = np.empty(n, np.float32)
+        check(lib().rg_proposal_get_params(self._h, _lib.ptr(out), n))
+        return out
+
+    def set_proposal_params(self, params: np.ndarray):
+        p = np.ascontiguousarray(params, np.float32)
+        check(lib().rg_proposal_set_params(self._h, _lib.ptr(p), p.size))
+
+    def proposal_infer(self, g: DeviceGBuffer, uniforms, stream=None):
+        gs = g.struct()
+        check(lib().rg_proposal_infer(self._h, C.byref(gs), C.byref(uniforms), _stream_handle(stream)))
+
+    def proposal_buffers(self, n_pixels: int):
+        """(candidates [n_pixels x 32] as CANDIDATE_DTYPE, row stats [n_pixels x 4] float32), copied to host."""
+        torch = _torch()
+        cp, sp = C.c_void_p(), C.c_void_p()
+        check(lib().rg_proposal_buffers(self._h, C.byref(cp), C.byref(sp)))
+        torch.cuda.synchronize()
+        cand = torch.as_tensor(device_view(cp.value, n_pixels * 32 * 8), device="cuda").cpu().numpy()
+        stat = torch.as_tensor(device_view(sp.value, n_pixels * 16), device="cuda").cpu().numpy()
+        return cand.view(_lib.CANDIDATE_DTYPE).reshape(n_pixels, 32), stat.view(np.float32).reshape(n_pixels, 4)
+
+    def proposal_gradients(self, g: DeviceGBuffer, camera_pos, rows, targets):
+        """(gradient as a float32 device tensor, summed loss) for device int32 tensors rows, targets."""
+        torch = _torch()
+        n = lib().rg_proposal_param_count(self.proposal_clusters)
+        grad = torch.zeros(n, dtype=torch.float32, device="cuda")
+        cam = (C.c_float * 3)(*camera_pos)
+        loss = C.c_double()
+        gs = g.struct()
+        check(lib().rg_proposal_gradients(self._h, C.byref(gs), cam, _lib.ptr(rows), _lib.ptr(targets),
+                                          rows.shape[0], _lib.ptr(grad), C.byref(loss), None))
+        return grad, loss.value
+
+    def proposal_train(self, g: DeviceGBuffer, uniforms, final_res_ptr: int, stream=None):
+        gs = g.struct()
+        check(lib().rg_proposal_train(self._h, C.byref(gs), C.byref(uniforms), final_res_ptr,
+                                      _stream_handle(stream)))
+
+    def proposal_last_loss(self):
+        loss, cnt = C.c_double(), C.c_int64()
+        check(lib().rg_proposal_last_loss(self._h, C.byref(loss), C.byref(cnt)))
+        return loss.value, cnt.value
+
+
+def cluster_lights(point_lights: np.ndarray, k: int, iterations: int = 10, seed: int = 1):
+    """Seeded k-means of the point lights (host): (cluster_of int32 [n], centers float32 [k x 3])."""
+    n = len(point_lights)
+    cluster_of = np.empty(n, np.int32)
+    centers = np.empty((k, 3), np.float32)
+    pl = np.ascontiguousarray(point_lights)
+    check(lib().rg_cluster_lights(_lib.ptr(pl), n, k, iterations, seed, _lib.ptr(cluster_of), _lib.ptr(centers)))
+    return cluster_of, centers

@@ -56,3 +56,24 @@ def oracle_frame(scene, frame_index, g_cur, g_prev, prev_res, crop=None):
     img = np.zeros((scene.height, scene.width, 4), np.float32)
     ob.shade(scene, g_cur, r, scene.lighting_uniforms(frame_index), img, crop=crop)
     return stages, img
+
+
+def mlp_params(count, clusters, seed, scale_w4=0.3):
+    """Seeded parameters of the learned proposal's network (packed layout:
+    W1 16x64 with rows 9..15 zero, b1, W2, b2, W3, b3, W4 64xC, b4)."""
+    rng = np.random.default_rng(seed)
+    p = np.zeros(count, np.float32)
+    o = 0
+    for rows, cols, used in ((16, 64, 9), (64, 64, 64), (64, 64, 64)):
+        w = rng.uniform(-1, 1, (rows, cols)) * np.sqrt(6.0 / used)
+        w[used:] = 0.0
+        p[o:o + rows * cols] = w.ravel()
+        o += rows * cols
+        p[o:o + cols] = rng.uniform(-0.1, 0.1, cols)
+        o += cols
+    p[o:o + 64 * clusters] = rng.uniform(-scale_w4, scale_w4, 64 * clusters)
+    o += 64 * clusters
+    p[o:o + clusters] = rng.uniform(-1, 1, clusters)
+    o += clusters
+    assert o == count
+    return p

@@ -19,7 +19,7 @@ def P(a):
 
 def test_library_exports_every_declared_symbol(restir_lib):
     header = (ROOT / "include" / "restir_gb300.h").read_text()
-    declared = set(re.findall(r"^(?:int|const char \*)\s*\*?\s*(rg_\w+)\s*\(", header, re.M))
+    declared = set(re.findall(r"^(?:int64_t|int|const char \*)\s*\*?\s*(rg_\w+)\s*\(", header, re.M))
     assert len(declared) >= 18
     for name in sorted(declared):
         assert hasattr(restir_lib, name), name
