@@ -1099,10 +1099,14 @@ void or_mlp_row_stats(const or_mlp *m, const or_gbuffer *g, const float cam[3], 
     free(w);
 }
 
-/* The proposal's candidates of pixel rows[r] (keys/q: [n x n_cand]): the
- * same branch draws as the product (PCG stream frame*MUL+ADD, pixel), then the
- * learned-branch uniforms placed on the double-precision softmax CDF
- * (a uniform at or beyond the total takes the most probable cluster). */
+/* The proposal's candidates of pixel rows[r] (keys/q: [n x n_cand]), drawn
+ * from the pixel's PCG stream (seed frame*MUL+ADD, sequence pixel):
+ *   per slot j two draws u0, u1: u0 < mix makes j a learned slot, otherwise
+ *   the slot holds light min(floor(N*u1), N-1) with q of its cluster;
+ *   then the n learned slots' uniforms as ascending order statistics,
+ *   u_k = 1 - (1 - u_{k-1}) * V^(1/(n-k)) with one draw V each, the k-th going
+ *   to the k-th learned slot and placed on the double-precision softmax CDF
+ *   (a uniform at or beyond the total takes the most probable cluster). */
 void or_mlp_sample(const or_mlp *m, const or_gbuffer *g, const float cam[3], uint32_t frame, int32_t n_cand,
                    int32_t n, const int32_t *rows, int32_t *keys, float *qs) {
     const mlp_layout L = mlp_layout_of(m->clusters);
@@ -1121,27 +1125,32 @@ void or_mlp_sample(const or_mlp *m, const or_gbuffer *g, const float cam[3], uin
             int32_t amax = 0;
             const double lse = mlp_lse(z, m->clusters, &amax);
             pcg_t rng = pcg_seed((uint64_t)frame * MLP_SEED_MUL + MLP_SEED_ADD, (uint64_t)px);
+            int32_t learned[MLP_CAND];
+            int32_t n_u = 0;
             for (int32_t j = 0; j < n_cand; ++j) {
                 const float u0 = rand_float(&rng);
                 const float u1 = rand_float(&rng);
-                int32_t key;
-                double q;
                 if (u0 < m->mix) {
-                    double cum = 0.0;
-                    key = -1 - amax;
-                    q = exp(z[amax] - lse);
-                    for (int32_t c = 0; c < m->clusters; ++c) {
-                        const double pr = exp(z[c] - lse);
-                        cum += pr;
-                        if ((double)u1 < cum) { key = -1 - c; q = pr; break; }
-                    }
+                    learned[n_u++] = j;
                 } else {
                     const int32_t l = imin((int)((float)m->n_lights * u1), m->n_lights - 1);
-                    key = l;
-                    q = exp(z[m->cluster_of[l]] - lse);
+                    keys[(size_t)r * n_cand + j] = l;
+                    qs[(size_t)r * n_cand + j] = (float)exp(z[m->cluster_of[l]] - lse);
                 }
-                keys[(size_t)r * n_cand + j] = key;
-                qs[(size_t)r * n_cand + j] = (float)q;
+            }
+            float u = 0.0f;
+            int32_t c = 0;
+            double cum = exp(z[0] - lse);
+            for (int32_t k = 0; k < n_u; ++k) {
+                const float v = rand_float(&rng);
+                u = 1.0f - (1.0f - u) * powf(v, 1.0f / (float)(n_u - k));
+                while (c < m->clusters && !((double)u < cum)) {
+                    ++c;
+                    if (c < m->clusters) cum += exp(z[c] - lse);
+                }
+                const int32_t col = c < m->clusters ? c : amax;
+                keys[(size_t)r * n_cand + learned[k]] = -1 - col;
+                qs[(size_t)r * n_cand + learned[k]] = (float)exp(z[col] - lse);
             }
         }
         free(z);

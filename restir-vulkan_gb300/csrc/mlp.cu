@@ -3,20 +3,27 @@
 // The forward pass of a 128-pixel tile is one CTA on the tcgen05 tensor cores:
 // features -> x tile (shared memory, bf16) -> three 64-wide layers (MMA into
 // tensor memory, bias + ReLU + bf16 epilogue back into shared memory) -> the
-// cluster logit layer in chunks of 128 clusters, double-buffered in tensor
+// cluster logit layer in chunks of 64 clusters, double-buffered in tensor
 // memory so that the MMA of chunk c+1 runs under the epilogue of chunk c.
 // Weight tiles arrive by cp.async from bf16 images that are already in the MMA
 // operand layout.  Logits never leave the SM.  Three epilogues:
 //   kLse     log-sum-exp, arg-max and its probability per row;
-//   kSample  the proposal's candidates: each row walks its softmax CDF once,
-//            with its sorted uniforms and the clusters of its uniform-branch
-//            lights (the walk skips 32-column pieces that hold neither);
-//   kGrad    d(loss)/d(logits) = (softmax - onehot) / n as bf16 rows, and the
-//            cross-entropy loss, for training.
+// Exponentials are 2^x on the MUFU unit with the log2(e) scale folded into
+// one FMA per logit.
+//   kSample  the learned-branch candidates: each row walks its softmax CDF
+//            once with its uniforms drawn as ascending order statistics; a
+//            uniform's column is found by a branch-free count inside the
+//            32-column piece that holds it.  (The uniform-branch candidates,
+//            a light and q of its cluster, are written at the end of kLse.)
+//   kGrad    for training: dz = d(loss)/d(logits) = (softmax - onehot) / n
+//            per chunk into a bf16 tile, then dh3 += dz W4^T on the tensor
+//            cores (accumulated in tensor memory over the chunks), and the
+//            cross-entropy loss.  dz never leaves the SM; dW4 and db4 come
+//            from k_mlp_dw4, which recomputes the logits chunk by chunk.
 // Every wait on the tensor core is bounded; a CTA whose wait runs out records
 // an error, waits (bounded) for its last MMA, frees its tensor memory and
-// leaves.  At most two CTAs share an SM: each holds 256 tensor-memory columns
-// and asks for at least 80 KB of shared memory.
+// leaves.  At most four CTAs share an SM: each holds 128 tensor-memory
+// columns and uses more than a fifth of the shared memory.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
@@ -33,7 +40,8 @@ namespace {
 constexpr int kRows = 128;                 // rows (pixels) per CTA
 constexpr int kChunkN = mlp::kChunkN;      // clusters per logit MMA chunk
 constexpr uint32_t kMaxPolls = 1u << 26;   // bounded mbarrier waits
-constexpr int kTmemCols = 256;
+constexpr int kTmemCols = 2 * kChunkN;    // two chunk accumulators; the hidden layers use them first
+constexpr int kTmemColsGrad = 4 * kChunkN;  // kGrad: plus the dh3 accumulator (64 columns), rounded up
 
 // shared-memory map (bytes)
 constexpr int kOffX = 0;                               // x tile, 128 x 16 bf16
@@ -44,14 +52,67 @@ constexpr int kOffW3 = kOffW2 + mlp::kH * mlp::kH * 2;
 constexpr int kOffB = kOffW3 + mlp::kH * mlp::kH * 2;  // two chunk tiles, 128 x 64
 constexpr int kChunkBytes = kChunkN * mlp::kH * 2;
 constexpr int kOffBias = kOffB + 2 * kChunkBytes;      // b1 | b2 | b3
-constexpr int kOffRow = kOffBias + 3 * mlp::kH * 4;    // per-row arrays (kSample)
-constexpr int kRowBytes = mlp::kCand * kRows * (4 + 1 + 4);
-constexpr int kSmemMin = 80 * 1024;                    // caps residency at two CTAs per SM
+constexpr int kSmemUsed = kOffBias + 3 * mlp::kH * 4;
+// kGrad: the logit-gradient tile (128 rows x 64 clusters, K-major over
+// clusters) and two W4 chunk tiles (64 hidden x 64 clusters) for dh3 += dz W4^T
+constexpr int kOffDz = (kSmemUsed + 1023) / 1024 * 1024;
+constexpr int kOffWk = kOffDz + kRows * kChunkN * 2;
+constexpr int kWkBytes = mlp::kH * kChunkN * 2;
+constexpr int kSmemGrad = kOffWk + 2 * kWkBytes;
+constexpr int kSmemMin = 52 * 1024;                    // caps residency at four CTAs per SM (TMEM: 4 x 128 columns)
 constexpr int kWeightImgBytes = (mlp::kH * mlp::kIn + 2 * mlp::kH * mlp::kH) * 2;
 
 enum { kLse = 0, kSample = 1, kGrad = 2 };
 
 __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+constexpr float kLog2e = 1.44269504088896341f;
+// 2^x by the MUFU instruction (results below 2^-126 flush to zero)
+__device__ __forceinline__ float ex2(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float max32(const float (&v)[32]) {
+    float a[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) a[i] = fmaxf(v[2 * i], v[2 * i + 1]);
+#pragma unroll
+    for (int w = 8; w >= 1; w >>= 1)
+#pragma unroll
+        for (int i = 0; i < w; ++i) a[i] = fmaxf(a[i], a[i + w]);
+    return a[0];
+}
+__device__ __forceinline__ float sum32(const float (&v)[32]) {
+    float a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = (v[i] + v[i + 8]) + (v[i + 16] + v[i + 24]);
+    return ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+}
+// Next of n ascending order statistics of U(0,1) given the previous one:
+// 1 - (1 - prev) * V^(1/remaining), V uniform.
+__device__ __forceinline__ float next_order_stat(Pcg &rng, float prev, int remaining) {
+    const float v = rand_float(rng);
+    return 1.0f - (1.0f - prev) * powf(v, 1.0f / (float)remaining);
+}
+// z of cluster cl for the row whose h3 is h: FP32 dot with the bf16 W4^T
+// image (chunk tiles in the MMA operand layout) plus b4.
+__device__ __forceinline__ float logit_of(const mlp::ProposalDev &pd, const float (&h)[64], int cl) {
+    const unsigned char *tile = reinterpret_cast<const unsigned char *>(pd.w4t) + (size_t)(cl / kChunkN) * kChunkBytes;
+    float z = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const uint4 w = __ldg(reinterpret_cast<const uint4 *>(tile + umma::kmajor_offset(cl % kChunkN, 8 * j, mlp::kH)));
+        const __nv_bfloat162 *b = reinterpret_cast<const __nv_bfloat162 *>(&w);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const float2 f = __bfloat1622float2(b[i]);
+            z += h[8 * j + 2 * i] * f.x;
+            z += h[8 * j + 2 * i + 1] * f.y;
+        }
+    }
+    return z + __ldg(pd.b4e + cl);
+}
 
 __device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(umma::smem_addr(smem_dst)), "l"(gsrc)
@@ -76,7 +137,7 @@ struct FusedParams {
     int save;
     __nv_bfloat16 *x, *h1, *h2, *h3;  // [n x 16], [n x 64] x 3
     const int32_t *target;     // cluster per row, -1: no target
-    __nv_bfloat16 *dz;         // [n x C]
+    float *dh3;                // [n x 64] FP32: d(loss)/d(h3)
     float inv_n;
     float *loss_sum;
     // sampling
@@ -129,10 +190,11 @@ __device__ __forceinline__ bool mma_wait(uint64_t *mbar, uint32_t parity) {
 }
 
 template <int kMode>
-__global__ void __launch_bounds__(128, 1) k_mlp_fused(const FusedParams p) {
+__global__ void __launch_bounds__(128, 4) k_mlp_fused(const FusedParams p) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    __shared__ uint64_t mbar_layer, mbar_chunk[2];
+    __shared__ uint64_t mbar_layer, mbar_chunk[2], mbar_dh;
     __shared__ uint32_t tmem_base;
+    constexpr int kCols = kMode == kGrad ? kTmemColsGrad : kTmemCols;
     const int tid = threadIdx.x, warp = tid >> 5;
     const int row = blockIdx.x * kRows + tid;
     const bool valid = row < p.n;
@@ -144,21 +206,30 @@ __global__ void __launch_bounds__(128, 1) k_mlp_fused(const FusedParams p) {
     float *bias = reinterpret_cast<float *>(smem + kOffBias);
     const unsigned char *w4img = reinterpret_cast<const unsigned char *>(p.pd.w4t);
 
+    unsigned char *dztile = smem + kOffDz;
+    unsigned char *wkslot[2] = {smem + kOffWk, smem + kOffWk + kWkBytes};
+    const unsigned char *w4kimg = reinterpret_cast<const unsigned char *>(p.pd.w4k);
+
     // weights and the first two logit chunks start moving
     copy_bytes(smem + kOffW1, reinterpret_cast<const unsigned char *>(p.pd.w123img), kWeightImgBytes);
     copy_bytes(btile[0], w4img, kChunkBytes);
+    if (kMode == kGrad) copy_bytes(wkslot[0], w4kimg, kWkBytes);
     cp_async_commit();
-    if (nch > 1) copy_bytes(btile[1], w4img + kChunkBytes, kChunkBytes);
+    if (nch > 1) {
+        copy_bytes(btile[1], w4img + kChunkBytes, kChunkBytes);
+        if (kMode == kGrad) copy_bytes(wkslot[1], w4kimg + kWkBytes, kWkBytes);
+    }
     cp_async_commit();
     for (int i = tid; i < 3 * mlp::kH; i += blockDim.x) {
         const size_t b = i < mlp::kH ? L.b1 : i < 2 * mlp::kH ? L.b2 : L.b3;
         bias[i] = p.pd.params[b + (size_t)(i % mlp::kH)];
     }
-    if (warp == 0) umma::tmem_alloc(&tmem_base, kTmemCols);
+    if (warp == 0) umma::tmem_alloc(&tmem_base, kCols);
     if (tid == 0) {
         umma::mbar_init(&mbar_layer, 1);
         umma::mbar_init(&mbar_chunk[0], 1);
         umma::mbar_init(&mbar_chunk[1], 1);
+        umma::mbar_init(&mbar_dh, 1);
     }
     {
         float x[mlp::kIn];
@@ -176,38 +247,22 @@ __global__ void __launch_bounds__(128, 1) k_mlp_fused(const FusedParams p) {
         }
     }
 
-    // kSample: the row's branches and uniforms from a PCG stream of its own
-    float *u_val = reinterpret_cast<float *>(smem + kOffRow);          // [kCand][128]
-    uint8_t *u_slot = reinterpret_cast<uint8_t *>(u_val + mlp::kCand * kRows);
-    int32_t *lk = reinterpret_cast<int32_t *>(u_slot + mlp::kCand * kRows);  // cluster << 5 | slot
-    int n_u = 0, n_lk = 0;
+    // kSample: which candidate slots take the learned branch, and the learned
+    // slots' uniforms as ascending order statistics, from the pixel's own PCG
+    // stream (two draws per slot: branch, uniform light; then one per
+    // learned slot).  The k-th smallest uniform goes to the k-th learned slot.
+    uint32_t lmask = 0;  // learned slots not yet assigned
+    int n_u = 0, k_u = 0;
+    float u_prev = 0.0f;
+    Pcg rng{};
     if (kMode == kSample && valid) {
-        Pcg rng = pcg_seed((uint64_t)p.frame * mlp::kSeedMul + mlp::kSeedAdd, (uint64_t)px);
-        mlp::Candidate *out = p.cand + (size_t)row * mlp::kCand;
+        rng = pcg_seed((uint64_t)p.frame * mlp::kSeedMul + mlp::kSeedAdd, (uint64_t)px);
         for (int j = 0; j < p.n_cand; ++j) {
             const float u0 = rand_float(rng);
-            const float u1 = rand_float(rng);
-            if (u0 < p.pd.mix) {
-                int k = n_u++;
-                while (k > 0 && u_val[(k - 1) * kRows + tid] > u1) {
-                    u_val[k * kRows + tid] = u_val[(k - 1) * kRows + tid];
-                    u_slot[k * kRows + tid] = u_slot[(k - 1) * kRows + tid];
-                    --k;
-                }
-                u_val[k * kRows + tid] = u1;
-                u_slot[k * kRows + tid] = (uint8_t)j;
-            } else {
-                const int l = imin((int)((float)p.pd.n_lights * u1), p.pd.n_lights - 1);
-                const int32_t key = (p.pd.cluster_of[l] << 5) | j;
-                out[j] = mlp::Candidate{l, 0.0f};
-                int k = n_lk++;
-                while (k > 0 && lk[(k - 1) * kRows + tid] > key) {
-                    lk[k * kRows + tid] = lk[(k - 1) * kRows + tid];
-                    --k;
-                }
-                lk[k * kRows + tid] = key;
-            }
+            rand_float(rng);
+            if (u0 < p.pd.mix) lmask |= 1u << j;
         }
+        n_u = __popc(lmask);
     }
 
     cp_async_wait_one();
@@ -217,24 +272,30 @@ __global__ void __launch_bounds__(128, 1) k_mlp_fused(const FusedParams p) {
     umma::fence_after_sync();
     const uint32_t tmem = tmem_base;
     bool ok = true;
-    int issued = 0;          // logit chunks whose MMA was issued
-    int layer_commits = 0;
+    // thread 0's most recent MMA commit (the barrier and the parity of that
+    // phase): on a timeout it waits, bounded, for that commit, which covers
+    // every MMA issued before it
+    uint64_t *last_mbar = nullptr;
+    uint32_t last_parity = 0;
 
     // ---- hidden layers: MMA into columns 64*l, epilogue into the h tile
     const unsigned char *wimg[3] = {smem + kOffW1, smem + kOffW2, smem + kOffW3};
     __nv_bfloat16 *hsave[3] = {p.h1, p.h2, p.h3};
     for (int l = 0; l < 3 && ok; ++l) {
+        // layer l accumulates in columns 64*(l&1): layer 3 reuses layer 1's,
+        // whose loads completed before the barrier that preceded layer 2
+        const uint32_t lcol = tmem + (uint32_t)(64 * (l & 1));
         if (tid == 0) {
-            umma::mma_chunk(tmem + (uint32_t)(64 * l), l == 0 ? xtile : htile, wimg[l], l == 0 ? mlp::kIn : mlp::kH,
-                            kRows, mlp::kH, false);
+            umma::mma_chunk(lcol, l == 0 ? xtile : htile, wimg[l], l == 0 ? mlp::kIn : mlp::kH, kRows, mlp::kH, false);
             umma::mma_commit(&mbar_layer);
+            last_mbar = &mbar_layer;
+            last_parity = (uint32_t)(l & 1);
         }
-        ++layer_commits;
         const bool w = mma_wait(&mbar_layer, (uint32_t)(l & 1));
         if (w) {
             float v[64];
-            umma::tmem_ld32(tmem + (uint32_t)(64 * l), warp, 0, *reinterpret_cast<float(*)[32]>(v));
-            umma::tmem_ld32(tmem + (uint32_t)(64 * l), warp, 32, *reinterpret_cast<float(*)[32]>(v + 32));
+            umma::tmem_ld32(lcol, warp, 0, *reinterpret_cast<float(*)[32]>(v));
+            umma::tmem_ld32(lcol, warp, 32, *reinterpret_cast<float(*)[32]>(v + 32));
 #pragma unroll
             for (int j = 0; j < 64; ++j) v[j] = bf16r(fmaxf(v[j] + bias[64 * l + j], 0.0f));
 #pragma unroll
@@ -254,26 +315,49 @@ __global__ void __launch_bounds__(128, 1) k_mlp_fused(const FusedParams p) {
     float m = -INFINITY, s = 0.0f;  // kLse: running max and sum
     int amax = 0;
     float lse = 0.0f, cum = 0.0f;   // kSample / kGrad
-    int iu = 0, ik = 0;
     float next_u = INFINITY;  // no uniform left (cum never exceeds it, even when it overflows)
-    int next_lk = p.pd.c;
+    int amax_row = 0;
+    float qmax_row = 0.0f;
     int target = -1;
     float zt = 0.0f;
     if (kMode != kLse && valid) {
-        lse = p.stat[row].x;
+        const float4 st = p.stat[row];
+        lse = st.x;
+        amax_row = __float_as_int(st.y);
+        qmax_row = st.z;
         if (kMode == kSample) {
-            if (n_u > 0) next_u = u_val[tid];
-            if (n_lk > 0) next_lk = lk[tid] >> 5;
+            if (n_u > 0) {
+                u_prev = next_order_stat(rng, 0.0f, n_u);
+                k_u = 1;
+                next_u = u_prev;
+            }
         } else {
             target = p.target[row];
         }
     }
-    if (ok) {
-        if (tid == 0) {
-            umma::mma_chunk(tmem, htile, btile[0], mlp::kH, kRows, kChunkN, false);
-            umma::mma_commit(&mbar_chunk[0]);
+    const float nl2 = -lse * kLog2e;
+    // kSample: the learned slot of the current uniform gets cluster col with q
+    auto take = [&](int col, float q) {
+        if (!(q > 0.0f)) {  // rounding put the uniform on an empty column: the most probable cluster
+            col = amax_row;
+            q = qmax_row;
         }
-        issued = 1;
+        const int slot = __ffs(lmask) - 1;
+        lmask &= lmask - 1;
+        p.cand[(size_t)row * mlp::kCand + slot] = mlp::Candidate{-1 - col, q};
+        if (k_u < n_u) {
+            u_prev = next_order_stat(rng, u_prev, n_u - k_u);
+            ++k_u;
+            next_u = u_prev;
+        } else {
+            next_u = INFINITY;
+        }
+    };
+    if (ok && tid == 0) {
+        umma::mma_chunk(tmem, htile, btile[0], mlp::kH, kRows, kChunkN, false);
+        umma::mma_commit(&mbar_chunk[0]);
+        last_mbar = &mbar_chunk[0];
+        last_parity = 0;
     }
     // `ok` changes only at block barriers (uniform); `ok_warp` records this
     // warp's waits and joins `ok` at the next barrier, so every warp passes
@@ -292,20 +376,28 @@ __global__ void __launch_bounds__(128, 1) k_mlp_fused(const FusedParams p) {
                 umma::mma_chunk(tmem + (uint32_t)(((c + 1) & 1) * kChunkN), htile, btile[(c + 1) & 1], mlp::kH, kRows,
                                 kChunkN, false);
                 umma::mma_commit(&mbar_chunk[(c + 1) & 1]);
+                last_mbar = &mbar_chunk[(c + 1) & 1];
+                last_parity = (uint32_t)(((c + 1) >> 1) & 1);
             }
-            issued = c + 2;
         }
         const bool w = mma_wait(&mbar_chunk[c & 1], (uint32_t)((c >> 1) & 1));
         ok_warp = ok_warp && w;
-        if (!w) continue;
+        if (w) {
         if (c + 2 < nch) {
             copy_bytes(btile[c & 1], w4img + (size_t)(c + 2) * kChunkBytes, kChunkBytes);
             cp_async_commit();
         }
         const uint32_t half = tmem + (uint32_t)((c & 1) * kChunkN);
+        uint32_t raw[2][32];
+        umma::tmem_ld32_issue(half, warp, 0, raw[0]);
+#pragma unroll
         for (int piece = 0; piece < kChunkN / 32; ++piece) {
+            umma::tmem_ld32_wait(raw[piece & 1]);
+            // the next piece's load runs under this piece's arithmetic
+            if (piece + 1 < kChunkN / 32) umma::tmem_ld32_issue(half, warp, (piece + 1) * 32, raw[(piece + 1) & 1]);
             float v[32];
-            umma::tmem_ld32(half, warp, piece * 32, v);
+#pragma unroll
+            for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(raw[piece & 1][i]);
             const int col0 = c * kChunkN + piece * 32;
             const float4 *be = reinterpret_cast<const float4 *>(p.pd.b4e + col0);
 #pragma unroll
@@ -314,86 +406,128 @@ __global__ void __launch_bounds__(128, 1) k_mlp_fused(const FusedParams p) {
                 v[4 * q] += b.x; v[4 * q + 1] += b.y; v[4 * q + 2] += b.z; v[4 * q + 3] += b.w;
             }
             if (kMode == kLse) {
-                float mp = v[0];
-#pragma unroll
-                for (int i = 1; i < 32; ++i) mp = fmaxf(mp, v[i]);
+                const float mp = max32(v);
                 if (mp == -INFINITY) continue;
-                float sp = 0.0f;
-#pragma unroll
-                for (int i = 0; i < 32; ++i) sp += __expf(v[i] - mp);
                 if (mp > m) {
-                    s = (m == -INFINITY) ? sp : s * __expf(m - mp) + sp;
-                    m = mp;
 #pragma unroll
                     for (int i = 31; i >= 0; --i)
                         if (v[i] == mp) amax = col0 + i;
+                }
+                const float nm = -mp * kLog2e;
+#pragma unroll
+                for (int i = 0; i < 32; ++i) v[i] = ex2(__fmaf_rn(v[i], kLog2e, nm));
+                const float sp = sum32(v);
+                if (mp > m) {
+                    s = (m == -INFINITY) ? sp : __fmaf_rn(s, ex2((m - mp) * kLog2e), sp);
+                    m = mp;
                 } else {
-                    s += sp * __expf(mp - m);
+                    s = __fmaf_rn(sp, ex2((mp - m) * kLog2e), s);
                 }
             } else if (kMode == kSample) {
                 if (!valid) continue;
-                float pr[32], psum = 0.0f;
 #pragma unroll
-                for (int i = 0; i < 32; ++i) {
-                    pr[i] = __expf(v[i] - lse);
-                    psum += pr[i];
-                }
-                if (next_u < cum + psum || next_lk < col0 + 32) {
-                    mlp::Candidate *out = p.cand + (size_t)row * mlp::kCand;
+                for (int i = 0; i < 32; ++i) v[i] = ex2(__fmaf_rn(v[i], kLog2e, nl2));
+                const float end = cum + sum32(v);
+                // each uniform below `end` belongs to this piece: its column is
+                // the first whose running sum exceeds it (at most the last)
+                while (next_u < end) {
+                    float c = cum, q = v[0];
+                    int idx = 0;
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) {
-                        cum += pr[i];
-                        while (next_u < cum) {
-                            out[u_slot[iu * kRows + tid]] = mlp::Candidate{-1 - (col0 + i), pr[i]};
-                            ++iu;
-                            next_u = iu < n_u ? u_val[iu * kRows + tid] : INFINITY;
-                        }
-                        while (next_lk == col0 + i) {
-                            out[lk[ik * kRows + tid] & 31].q = pr[i];
-                            ++ik;
-                            next_lk = ik < n_lk ? lk[ik * kRows + tid] >> 5 : p.pd.c;
-                        }
+                    for (int i = 0; i < 31; ++i) {
+                        c += v[i];
+                        const bool past = c <= next_u;
+                        idx += past ? 1 : 0;
+                        q = past ? v[i + 1] : q;
                     }
-                } else {
-                    cum += psum;
+                    take(col0 + idx, q);
                 }
-            } else {  // kGrad
+                cum = end;
+            } else {  // kGrad: the gradient rows go to the dz tile (bf16)
                 float d[32];
 #pragma unroll
                 for (int i = 0; i < 32; ++i) {
-                    const float pr = __expf(v[i] - lse);
+                    const float pr = ex2(__fmaf_rn(v[i], kLog2e, nl2));
                     const bool hit = (col0 + i) == target;
                     if (hit) zt = v[i];
                     d[i] = target < 0 ? 0.0f : (pr - (hit ? 1.0f : 0.0f)) * p.inv_n;
                 }
-                if (valid) {
-                    __nv_bfloat16 *dst = p.dz + (size_t)row * p.pd.c + col0;
 #pragma unroll
-                    for (int q = 0; q < 32; q += 8) store8(dst + q, d + q);
-                }
+                for (int q = 0; q < 32; q += 8) put8(dztile, tid, piece * 32 + q, kChunkN, d + q);
             }
         }
+        }  // w
         umma::fence_before_sync();
+        if (kMode == kGrad) {
+            // dh3 += dz_tile . W4[:, chunk]^T once every row's gradient is in the tile
+            umma::fence_proxy_async();
+            ok = __syncthreads_and(ok && ok_warp) != 0;
+            umma::fence_after_sync();
+            if (!ok) break;
+            if (tid == 0) {
+                umma::mma_chunk(tmem + (uint32_t)(2 * kChunkN), dztile, wkslot[c & 1], kChunkN, kRows, mlp::kH, c > 0);
+                umma::mma_commit(&mbar_dh);
+                last_mbar = &mbar_dh;
+                last_parity = (uint32_t)(c & 1);
+            }
+            const bool w2 = mma_wait(&mbar_dh, (uint32_t)(c & 1));
+            ok_warp = ok_warp && w2;
+            if (w2 && c + 2 < nch) {  // the slot is free once this product completed
+                copy_bytes(wkslot[c & 1], w4kimg + (size_t)(c + 2) * kWkBytes, kWkBytes);
+                cp_async_commit();
+            }
+        }
     }
     ok = __syncthreads_and(ok && ok_warp) != 0;
     if (!ok) {
         if (tid == 0) {
             atomicAdd(p.err, 1);
-            if (issued > 0)
-                umma::mbar_wait(&mbar_chunk[(issued - 1) & 1], (uint32_t)(((issued - 1) >> 1) & 1), kMaxPolls);
-            else if (layer_commits > 0)
-                umma::mbar_wait(&mbar_layer, (uint32_t)((layer_commits - 1) & 1), kMaxPolls);
+            if (last_mbar) umma::mbar_wait(last_mbar, last_parity, kMaxPolls);
         }
         cp_async_wait_all();
     } else if (valid) {
         if (kMode == kLse) {
             const float lse_row = m + __logf(s);
-            p.stat[row] = make_float4(lse_row, __int_as_float(amax), __expf(m - lse_row), 0.0f);
+            p.stat[row] = make_float4(lse_row, __int_as_float(amax), ex2((m - lse_row) * kLog2e), 0.0f);
+            if (p.cand) {
+                // uniform-branch candidates: the light and q of its cluster (the
+                // same PCG stream as the learned branch's draws in kSample)
+                float h[64];
+#pragma unroll
+                for (int j = 0; j < 64; j += 8) {
+                    const uint4 w = *reinterpret_cast<const uint4 *>(htile + umma::kmajor_offset(tid, j, mlp::kH));
+                    const __nv_bfloat162 *b = reinterpret_cast<const __nv_bfloat162 *>(&w);
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const float2 f = __bfloat1622float2(b[i]);
+                        h[j + 2 * i] = f.x;
+                        h[j + 2 * i + 1] = f.y;
+                    }
+                }
+                Pcg r2 = pcg_seed((uint64_t)p.frame * mlp::kSeedMul + mlp::kSeedAdd, (uint64_t)px);
+                const float nl = -lse_row * kLog2e;
+                for (int j = 0; j < p.n_cand; ++j) {
+                    const float u0 = rand_float(r2);
+                    const float u1 = rand_float(r2);
+                    if (u0 < p.pd.mix) continue;
+                    const int l = imin((int)((float)p.pd.n_lights * u1), p.pd.n_lights - 1);
+                    const float z = logit_of(p.pd, h, __ldg(p.pd.cluster_of + l));
+                    p.cand[(size_t)row * mlp::kCand + j] = mlp::Candidate{l, ex2(__fmaf_rn(z, kLog2e, nl))};
+                }
+            }
         } else if (kMode == kSample) {
-            // a uniform beyond the rounded CDF total: the most probable cluster
-            const float4 st = p.stat[row];
-            mlp::Candidate *out = p.cand + (size_t)row * mlp::kCand;
-            for (; iu < n_u; ++iu) out[u_slot[iu * kRows + tid]] = mlp::Candidate{-1 - __float_as_int(st.y), st.z};
+            // uniforms beyond the rounded CDF total: the most probable cluster
+            while (next_u < INFINITY) take(amax_row, qmax_row);
+        }
+    }
+    if (kMode == kGrad && ok) {
+        float d[64];
+        umma::tmem_ld32(tmem + (uint32_t)(2 * kChunkN), warp, 0, *reinterpret_cast<float(*)[32]>(d));
+        umma::tmem_ld32(tmem + (uint32_t)(2 * kChunkN), warp, 32, *reinterpret_cast<float(*)[32]>(d + 32));
+        if (valid) {
+            float4 *dst = reinterpret_cast<float4 *>(p.dh3 + (size_t)row * mlp::kH);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) dst[j] = make_float4(d[4 * j], d[4 * j + 1], d[4 * j + 2], d[4 * j + 3]);
         }
     }
     if (kMode == kGrad && ok) {
@@ -403,7 +537,172 @@ __global__ void __launch_bounds__(128, 1) k_mlp_fused(const FusedParams p) {
     }
     umma::fence_before_sync();
     __syncthreads();
-    if (warp == 0) umma::tmem_dealloc(tmem, kTmemCols);
+    if (warp == 0) umma::tmem_dealloc(tmem, kCols);
+}
+
+// ---------------------------------------------------------------- dW4, db4
+// One CTA per (chunk of 64 clusters, slice of row tiles).  Per 128-row tile:
+// the chunk's logits z = h3 . W4[:, chunk] on the tensor cores, the bf16
+// gradient dz = (softmax - onehot) / n as in kGrad (same formula, so the same
+// values), then dW[0..63] += h3^T dz and dW[64] += 1^T dz (db4) as one MMA
+// with M = 128 (rows 0..63: h3^T, row 64: ones for the valid rows, rows
+// 65..127: zero) and K = the tile's 128 rows, accumulated in tensor memory;
+// the CTA adds its 65 x 64 result to the gradient with atomics at the end.
+// Both transposed operands are written element-wise into the K-major layout.
+struct Dw4Params {
+    mlp::ProposalDev pd;
+    const __nv_bfloat16 *h3;   // [n x 64]
+    const float4 *stat;        // lse per row
+    const int32_t *target;
+    int n, tiles_per_slice;
+    float inv_n;
+    float *gw4, *gb4;          // gradient blocks of W4 (64 x C) and b4
+    int *err;
+};
+
+constexpr int kDwOffBz = 0;                                 // W4^T chunk (64 x 64, K = hidden)
+constexpr int kDwOffH = kDwOffBz + kChunkBytes;             // h3 tile (128 x 64, K = hidden)
+constexpr int kDwOffHt = kDwOffH + kRows * mlp::kH * 2;     // [h3 | 1 | 0]^T (128 x 128, K = rows)
+constexpr int kDwOffDzt = kDwOffHt + 128 * kRows * 2;       // dz^T (64 x 128, K = rows)
+constexpr int kDwSmem = kDwOffDzt + kChunkN * kRows * 2;
+
+__global__ void __launch_bounds__(128) k_mlp_dw4(const Dw4Params p) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint64_t mbar_z, mbar_w;
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int chunk = blockIdx.x;
+    const int t0 = blockIdx.y * p.tiles_per_slice;
+    const int t1 = min((p.n + kRows - 1) / kRows, t0 + p.tiles_per_slice);
+    unsigned char *bz = smem + kDwOffBz, *ht = smem + kDwOffH, *htt = smem + kDwOffHt, *dzt = smem + kDwOffDzt;
+    copy_bytes(bz, reinterpret_cast<const unsigned char *>(p.pd.w4t) + (size_t)chunk * kChunkBytes, kChunkBytes);
+    cp_async_commit();
+    for (int i = tid; i < 128 * kRows / 8; i += blockDim.x)  // zero [h3 | 1 | 0]^T (rows 65..127 stay zero)
+        reinterpret_cast<uint4 *>(htt)[i] = make_uint4(0, 0, 0, 0);
+    if (warp == 0) umma::tmem_alloc(&tmem_base, 128);
+    if (tid == 0) {
+        umma::mbar_init(&mbar_z, 1);
+        umma::mbar_init(&mbar_w, 1);
+    }
+    cp_async_wait_all();
+    umma::fence_proxy_async();
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tmem_base;
+    bool ok = t0 < t1, ok_warp = true;
+    uint64_t *last_mbar = nullptr;
+    uint32_t last_parity = 0;
+    const float4 *be = reinterpret_cast<const float4 *>(p.pd.b4e + chunk * kChunkN);
+    for (int t = t0; t < t1 && ok; ++t) {
+        const int k = t - t0;
+        if (k > 0) ok_warp = ok_warp && mma_wait(&mbar_w, (uint32_t)((k - 1) & 1));  // previous tile's operands free
+        const int row = t * kRows + tid;
+        const bool valid = row < p.n;
+        float h[64];
+        if (valid) {
+            const uint4 *src = reinterpret_cast<const uint4 *>(p.h3 + (size_t)row * mlp::kH);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const uint4 w = src[j];
+                *reinterpret_cast<uint4 *>(ht + umma::kmajor_offset(tid, 8 * j, mlp::kH)) = w;
+                const __nv_bfloat162 *b = reinterpret_cast<const __nv_bfloat162 *>(&w);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const float2 f = __bfloat1622float2(b[i]);
+                    h[8 * j + 2 * i] = f.x;
+                    h[8 * j + 2 * i + 1] = f.y;
+                }
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < 64; ++j) h[j] = 0.0f;
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                *reinterpret_cast<uint4 *>(ht + umma::kmajor_offset(tid, 8 * j, mlp::kH)) = make_uint4(0, 0, 0, 0);
+        }
+#pragma unroll
+        for (int j = 0; j < 64; ++j)
+            *reinterpret_cast<__nv_bfloat16 *>(htt + umma::kmajor_offset(j, tid, kRows)) = __float2bfloat16_rn(h[j]);
+        *reinterpret_cast<__nv_bfloat16 *>(htt + umma::kmajor_offset(64, tid, kRows)) =
+            __float2bfloat16_rn(valid ? 1.0f : 0.0f);
+        umma::fence_proxy_async();
+        umma::fence_before_sync();
+        ok = __syncthreads_and(ok_warp) != 0;
+        umma::fence_after_sync();
+        if (!ok) break;
+        if (tid == 0) {
+            umma::mma_chunk(tmem, ht, bz, mlp::kH, kRows, kChunkN, false);
+            umma::mma_commit(&mbar_z);
+            last_mbar = &mbar_z;
+            last_parity = (uint32_t)(k & 1);
+        }
+        const bool w = mma_wait(&mbar_z, (uint32_t)(k & 1));
+        ok_warp = ok_warp && w;
+        if (w) {
+            float lse = 0.0f;
+            int target = -1;
+            if (valid) {
+                lse = p.stat[row].x;
+                target = p.target[row];
+            }
+            const float nl2 = -lse * kLog2e;
+#pragma unroll
+            for (int piece = 0; piece < kChunkN / 32; ++piece) {
+                float v[32];
+                umma::tmem_ld32(tmem, warp, piece * 32, v);
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const float4 b = __ldg(be + piece * 8 + q);
+                    v[4 * q] += b.x; v[4 * q + 1] += b.y; v[4 * q + 2] += b.z; v[4 * q + 3] += b.w;
+                }
+#pragma unroll
+                for (int i = 0; i < 32; ++i) {
+                    const int col = chunk * kChunkN + piece * 32 + i;
+                    const float pr = ex2(__fmaf_rn(v[i], kLog2e, nl2));
+                    const float d = target < 0 ? 0.0f : (pr - (col == target ? 1.0f : 0.0f)) * p.inv_n;
+                    *reinterpret_cast<__nv_bfloat16 *>(dzt + umma::kmajor_offset(piece * 32 + i, tid, kRows)) =
+                        __float2bfloat16_rn(d);
+                }
+            }
+        }
+        umma::fence_proxy_async();
+        umma::fence_before_sync();
+        ok = __syncthreads_and(ok_warp) != 0;
+        umma::fence_after_sync();
+        if (!ok) break;
+        if (tid == 0) {
+            umma::mma_chunk(tmem + 64, htt, dzt, kRows, 128, kChunkN, k > 0);
+            umma::mma_commit(&mbar_w);
+            last_mbar = &mbar_w;
+            last_parity = (uint32_t)(k & 1);
+        }
+    }
+    if (ok && t1 > t0) ok_warp = ok_warp && mma_wait(&mbar_w, (uint32_t)((t1 - t0 - 1) & 1));
+    ok = __syncthreads_and(ok && ok_warp) != 0;
+    if (!ok && t1 > t0) {
+        if (tid == 0) {
+            atomicAdd(p.err, 1);
+            if (last_mbar) umma::mbar_wait(last_mbar, last_parity, kMaxPolls);
+        }
+    } else if (ok && warp < 3) {
+        // lanes 0..63: dW4 rows (hidden unit), lane 64: db4
+        const int m = tid;
+#pragma unroll
+        for (int piece = 0; piece < kChunkN / 32; ++piece) {
+            float v[32];
+            umma::tmem_ld32(tmem + 64, warp, piece * 32, v);
+            if (m <= 64) {
+                float *dst = m < 64 ? p.gw4 + (size_t)m * p.pd.c + chunk * kChunkN + piece * 32
+                                    : p.gb4 + chunk * kChunkN + piece * 32;
+#pragma unroll
+                for (int i = 0; i < 32; ++i) atomicAdd(dst + i, v[i]);
+            }
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, 128);
 }
 
 // ---------------------------------------------------------------- training helpers
@@ -473,10 +772,13 @@ __global__ void k_adam(float *w, const float *g, float *m, float *v, size_t n, f
 }
 
 // bf16 images of the weights: W1^T | W2^T | W3^T in the MMA operand layout
-// (w123img), W4^T in 128-cluster chunk tiles (w4t), W1 | W2 | W3 row-major
-// (w123), W4 row-major (w4), and b4 with -inf for clusters without lights.
+// (w123img), W4^T in chunk tiles (w4t: cluster x hidden, K-major over
+// hidden), W4 in chunk tiles (w4k: hidden x cluster, K-major over clusters),
+// W1 | W2 | W3 row-major (w123), W4 row-major (w4), and b4 with -inf for
+// clusters without lights.
 __global__ void k_refresh(const float *params, int c, const uint8_t *valid, __nv_bfloat16 *w123img,
-                          __nv_bfloat16 *w4t, __nv_bfloat16 *w123, __nv_bfloat16 *w4, float *b4e) {
+                          __nv_bfloat16 *w4t, __nv_bfloat16 *w4k, __nv_bfloat16 *w123, __nv_bfloat16 *w4,
+                          float *b4e) {
     const mlp::Layout L(c);
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t n1 = (size_t)mlp::kIn * mlp::kH, n2 = (size_t)mlp::kH * mlp::kH;
@@ -502,6 +804,8 @@ __global__ void k_refresh(const float *params, int c, const uint8_t *valid, __nv
         w4[e] = b;
         unsigned char *tile = reinterpret_cast<unsigned char *>(w4t) + (size_t)(cl / kChunkN) * kChunkBytes;
         *reinterpret_cast<__nv_bfloat16 *>(tile + umma::kmajor_offset(cl % kChunkN, k, mlp::kH)) = b;
+        unsigned char *ktile = reinterpret_cast<unsigned char *>(w4k) + (size_t)(cl / kChunkN) * kWkBytes;
+        *reinterpret_cast<__nv_bfloat16 *>(ktile + umma::kmajor_offset(k, cl % kChunkN, kChunkN)) = b;
     } else if (i < n1 + 2 * n2 + (size_t)(mlp::kH + 1) * c) {
         const size_t cl = i - n1 - 2 * n2 - (size_t)mlp::kH * c;
         b4e[cl] = valid[cl] ? params[L.b4 + cl] : -INFINITY;
@@ -532,7 +836,7 @@ __global__ void k_batch_rows(int32_t *rows, int n, uint32_t pixels, uint32_t off
 template <int kMode>
 cudaError_t launch_fused(const FusedParams &p, cudaStream_t st) {
     if (p.pd.c % kChunkN != 0 || p.pd.c < kChunkN) return cudaErrorInvalidValue;
-    int smem = kOffRow + (kMode == kSample ? kRowBytes : 0);
+    int smem = kMode == kGrad ? kSmemGrad : kSmemUsed;
     if (smem < kSmemMin) smem = kSmemMin;
     cudaError_t e = cudaFuncSetAttribute(k_mlp_fused<kMode>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
@@ -548,10 +852,13 @@ namespace mlp {
 size_t weight_image_bytes() { return (size_t)kWeightImgBytes; }
 
 cudaError_t forward_lse(const ProposalDev &pd, const GBufView &g, const float cam[3], const int32_t *rows, int n,
-                        float4 *stat, const TrainBuffers *save, int *err, cudaStream_t st) {
+                        float4 *stat, const TrainBuffers *save, uint32_t frame, int n_cand, Candidate *cand, int *err,
+                        cudaStream_t st) {
+    if (cand && (n_cand < 1 || n_cand > kCand)) return cudaErrorInvalidValue;
     FusedParams p{};
     p.pd = pd; p.g = g; p.cam[0] = cam[0]; p.cam[1] = cam[1]; p.cam[2] = cam[2];
     p.rows = rows; p.n = n; p.stat = stat; p.err = err;
+    p.frame = frame; p.n_cand = n_cand; p.cand = cand;
     if (save) { p.save = 1; p.x = save->x; p.h1 = save->h1; p.h2 = save->h2; p.h3 = save->h3; }
     return launch_fused<kLse>(p, st);
 }
@@ -566,13 +873,30 @@ cudaError_t forward_sample(const ProposalDev &pd, const GBufView &g, const float
 }
 
 cudaError_t forward_grad(const ProposalDev &pd, const GBufView &g, const float cam[3], const int32_t *rows, int n,
-                         const float4 *stat, const int32_t *target, float inv_n, __nv_bfloat16 *dz, float *loss_sum,
+                         const float4 *stat, const int32_t *target, float inv_n, float *dh3, float *loss_sum,
                          int *err, cudaStream_t st) {
     FusedParams p{};
     p.pd = pd; p.g = g; p.cam[0] = cam[0]; p.cam[1] = cam[1]; p.cam[2] = cam[2];
-    p.rows = rows; p.n = n; p.stat = const_cast<float4 *>(stat); p.target = target; p.inv_n = inv_n; p.dz = dz;
+    p.rows = rows; p.n = n; p.stat = const_cast<float4 *>(stat); p.target = target; p.inv_n = inv_n; p.dh3 = dh3;
     p.loss_sum = loss_sum; p.err = err;
     return launch_fused<kGrad>(p, st);
+}
+
+cudaError_t dw4(const ProposalDev &pd, const __nv_bfloat16 *h3, const float4 *stat, const int32_t *target, int n,
+                float inv_n, float *gw4, float *gb4, int *err, cudaStream_t st) {
+    if (pd.c % kChunkN != 0 || n <= 0) return cudaErrorInvalidValue;
+    Dw4Params p{pd, h3, stat, target, n, 0, inv_n, gw4, gb4, err};
+    const int tiles = (n + kRows - 1) / kRows;
+    const int chunks = pd.c / kChunkN;
+    // enough CTAs for about four per SM; each keeps its tiles' sum in tensor memory
+    int slices = (4 * 152 + chunks - 1) / chunks;
+    if (slices > tiles) slices = tiles;
+    p.tiles_per_slice = (tiles + slices - 1) / slices;
+    slices = (tiles + p.tiles_per_slice - 1) / p.tiles_per_slice;
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_dw4, cudaFuncAttributeMaxDynamicSharedMemorySize, kDwSmem);
+    if (e != cudaSuccess) return e;
+    k_mlp_dw4<<<dim3(chunks, slices), 128, kDwSmem, st>>>(p);
+    return cudaGetLastError();
 }
 
 cudaError_t colsum_bf16(const __nv_bfloat16 *a, int n, int c, float *out, cudaStream_t st) {
@@ -601,9 +925,9 @@ cudaError_t adam(float *w, const float *g, float *m, float *v, size_t n, float l
 }
 
 cudaError_t refresh(const float *params, int c, const uint8_t *valid, __nv_bfloat16 *w123img, __nv_bfloat16 *w4t,
-                    __nv_bfloat16 *w123, __nv_bfloat16 *w4, float *b4e, cudaStream_t st) {
+                    __nv_bfloat16 *w4k, __nv_bfloat16 *w123, __nv_bfloat16 *w4, float *b4e, cudaStream_t st) {
     const size_t n = (size_t)kIn * kH + 2 * (size_t)kH * kH + (size_t)(kH + 1) * c;
-    k_refresh<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(params, c, valid, w123img, w4t, w123, w4, b4e);
+    k_refresh<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(params, c, valid, w123img, w4t, w4k, w123, w4, b4e);
     return cudaGetLastError();
 }
 

@@ -30,7 +30,7 @@ constexpr int kIn = 16;
 constexpr int kInUsed = 9;
 constexpr int kH = 64;
 constexpr int kCand = 32;  // candidate slots per pixel in the learned candidate buffer
-constexpr int kChunkN = 128;  // clusters per logit MMA chunk (clusters must be a multiple)
+constexpr int kChunkN = 64;   // clusters per logit MMA chunk (clusters must be a multiple)
 // PCG stream of the proposal's draws for pixel px in frame f:
 // pcg_seed(f * kSeedMul + kSeedAdd, px), distinct from the RIS stream.
 constexpr uint64_t kSeedMul = 0x9E3779B97F4A7C15ULL;
@@ -78,7 +78,8 @@ struct ProposalDev {
     const float *params;            // FP32 master (packed, Layout)
     const float *b4e;               // b4, or -inf for clusters without lights
     const __nv_bfloat16 *w123img;   // bf16 W1^T | W2^T | W3^T in the MMA operand layout
-    const __nv_bfloat16 *w4t;       // bf16 W4^T in 128-cluster chunk tiles, MMA operand layout
+    const __nv_bfloat16 *w4t;       // bf16 W4^T in chunk tiles (cluster x hidden), MMA operand layout
+    const __nv_bfloat16 *w4k;       // bf16 W4 in chunk tiles (hidden x cluster), MMA operand layout
     const __nv_bfloat16 *w123;      // bf16 W1 | W2 | W3 row-major (row = input)
     const __nv_bfloat16 *w4;        // bf16 W4, 64 x C row-major
     const uint8_t *cluster_valid;   // 1 if the cluster has lights
@@ -101,20 +102,25 @@ struct TrainBuffers {
 };
 
 size_t weight_image_bytes();
+// cand != nullptr (inference): also writes the uniform-branch candidates of frame `frame`
 cudaError_t forward_lse(const ProposalDev &pd, const GBufView &g, const float cam[3], const int32_t *rows, int n,
-                        float4 *stat, const TrainBuffers *save, int *err, cudaStream_t st);
+                        float4 *stat, const TrainBuffers *save, uint32_t frame, int n_cand, Candidate *cand, int *err,
+                        cudaStream_t st);
 cudaError_t forward_sample(const ProposalDev &pd, const GBufView &g, const float cam[3], int n, const float4 *stat,
                            uint32_t frame, int n_cand, Candidate *cand, int *err, cudaStream_t st);
 cudaError_t forward_grad(const ProposalDev &pd, const GBufView &g, const float cam[3], const int32_t *rows, int n,
-                         const float4 *stat, const int32_t *target, float inv_n, __nv_bfloat16 *dz, float *loss_sum,
+                         const float4 *stat, const int32_t *target, float inv_n, float *dh3, float *loss_sum,
                          int *err, cudaStream_t st);
+// Adds dW4 (64 x C) and db4 of the mean loss to gw4 / gb4.
+cudaError_t dw4(const ProposalDev &pd, const __nv_bfloat16 *h3, const float4 *stat, const int32_t *target, int n,
+                float inv_n, float *gw4, float *gb4, int *err, cudaStream_t st);
 cudaError_t colsum_bf16(const __nv_bfloat16 *a, int n, int c, float *out, cudaStream_t st);
 cudaError_t colsum_f32(const float *a, int n, int c, float *out, cudaStream_t st);
 cudaError_t backward_rows(const __nv_bfloat16 *w123, const TrainBuffers &t, const float *dh3, float *da1, float *da2,
                           float *da3, int n, cudaStream_t st);
 cudaError_t adam(float *w, const float *g, float *m, float *v, size_t n, float lr, int step, int c, cudaStream_t st);
 cudaError_t refresh(const float *params, int c, const uint8_t *valid, __nv_bfloat16 *w123img, __nv_bfloat16 *w4t,
-                    __nv_bfloat16 *w123, __nv_bfloat16 *w4, float *b4e, cudaStream_t st);
+                    __nv_bfloat16 *w4k, __nv_bfloat16 *w123, __nv_bfloat16 *w4, float *b4e, cudaStream_t st);
 cudaError_t targets(const rg_reservoir *res, const int32_t *rows, int n, const int32_t *cluster_of, int n_lights,
                     int32_t *target, int *count, cudaStream_t st);
 cudaError_t batch_rows(int32_t *rows, int n, uint32_t pixels, uint32_t offset, uint32_t stride, cudaStream_t st);

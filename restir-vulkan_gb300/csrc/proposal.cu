@@ -61,7 +61,7 @@ struct ProposalState {
     size_t n_params = 0;
     int step = 0;
     float *params = nullptr, *grad = nullptr, *adam_m = nullptr, *adam_v = nullptr;
-    __nv_bfloat16 *w123img = nullptr, *w4t = nullptr, *w123 = nullptr, *w4 = nullptr;
+    __nv_bfloat16 *w123img = nullptr, *w4t = nullptr, *w4k = nullptr, *w123 = nullptr, *w4 = nullptr;
     float *b4e = nullptr;
     uint8_t *valid = nullptr;
     int32_t *cluster_of = nullptr, *offset = nullptr;
@@ -79,7 +79,7 @@ struct ProposalState {
     int train_cap = 0;
     int32_t *rows = nullptr, *target = nullptr;
     float4 *tstat = nullptr;
-    __nv_bfloat16 *x = nullptr, *h1 = nullptr, *h2 = nullptr, *h3 = nullptr, *dz = nullptr;
+    __nv_bfloat16 *x = nullptr, *h1 = nullptr, *h2 = nullptr, *h3 = nullptr;
     float *dh3 = nullptr, *da1 = nullptr, *da2 = nullptr, *da3 = nullptr;
     float *loss = nullptr;
     int *count = nullptr;
@@ -96,6 +96,7 @@ struct ProposalState {
         d.b4e = b4e;
         d.w123img = w123img;
         d.w4t = w4t;
+        d.w4k = w4k;
         d.w123 = w123;
         d.w4 = w4;
         d.cluster_valid = valid;
@@ -104,11 +105,11 @@ struct ProposalState {
     }
     void release_train() {
         release(rows); release(target); release(tstat); release(x); release(h1); release(h2); release(h3);
-        release(dz); release(dh3); release(da1); release(da2); release(da3);
+        release(dh3); release(da1); release(da2); release(da3);
         train_cap = 0;
     }
     void release_all() {
-        release(params); release(grad); release(adam_m); release(adam_v); release(w123img); release(w4t);
+        release(params); release(grad); release(adam_m); release(adam_v); release(w123img); release(w4t); release(w4k);
         release(w123); release(w4); release(b4e); release(valid); release(cluster_of); release(offset); release(lcol);
         release(within); release(stat); release(cand); release(loss); release(count);
         release_train();
@@ -136,7 +137,7 @@ int get_state(rg_context *ctx, ProposalState **ps, const DevScene **scene = null
 }
 
 cudaError_t refresh_images(ProposalState &ps, cudaStream_t st) {
-    return mlp::refresh(ps.params, ps.c, ps.valid, ps.w123img, ps.w4t, ps.w123, ps.w4, ps.b4e, st);
+    return mlp::refresh(ps.params, ps.c, ps.valid, ps.w123img, ps.w4t, ps.w4k, ps.w123, ps.w4, ps.b4e, st);
 }
 
 int ensure_train(ProposalState &ps, int n) {
@@ -150,7 +151,6 @@ int ensure_train(ProposalState &ps, int n) {
     if (e == cudaSuccess) e = alloc(&ps.h1, nn * mlp::kH);
     if (e == cudaSuccess) e = alloc(&ps.h2, nn * mlp::kH);
     if (e == cudaSuccess) e = alloc(&ps.h3, nn * mlp::kH);
-    if (e == cudaSuccess) e = alloc(&ps.dz, nn * (size_t)ps.c);
     if (e == cudaSuccess) e = alloc(&ps.dh3, nn * mlp::kH);
     if (e == cudaSuccess) e = alloc(&ps.da1, nn * mlp::kH);
     if (e == cudaSuccess) e = alloc(&ps.da2, nn * mlp::kH);
@@ -181,21 +181,15 @@ int gradients(ProposalState &ps, const GBufView &g, const float cam[3], int n, c
     const mlp::ProposalDev pd = ps.dev();
     const mlp::Layout L(ps.c);
     const mlp::TrainBuffers tb{ps.x, ps.h1, ps.h2, ps.h3};
-    const int C = ps.c;
-    PR_CUDA(mlp::forward_lse(pd, g, cam, ps.rows, n, ps.tstat, &tb, ps.err, st), "proposal forward");
+    PR_CUDA(mlp::forward_lse(pd, g, cam, ps.rows, n, ps.tstat, &tb, 0, 0, nullptr, ps.err, st), "proposal forward");
     PR_CUDA(cudaMemsetAsync(ps.loss, 0, sizeof(float), st), "memset");
-    PR_CUDA(mlp::forward_grad(pd, g, cam, ps.rows, n, ps.tstat, ps.target, 1.0f / (float)n, ps.dz, ps.loss, ps.err, st),
-            "proposal logits gradient");
     PR_CUDA(cudaMemsetAsync(ps.grad, 0, ps.n_params * sizeof(float), st), "memset");
-    const int sp = splits_for(n);
-    // dW4 = h3^T dz, db4 = colsum(dz)
-    PR_CUDA(launch_gemm_tc(ps.h3, 0, 1, mlp::kH, mlp::kH, ps.dz, 0, 1, C, C, n, ps.grad + L.w4, C, 1, 1.0f, sp, ps.err,
-                           st),
+    // dh3 = dz W4^T and the loss (dz stays on chip), then dW4 and db4
+    PR_CUDA(mlp::forward_grad(pd, g, cam, ps.rows, n, ps.tstat, ps.target, 1.0f / (float)n, ps.dh3, ps.loss, ps.err, st),
+            "proposal logits gradient");
+    PR_CUDA(mlp::dw4(pd, ps.h3, ps.tstat, ps.target, n, 1.0f / (float)n, ps.grad + L.w4, ps.grad + L.b4, ps.err, st),
             "dW4");
-    PR_CUDA(mlp::colsum_bf16(ps.dz, n, C, ps.grad + L.b4, st), "db4");
-    // dh3 = dz W4^T
-    PR_CUDA(launch_gemm_tc(ps.dz, 0, C, 1, n, ps.w4, 0, C, 1, mlp::kH, C, ps.dh3, mlp::kH, 0, 1.0f, 1, ps.err, st),
-            "dh3");
+    const int sp = splits_for(n);
     PR_CUDA(mlp::backward_rows(ps.w123, tb, ps.dh3, ps.da1, ps.da2, ps.da3, n, st), "hidden backward");
     // dW3 = h2^T da3, dW2 = h1^T da2, dW1 = x^T da1, and the bias sums
     PR_CUDA(launch_gemm_tc(ps.h2, 0, 1, mlp::kH, mlp::kH, ps.da3, 1, 1, mlp::kH, mlp::kH, n, ps.grad + L.w3, mlp::kH,
@@ -325,6 +319,7 @@ int rg_proposal_create(rg_context *ctx, const rg_proposal_config *cfg, const rg_
     if (e == cudaSuccess) e = alloc(&ps->adam_v, L.total);
     if (e == cudaSuccess) e = alloc(&ps->w123img, n123);
     if (e == cudaSuccess) e = alloc(&ps->w4t, (size_t)mlp::kH * C);
+    if (e == cudaSuccess) e = alloc(&ps->w4k, (size_t)mlp::kH * C);
     if (e == cudaSuccess) e = alloc(&ps->w123, n123);
     if (e == cudaSuccess) e = alloc(&ps->w4, (size_t)mlp::kH * C);
     if (e == cudaSuccess) e = alloc(&ps->b4e, (size_t)C);
@@ -422,7 +417,9 @@ int rg_proposal_infer(rg_context *ctx, const rg_gbuffer *g, const rg_restir_unif
     cudaStream_t st = (cudaStream_t)stream;
     const GBufView gv = make_view(g);
     const mlp::ProposalDev pd = ps->dev();
-    PR_CUDA(mlp::forward_lse(pd, gv, u->camera_pos, nullptr, (int)np, ps->stat, nullptr, ps->err, st), "proposal lse");
+    PR_CUDA(mlp::forward_lse(pd, gv, u->camera_pos, nullptr, (int)np, ps->stat, nullptr, u->frame, (int)count,
+                             ps->cand, ps->err, st),
+            "proposal lse");
     PR_CUDA(mlp::forward_sample(pd, gv, u->camera_pos, (int)np, ps->stat, u->frame, (int)count, ps->cand, ps->err, st),
             "proposal sample");
     ps->cand_ready = true;
