@@ -280,6 +280,48 @@ int rg_spatial_unbiased_chain_noalloc(rg_context *ctx, const rg_gbuffer *gbuf, c
                                       rg_reservoir *out, const rg_restir_uniforms *uniforms, int32_t num_neighbors,
                                       int32_t num_passes, void *stream);
 
+/* ---- many views per launch ----
+ * No counterpart in the reference (one view per frame there).  A batch runs the
+ * frame driver's pass sequence (rg_render_frame) for many views of the
+ * uploaded scene with one launch per pass over all views: a persistent grid
+ * takes the tiles of every view from a work counter.  Each view's results
+ * equal those of rg_render_frame on that view.  The parameters of every view
+ * stay on the device, so a run is stream work only (no host copy, no
+ * allocation) and can be captured into a CUDA graph, one per parity. */
+typedef struct rg_view {
+    rg_gbuffer cur;               /* device G-buffer planes of the view */
+    rg_gbuffer prev;              /* previous frame's (may equal cur: a static camera) */
+    rg_reservoir *reservoirs[2];  /* parity p writes reservoirs[p] and reads reservoirs[1-p] as the
+                                     previous frame's */
+    rg_reservoir *tmp;            /* temporary for the spatial chain */
+    float *rgba_out;              /* shaded image, float4 per pixel */
+    rg_restir_uniforms uniforms;  /* frame = the first run's frame index; each run adds one */
+} rg_view;
+
+/* Launch shapes; none of them changes a result. */
+typedef struct rg_batch_tuning {
+    int32_t ris_pixels_per_thread; /* 1, 2 or 4: RIS tiles of 32 x (4 * this) pixels */
+    int32_t spatial_tile_width;    /* 8, 16 or 32: unbiased spatial tiles of w x (128 / w) pixels */
+    int32_t ctas_per_sm;           /* persistent CTAs per SM; 0: as many as fit */
+} rg_batch_tuning;
+
+typedef struct rg_batch rg_batch;
+/* params: unbiased, spatial_iterations, unbiased_neighbors and gamma as for
+ * rg_render_frame (its uniforms are not used); tuning may be null. */
+int rg_batch_create(rg_context *ctx, const rg_view *views, int32_t n_views, const rg_frame_params *params,
+                    const rg_batch_tuning *tuning, rg_batch **out);
+/* One frame of every view on `stream`. */
+int rg_batch_run(rg_batch *batch, int32_t parity, void *stream);
+/* The next run uses the views' starting frame indices again. */
+int rg_batch_reset_frames(rg_batch *batch, void *stream);
+int rg_batch_set_tuning(rg_batch *batch, const rg_batch_tuning *tuning);
+int rg_batch_get_tuning(rg_batch *batch, rg_batch_tuning *tuning);
+/* Times every tuning candidate over `repeats` runs (which advance the frame
+ * index and overwrite the views' reservoirs), keeps the fastest and returns it
+ * with its mean run time. */
+int rg_batch_autotune(rg_batch *batch, int32_t repeats, rg_batch_tuning *best, float *best_ms, void *stream);
+int rg_batch_destroy(rg_batch *batch);
+
 /* ---- learned light-cluster proposal ----
  * No counterpart in the reference: it replaces the source pdf of the initial
  * RIS candidates (restirOmni.glsl:73-83).  Per pixel an MLP (9 features:

@@ -11,6 +11,7 @@
 // Compiled with -fmad=false and IEEE div/sqrt: see rg_math.cuh.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "mlp.cuh"
 #include "rg_internal.h"
@@ -162,8 +163,7 @@ __device__ __forceinline__ void count_block_rays(const DevScene &s, int rays, co
 #define RG_SMEM_CARVEOUT -1
 #endif
 
-constexpr int kRisPpt = 4;
-constexpr int kRisTile = 128 * kRisPpt;
+constexpr int kRisPpt = 4;  // pixels per thread of the single-view launch (the batched one is tuned)
 
 struct InitialParams {
     DevScene s;
@@ -251,25 +251,28 @@ __device__ __forceinline__ Res ris(const DevScene &s, const Texel &t, float albe
 #ifndef RG_RIS_MIN_BLOCKS
 #define RG_RIS_MIN_BLOCKS 8
 #endif
-__global__ void __launch_bounds__(128, RG_RIS_MIN_BLOCKS) k_initial_temporal(const InitialParams p) {
+// The pass over one 32 x (4*PPT) pixel tile (tile coordinates bx, by).
+template <int PPT>
+__device__ __forceinline__ void initial_temporal_tile(const InitialParams &p, int bx, int by) {
+    constexpr int kTile = 128 * PPT;
     extern __shared__ __align__(16) unsigned char smem[];
     rgpool::Ray *pool = reinterpret_cast<rgpool::Ray *>(smem);
-    float4 *endp = reinterpret_cast<float4 *>(pool + kRisTile);  // sample position per pixel slot
-    uint8_t *shadow = reinterpret_cast<uint8_t *>(endp + kRisTile);
-    int *stack = reinterpret_cast<int *>(shadow + kRisTile);
+    float4 *endp = reinterpret_cast<float4 *>(pool + kTile);  // sample position per pixel slot
+    uint8_t *shadow = reinterpret_cast<uint8_t *>(endp + kTile);
+    int *stack = reinterpret_cast<int *>(shadow + kTile);
     __shared__ int s_count, s_next;
     const int tid = threadIdx.x + threadIdx.y * 32;
     if (tid == 0) { s_count = 0; s_next = 0; }
     __syncthreads();
     const DevScene &s = p.s;
     const int W = (int)p.u.screen_size[0], H = (int)p.u.screen_size[1];
-    const int x = blockIdx.x * 32 + threadIdx.x;
-    const int y0 = blockIdx.y * (4 * kRisPpt) + threadIdx.y;
+    const int x = bx * 32 + threadIdx.x;
+    const int y0 = by * (4 * PPT) + threadIdx.y;
     const f3 cam = mk(p.u.camera_pos[0], p.u.camera_pos[1], p.u.camera_pos[2]);
     const bool vis = (p.u.flags & RG_FLAG_VISIBILITY_REUSE) != 0;
-    uint64_t rng_state[kRisPpt];
+    uint64_t rng_state[PPT];
 #pragma unroll
-    for (int j = 0; j < kRisPpt; ++j) {
+    for (int j = 0; j < PPT; ++j) {
         const int y = y0 + 4 * j;
         const bool valid = x < W && y < H;
         bool want = false;
@@ -305,7 +308,7 @@ __global__ void __launch_bounds__(128, RG_RIS_MIN_BLOCKS) k_initial_temporal(con
         [&](int owner, bool hit) { shadow[owner] = hit ? 1 : 0; });
     __syncthreads();
 #pragma unroll
-    for (int j = 0; j < kRisPpt; ++j) {
+    for (int j = 0; j < PPT; ++j) {
         const int y = y0 + 4 * j;
         if (x >= W || y >= H) continue;
         const size_t i = (size_t)y * (size_t)W + (size_t)x;
@@ -354,6 +357,11 @@ __global__ void __launch_bounds__(128, RG_RIS_MIN_BLOCKS) k_initial_temporal(con
     count_block_rays(s, tid == 0 ? s_count : 0, ts);
 }
 
+template <int PPT>
+__global__ void __launch_bounds__(128, RG_RIS_MIN_BLOCKS) k_initial_temporal(const InitialParams p) {
+    initial_temporal_tile<PPT>(p, blockIdx.x, blockIdx.y);
+}
+
 // ---------------------------------------------------------------- biased spatial (spatialReuse.comp:30-86)
 struct SpatialParams {
     DevScene s;
@@ -366,9 +374,10 @@ struct SpatialParams {
     float cos_thr;
 };
 
-__global__ void __launch_bounds__(128) k_spatial_biased(const SpatialParams p) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+// One 32 x 4 pixel tile.
+__device__ __forceinline__ void spatial_biased_tile(const SpatialParams &p, int bx, int by) {
+    const int x = bx * 32 + threadIdx.x;
+    const int y = by * 4 + threadIdx.y;
     const int W = (int)p.u.screen_size[0], H = (int)p.u.screen_size[1];
     if (x >= W || y >= H) return;
     const size_t i = (size_t)y * (size_t)W + (size_t)x;
@@ -399,6 +408,10 @@ __global__ void __launch_bounds__(128) k_spatial_biased(const SpatialParams p) {
     store_res(p.out, i, r);
 }
 
+__global__ void __launch_bounds__(128) k_spatial_biased(const SpatialParams p) {
+    spatial_biased_tile(p, blockIdx.x, blockIdx.y);
+}
+
 // ---------------------------------------------------------------- unbiased spatial (unbiasedReuse.glsl:50-185)
 // One pixel per thread, 32x4 threads per block:
 //   1. neighbour streaming (:84-124); then, for every neighbour whose
@@ -424,7 +437,10 @@ __host__ __device__ inline size_t unbiased_smem_bytes(int K, int depth) {
 #ifndef RG_UNBIASED_MIN_BLOCKS
 #define RG_UNBIASED_MIN_BLOCKS 8
 #endif
-__global__ void __launch_bounds__(128, RG_UNBIASED_MIN_BLOCKS) k_spatial_unbiased(const SpatialParams p) {
+// One TW x (128/TW) pixel tile; the tile shape changes which pixels share a
+// ray pool, never a result.
+template <int TW>
+__device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, int bx, int by) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int K = p.num_neighbors;
     const int slots = K + 1;
@@ -440,8 +456,8 @@ __global__ void __launch_bounds__(128, RG_UNBIASED_MIN_BLOCKS) k_spatial_unbiase
     __syncthreads();
     const DevScene &s = p.s;
     const int W = (int)p.u.screen_size[0], H = (int)p.u.screen_size[1];
-    const int x = blockIdx.x * 32 + threadIdx.x;
-    const int y = blockIdx.y * 4 + threadIdx.y;
+    const int x = bx * TW + tid % TW;
+    const int y = by * (128 / TW) + tid / TW;
     const bool valid = x < W && y < H;
     const bool vis = (p.u.flags & RG_FLAG_VISIBILITY_REUSE) != 0;
     const size_t i = valid ? (size_t)y * (size_t)W + (size_t)x : 0;
@@ -523,6 +539,11 @@ __global__ void __launch_bounds__(128, RG_UNBIASED_MIN_BLOCKS) k_spatial_unbiase
     count_block_rays(s, tid == 0 ? s_count : 0, ts);
 }
 
+template <int TW>
+__global__ void __launch_bounds__(128, RG_UNBIASED_MIN_BLOCKS) k_spatial_unbiased(const SpatialParams p) {
+    spatial_unbiased_tile<TW>(p, blockIdx.x, blockIdx.y);
+}
+
 // ---------------------------------------------------------------- shading (lighting.frag:43-71,103)
 struct ShadeParams {
     DevScene s;
@@ -532,9 +553,10 @@ struct ShadeParams {
     rg_lighting_uniforms u;
 };
 
-__global__ void __launch_bounds__(128) k_shade(const ShadeParams p) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+// One 32 x 4 pixel tile.
+__device__ __forceinline__ void shade_tile(const ShadeParams &p, int bx, int by) {
+    const int x = bx * 32 + threadIdx.x;
+    const int y = by * 4 + threadIdx.y;
     const int W = (int)p.u.buffer_size[0], H = (int)p.u.buffer_size[1];
     if (x >= W || y >= H) return;
     const size_t i = (size_t)y * (size_t)W + (size_t)x;
@@ -565,6 +587,8 @@ __global__ void __launch_bounds__(128) k_shade(const ShadeParams p) {
     p.out[i] = make_float4(col.x, col.y, col.z, 1.0f);
 }
 
+__global__ void __launch_bounds__(128) k_shade(const ShadeParams p) { shade_tile(p, blockIdx.x, blockIdx.y); }
+
 // ---------------------------------------------------------------- visibility batch (testVisibility)
 // 128 threads take a chunk of 512 segments into the pool and trace it.
 constexpr int kVisChunk = 512;
@@ -592,6 +616,69 @@ __global__ void __launch_bounds__(128) k_visibility_batch(const DevScene s, cons
         [&](int owner) { const float4 e = endp[owner]; return mk(e.x, e.y, e.z); },
         [&](int owner, bool hit) { out[base + owner] = hit ? 1 : 0; });
     count_block_rays(s, tid == 0 ? count : 0, ts);
+}
+
+// ---------------------------------------------------------------- many views, one launch per pass
+// A persistent grid takes tiles from an atomic counter over the tiles of all
+// views (view_start: prefix sums of the views' tile counts).  Each tile runs
+// the same body as the single-view kernels with that view's parameters (read
+// from the parameter array in device memory), so a view's results equal those
+// of its own single-view launches.
+template <typename P, typename F>
+__device__ __forceinline__ void for_each_view_tile(const P *views, const ViewTiles &vt, F body) {
+    __shared__ int s_item;
+    const int tid = threadIdx.x + threadIdx.y * 32;
+    for (;;) {
+        __syncthreads();  // the previous tile is done with s_item and shared memory
+        if (tid == 0) s_item = (int)atomicAdd(vt.counter, 1u);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= vt.total) break;
+        int lo = 0, hi = vt.n_views - 1;  // the last view whose first tile is <= item
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(vt.view_start + mid) <= item) lo = mid;
+            else hi = mid - 1;
+        }
+        const int local = item - __ldg(vt.view_start + lo);
+        const int tx = __ldg(vt.tiles_x + lo);
+        body(views[lo], local % tx, local / tx);
+    }
+}
+
+template <int PPT>
+__global__ void __launch_bounds__(128, RG_RIS_MIN_BLOCKS) k_initial_temporal_views(const InitialParams *views,
+                                                                                     const ViewTiles vt) {
+    for_each_view_tile(views, vt, [](const InitialParams &p, int bx, int by) { initial_temporal_tile<PPT>(p, bx, by); });
+}
+template <int TW>
+__global__ void __launch_bounds__(128, RG_UNBIASED_MIN_BLOCKS) k_spatial_unbiased_views(const SpatialParams *views,
+                                                                                          const ViewTiles vt) {
+    for_each_view_tile(views, vt, [](const SpatialParams &p, int bx, int by) { spatial_unbiased_tile<TW>(p, bx, by); });
+}
+__global__ void __launch_bounds__(128) k_spatial_biased_views(const SpatialParams *views, const ViewTiles vt) {
+    for_each_view_tile(views, vt, [](const SpatialParams &p, int bx, int by) { spatial_biased_tile(p, bx, by); });
+}
+__global__ void __launch_bounds__(128) k_shade_views(const ShadeParams *views, const ViewTiles vt) {
+    for_each_view_tile(views, vt, [](const ShadeParams &p, int bx, int by) { shade_tile(p, bx, by); });
+}
+
+// frame index of every view for the next run: start + (number of runs so far)
+__global__ void k_advance_frames(InitialParams *ip, SpatialParams *sp, int n_views, int n_spatial,
+                                 const uint32_t *start_frame, uint32_t *runs) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t r = *runs;  // read by every thread before thread 0's increment becomes visible to a later launch
+    if (v < n_views) {
+        const uint32_t f = start_frame[v] + r;
+        ip[v].u.frame = f;
+        for (int k = 0; k < n_spatial; ++k) sp[(size_t)k * n_views + v].u.frame = f;
+    }
+}
+__global__ void k_count_run(uint32_t *runs) { *runs += 1u; }
+
+size_t ris_smem_bytes(int ppt, int depth) {
+    return (size_t)128 * ppt * (sizeof(rgpool::Ray) + sizeof(float4) + 1) +
+           128 * (size_t)(RG_STACK_LOCAL ? 0 : depth) * sizeof(int);
 }
 
 dim3 pixel_grid(int w, int h, dim3 block) {
@@ -626,10 +713,11 @@ cudaError_t launch_initial_temporal(const DevScene &s, const GBufView &cur, cons
     p.u = u;
     const dim3 block(32, 4);
     const dim3 grid((u.screen_size[0] + 31u) / 32u, (u.screen_size[1] + 4u * kRisPpt - 1u) / (4u * kRisPpt));
-    const size_t smem = kRisTile * (sizeof(rgpool::Ray) + sizeof(float4) + 1) + 128 * (size_t)(RG_STACK_LOCAL ? 0 : s.depth) * sizeof(int);
-    cudaError_t e = cudaFuncSetAttribute(k_initial_temporal, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = ris_smem_bytes(kRisPpt, s.depth);
+    cudaError_t e = cudaFuncSetAttribute(k_initial_temporal<kRisPpt>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
     if (e != cudaSuccess) return e;
-    k_initial_temporal<<<grid, block, smem, st>>>(p);
+    k_initial_temporal<kRisPpt><<<grid, block, smem, st>>>(p);
     return cudaGetLastError();
 }
 
@@ -663,13 +751,14 @@ cudaError_t launch_spatial_unbiased(const DevScene &s, const GBufView &g, const 
     p.cos_thr = 0.0f;
     const dim3 block(32, 4);
     const size_t smem = unbiased_smem_bytes(num_neighbors, RG_STACK_LOCAL ? 0 : s.depth);
-    cudaError_t e = cudaFuncSetAttribute(k_spatial_unbiased, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_spatial_unbiased<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     if (RG_SMEM_CARVEOUT >= 0) {
-        e = cudaFuncSetAttribute(k_spatial_unbiased, cudaFuncAttributePreferredSharedMemoryCarveout, RG_SMEM_CARVEOUT);
+        e = cudaFuncSetAttribute(k_spatial_unbiased<32>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 RG_SMEM_CARVEOUT);
         if (e != cudaSuccess) return e;
     }
-    k_spatial_unbiased<<<pixel_grid((int)u.screen_size[0], (int)u.screen_size[1], block), block, smem, st>>>(p);
+    k_spatial_unbiased<32><<<pixel_grid((int)u.screen_size[0], (int)u.screen_size[1], block), block, smem, st>>>(p);
     return cudaGetLastError();
 }
 
@@ -693,5 +782,130 @@ cudaError_t launch_visibility_batch(const DevScene &s, const float4 *p1, const f
     cudaError_t e = cudaFuncSetAttribute(k_visibility_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k_visibility_batch<<<(unsigned)((n + kVisChunk - 1) / kVisChunk), 128, smem, st>>>(s, p1, p2, out, n);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- views: parameter records and launches
+size_t view_params_size(int kind) {
+    return kind == 0 ? sizeof(InitialParams) : kind == 1 ? sizeof(SpatialParams) : sizeof(ShadeParams);
+}
+
+void make_initial_params(void *dst, const DevScene &s, const GBufView &cur, const GBufView *prev,
+                         const rg_reservoir *prev_res, rg_reservoir *out, const rg_restir_uniforms &u,
+                         const mlp::LearnedRis *learned) {
+    InitialParams p;
+    p.learned = learned ? *learned : mlp::LearnedRis{};
+    p.s = s;
+    p.cur = cur;
+    p.has_prev = prev != nullptr && prev_res != nullptr;
+    p.prev = prev ? *prev : cur;
+    p.prev_res = prev_res;
+    p.out = out;
+    p.u = u;
+    memcpy(dst, &p, sizeof(p));
+}
+
+void make_spatial_params(void *dst, const DevScene &s, const GBufView &g, const rg_reservoir *in, rg_reservoir *out,
+                         const rg_restir_uniforms &u, bool unbiased, int iter_or_pass, int num_neighbors) {
+    SpatialParams p;
+    p.s = s;
+    p.g = g;
+    p.in = in;
+    p.out = out;
+    p.u = u;
+    p.iter = iter_or_pass;
+    p.num_neighbors = unbiased ? num_neighbors : 0;
+    p.cos_thr = unbiased ? 0.0f : cos_cw(u.spatial_normal_threshold * kDeg2Rad);
+    memcpy(dst, &p, sizeof(p));
+}
+
+void make_shade_params(void *dst, const DevScene &s, const GBufView &g, const rg_reservoir *res,
+                       const rg_lighting_uniforms &u, float4 *out) {
+    ShadeParams p;
+    p.s = s;
+    p.g = g;
+    p.res = res;
+    p.out = out;
+    p.u = u;
+    memcpy(dst, &p, sizeof(p));
+}
+
+void view_tile_shape(int kind, int variant, int *tw, int *th) {
+    if (kind == 0) { *tw = 32; *th = 4 * variant; }       // variant: pixels per thread
+    else if (kind == 1) { *tw = variant; *th = 128 / variant; }  // variant: tile width
+    else { *tw = 32; *th = 4; }
+}
+
+namespace {
+template <typename P>
+cudaError_t views_grid(void (*kernel)(const P *, const ViewTiles), size_t smem, int total, int ctas_per_sm,
+                       int *grid) {
+    int dev = 0, sms = 0, occ = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 128, smem);
+    if (e != cudaSuccess) return e;
+    if (occ < 1) return cudaErrorInvalidConfiguration;
+    const int per_sm = ctas_per_sm > 0 && ctas_per_sm < occ ? ctas_per_sm : occ;
+    *grid = sms * per_sm < total ? sms * per_sm : total;
+    return cudaSuccess;
+}
+template <typename P>
+cudaError_t views_launch(void (*kernel)(const P *, const ViewTiles), const void *views, const ViewTiles &vt,
+                         size_t smem, int grid, cudaStream_t st) {
+    if (grid < 1) return cudaSuccess;
+    kernel<<<grid, dim3(32, 4), smem, st>>>(static_cast<const P *>(views), vt);
+    return cudaGetLastError();
+}
+// Calls f(kernel, smem) for the kernel of (kind, variant).
+template <typename F>
+cudaError_t with_views_kernel(int kind, int variant, bool unbiased, int num_neighbors, int depth, F f) {
+    if (kind == 0) {
+        const size_t smem = ris_smem_bytes(variant, depth);
+        switch (variant) {
+            case 1: return f(k_initial_temporal_views<1>, smem);
+            case 2: return f(k_initial_temporal_views<2>, smem);
+            case 4: return f(k_initial_temporal_views<4>, smem);
+            default: return cudaErrorInvalidValue;
+        }
+    }
+    if (kind == 1) {
+        if (!unbiased) return f(k_spatial_biased_views, (size_t)0);
+        if (num_neighbors < 0 || num_neighbors > kMaxNeighbors) return cudaErrorInvalidValue;
+        const size_t smem = unbiased_smem_bytes(num_neighbors, RG_STACK_LOCAL ? 0 : depth);
+        switch (variant) {
+            case 8: return f(k_spatial_unbiased_views<8>, smem);
+            case 16: return f(k_spatial_unbiased_views<16>, smem);
+            case 32: return f(k_spatial_unbiased_views<32>, smem);
+            default: return cudaErrorInvalidValue;
+        }
+    }
+    return f(k_shade_views, (size_t)0);
+}
+}  // namespace
+
+cudaError_t views_pass_grid(int kind, int variant, bool unbiased, int num_neighbors, int depth, int total,
+                            int ctas_per_sm, int *grid) {
+    return with_views_kernel(kind, variant, unbiased, num_neighbors, depth, [&](auto kernel, size_t smem) {
+        return views_grid(kernel, smem, total, ctas_per_sm, grid);
+    });
+}
+
+cudaError_t launch_views_pass(int kind, int variant, bool unbiased, int num_neighbors, int depth, const void *params,
+                              const ViewTiles &vt, int grid, cudaStream_t st) {
+    return with_views_kernel(kind, variant, unbiased, num_neighbors, depth, [&](auto kernel, size_t smem) {
+        return views_launch(kernel, params, vt, smem, grid, st);
+    });
+}
+
+cudaError_t launch_advance_frames(void *initial_params, void *spatial_params, int n_views, int n_spatial,
+                                  const uint32_t *start_frame, uint32_t *runs, cudaStream_t st) {
+    k_advance_frames<<<(n_views + 127) / 128, 128, 0, st>>>(static_cast<InitialParams *>(initial_params),
+                                                             static_cast<SpatialParams *>(spatial_params), n_views,
+                                                             n_spatial, start_frame, runs);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_count_run<<<1, 1, 0, st>>>(runs);
     return cudaGetLastError();
 }

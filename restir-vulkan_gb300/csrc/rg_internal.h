@@ -84,6 +84,37 @@ cudaError_t launch_gemm_tc(const void *a, int a_fp32, int64_t a_rs, int64_t a_ks
 // host helpers (host_bvh.cpp, host_alias.cpp, host_gbuffer.cpp)
 void srgb_lut_host(float *out256);
 
+// ---- many views per launch (kernels.cu); kind 0: RIS + visibility + temporal,
+// 1: spatial pass, 2: shading.  A parameter record is the single-view kernel's
+// parameter block for one view.
+struct ViewTiles {
+    const int32_t *view_start;  // first tile of each view in the launch's tile order
+    const int32_t *tiles_x;     // tiles per row of each view
+    int32_t n_views;
+    int32_t total;              // tiles of all views
+    unsigned *counter;          // zero before the launch
+};
+size_t view_params_size(int kind);
+void make_initial_params(void *dst, const DevScene &s, const GBufView &cur, const GBufView *prev,
+                         const rg_reservoir *prev_res, rg_reservoir *out, const rg_restir_uniforms &u,
+                         const mlp::LearnedRis *learned);
+void make_spatial_params(void *dst, const DevScene &s, const GBufView &g, const rg_reservoir *in, rg_reservoir *out,
+                         const rg_restir_uniforms &u, bool unbiased, int iter_or_pass, int num_neighbors);
+void make_shade_params(void *dst, const DevScene &s, const GBufView &g, const rg_reservoir *res,
+                       const rg_lighting_uniforms &u, float4 *out);
+// tile of pass `kind` for tuning variant `variant` (RIS: pixels per thread 1/2/4;
+// unbiased spatial: tile width 8/16/32; others: 32 x 4)
+void view_tile_shape(int kind, int variant, int *tw, int *th);
+// Persistent grid of a pass (sets the kernel's shared-memory attribute; call
+// before any stream capture), then the launch itself (stream work only).
+cudaError_t views_pass_grid(int kind, int variant, bool unbiased, int num_neighbors, int depth, int total,
+                            int ctas_per_sm, int *grid);
+cudaError_t launch_views_pass(int kind, int variant, bool unbiased, int num_neighbors, int depth, const void *params,
+                              const ViewTiles &vt, int grid, cudaStream_t st);
+// Sets every view's frame index to start_frame[v] + *runs, then adds one to *runs.
+cudaError_t launch_advance_frames(void *initial_params, void *spatial_params, int n_views, int n_spatial,
+                                  const uint32_t *start_frame, uint32_t *runs, cudaStream_t st);
+
 // capi.cu: error reporting and context access for other translation units.
 int rg_internal_fail(int code, const char *msg);
 int rg_internal_prepare(rg_context *ctx, const DevScene **scene, int *device);

@@ -85,6 +85,15 @@ class Stats(C.Structure):
                 ("triangle_tests", C.c_uint64), ("mma_timeouts", C.c_uint64)]
 
 
+class View(C.Structure):
+    _fields_ = [("cur", GBuffer), ("prev", GBuffer), ("reservoirs", C.c_void_p * 2), ("tmp", C.c_void_p),
+                ("rgba_out", C.c_void_p), ("uniforms", RestirUniforms)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("ris_pixels_per_thread", C.c_int32), ("spatial_tile_width", C.c_int32), ("ctas_per_sm", C.c_int32)]
+
+
 class ProposalConfig(C.Structure):
     _fields_ = [("clusters", C.c_int32), ("mix", C.c_float), ("learning_rate", C.c_float), ("batch", C.c_int32),
                 ("box_min", C.c_float * 3), ("box_max", C.c_float * 3), ("seed", C.c_uint64)]
@@ -149,6 +158,15 @@ _SIGNATURES = {
                                C.c_int32, C.c_float, C.c_int32, C.c_void_p]),
     "rg_spatial_unbiased_chain_noalloc": (C.c_int, [C.c_void_p, C.POINTER(GBuffer), C.c_void_p, C.c_void_p,
                                                     C.POINTER(RestirUniforms), C.c_int32, C.c_int32, C.c_void_p]),
+    "rg_batch_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(FrameParams),
+                                  C.POINTER(BatchTuning), C.POINTER(C.c_void_p)]),
+    "rg_batch_run": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "rg_batch_reset_frames": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rg_batch_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(BatchTuning)]),
+    "rg_batch_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(BatchTuning)]),
+    "rg_batch_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(BatchTuning), C.POINTER(C.c_float),
+                                    C.c_void_p]),
+    "rg_batch_destroy": (C.c_int, [C.c_void_p]),
     "rg_cluster_lights": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_void_p,
                                     C.c_void_p]),
     "rg_proposal_param_count": (C.c_int64, [C.c_int32]),

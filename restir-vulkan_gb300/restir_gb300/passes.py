@@ -247,6 +247,61 @@ class Context:
         return loss.value, cnt.value
 
 
+class Batch:
+    """Many views through the passes with one launch per pass (rg_batch_*).
+
+    views: list of dicts with keys cur, prev (DeviceGBuffer), res0, res1, tmp
+    (reservoir tensors), image (float4 tensor) and uniforms (RestirUniforms);
+    params: FrameParams (unbiased, spatial_iterations, unbiased_neighbors, gamma)."""
+
+    def __init__(self, ctx: "Context", views: list, params, tuning: _lib.BatchTuning | None = None):
+        arr = (_lib.View * len(views))()
+        self._keep = views
+        for i, v in enumerate(views):
+            arr[i].cur = v["cur"].struct()
+            arr[i].prev = v["prev"].struct()
+            arr[i].reservoirs[0] = _lib.ptr(v["res0"])
+            arr[i].reservoirs[1] = _lib.ptr(v["res1"])
+            arr[i].tmp = _lib.ptr(v["tmp"])
+            arr[i].rgba_out = _lib.ptr(v["image"])
+            arr[i].uniforms = v["uniforms"]
+        self._h = C.c_void_p()
+        check(lib().rg_batch_create(ctx._h, arr, len(views), C.byref(params),
+                                    C.byref(tuning) if tuning is not None else None, C.byref(self._h)))
+
+    def run(self, parity: int, stream=None):
+        check(lib().rg_batch_run(self._h, parity, _stream_handle(stream)))
+
+    def reset_frames(self, stream=None):
+        check(lib().rg_batch_reset_frames(self._h, _stream_handle(stream)))
+
+    def set_tuning(self, ris_pixels_per_thread: int, spatial_tile_width: int, ctas_per_sm: int = 0):
+        t = _lib.BatchTuning(ris_pixels_per_thread, spatial_tile_width, ctas_per_sm)
+        check(lib().rg_batch_set_tuning(self._h, C.byref(t)))
+
+    def tuning(self) -> _lib.BatchTuning:
+        t = _lib.BatchTuning()
+        check(lib().rg_batch_get_tuning(self._h, C.byref(t)))
+        return t
+
+    def autotune(self, repeats: int = 3, stream=None):
+        t = _lib.BatchTuning()
+        ms = C.c_float()
+        check(lib().rg_batch_autotune(self._h, repeats, C.byref(t), C.byref(ms), _stream_handle(stream)))
+        return t, ms.value
+
+    def close(self):
+        if self._h:
+            lib().rg_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def cluster_lights(point_lights: np.ndarray, k: int, iterations: int = 10, seed: int = 1):
     """Seeded k-means of the point lights (host): (cluster_of int32 [n], centers float32 [k x 3])."""
     n = len(point_lights)

@@ -24,7 +24,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
-from dataclasses import dataclass, field
+from dataclasses import dataclass, field, replace
 
 import numpy as np
 
@@ -109,6 +109,10 @@ class Scene:
         lu.debug_mode = 0
         lu.gamma = gamma
         return lu
+
+    def view(self, camera, width: int, height: int, name: str | None = None) -> "Scene":
+        """The same scene seen by another camera at another resolution (arrays shared)."""
+        return replace(self, name=name or self.name, width=width, height=height, cameras=[camera])
 
     def frame_params(self, frame_index: int) -> _lib.FrameParams:
         fp = _lib.FrameParams()
@@ -330,6 +334,26 @@ def config3(seed: int = 3, width: int = 1920, height: int = 1080, grid=(64, 32, 
     cams = camera_path(rng, frames, width / height)
     return _finish("config3", tri_xyz, mats, lights, width, height, cams, uniform_pdf=False, candidates=32,
                    unbiased=True, spatial_passes=3, neighbors=5, radius=30.0, temporal=True, temporal_mult=20)
+
+
+def config5(seed: int = 5, n_views: int = 64, n_tris: int = 100_000, n_lights: int = 65_536,
+            min_size=(320, 240), max_size=(1920, 1080)):
+    """Batched multi-view workload: config 2's scene seen by n_views seeded
+    cameras whose widths and heights are each log-uniform between min_size and
+    max_size.  Returns (scene, views), every view a Scene sharing its arrays."""
+    base = config2(width=min_size[0], height=min_size[1], n_tris=n_tris, n_lights=n_lights, frames=1)
+    rng = np.random.default_rng(seed)
+    views = []
+    for v in range(n_views):
+        w = int(round(math.exp(rng.uniform(math.log(min_size[0]), math.log(max_size[0])))))
+        h = int(round(math.exp(rng.uniform(math.log(min_size[1]), math.log(max_size[1])))))
+        pos = rng.uniform(0.15, 0.85, 3)
+        target = rng.uniform(0.15, 0.85, 3)
+        while np.linalg.norm(target - pos) < 0.3:
+            target = rng.uniform(0.15, 0.85, 3)
+        cam = CameraModel(position=pos.astype(np.float32), look_at=target.astype(np.float32), aspect=w / h)
+        views.append(base.view(cam, w, h, name=f"config5_view{v}"))
+    return base, views
 
 
 def make_tri_lights(tri_xyz: np.ndarray, emission_rgb: np.ndarray) -> np.ndarray:
