@@ -17,6 +17,11 @@ Reported (one JSON line on rank 0):
             event-timed duration, against the measured HBM copy bandwidth;
   cpu_baseline  the CPU oracle on a crop of the same frame (all host threads),
             scaled per pixel.
+  learned_proposal  config 4's workload: inference, learned vs plain RIS, one
+            Adam step, and the tensor-core rate of the inference;
+  batched_views     config 5's 64 views through one persistent launch per pass
+            (autotuned launch shapes, CUDA-graph replay) against the same views
+            one by one (per-view p50/p99).
 --impl reference times the CPU implementation of the path (the oracle port
 of the reference's shaders) on the same workload instead.
 """
@@ -391,6 +396,16 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
                        "d2h_bytes_per_step": n * 16, "ms_per_step": e_ms / args.steps,
                        "api": "rg_render_frame_host (pinned host planes)"}
 
+    # the learned proposal and the batched views on this GPU (rank 0)
+    if not args.no_extras:
+        for key, fn in (("learned_proposal", learned_section), ("batched_views", batched_section)):
+            try:
+                line[key] = fn(dev)
+            except Exception as ex:  # reported, never hides the headline number
+                line[key] = {"error": f"{type(ex).__name__}: {ex}"}
+            import torch
+            torch.cuda.empty_cache()
+
     # CPU baseline on the host cores (rank 0, N = 1 only)
     if world == 1 and not args.no_cpu:
         host_g = [dgs[0].to_host(), dgs[1].to_host()]
@@ -400,6 +415,183 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
                                 "full_frame_seconds_estimate": round(cb["frame_seconds_estimate"], 2)}
     ctx.close()
     return line
+
+
+# ------------------------------------------------------------------ learned proposal (config 4 workload)
+def learned_section(dev: int, iters: int = 10) -> dict:
+    """Live timings of the learned light-cluster proposal on config 4's
+    workload (config 2's scene at 1080p, 65,536 lights in 4096 k-means
+    clusters): inference over every pixel, RIS with the learned candidates
+    against the plain alias-table RIS, one Adam step on 65,536 pixels; and the
+    tensor-core rate of the inference's products."""
+    import torch
+
+    from restir_gb300 import _lib, scenes
+    from restir_gb300.passes import Context, DeviceGBuffer, cluster_lights, reservoirs
+    s = scenes.config2(frames=1)
+    clusters = 4096
+    t0 = time.perf_counter()
+    co, _ = cluster_lights(s.point_lights, clusters, iterations=8, seed=4)
+    kmeans_s = time.perf_counter() - t0
+    ctx = Context(dev)
+    ctx.upload_scene(s)
+    g = DeviceGBuffer(s.width, s.height)
+    ctx.trace_gbuffer(s.cameras[0], g)
+    ctx.create_proposal(co, clusters, mix=0.9, batch=65_536, learning_rate=1e-2, seed=1)
+    n = s.width * s.height
+    res = reservoirs(n)
+    st = torch.cuda.current_stream()
+    base = s.uniforms(0)
+    base.flags = _lib.RG_FLAG_VISIBILITY_REUSE | _lib.RG_FLAG_FINAL_RIS_WEIGHT
+    learned = _lib.RestirUniforms.from_buffer_copy(bytes(base))
+    learned.flags |= _lib.RG_FLAG_LEARNED_PROPOSAL
+
+    def timed(fn):
+        for k in range(3):
+            fn(k)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for k in range(iters):
+            fn(3 + k)
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / iters
+
+    def infer(k):
+        learned.frame = 1 + k
+        ctx.proposal_infer(g, learned, st)
+
+    def ris_learned(k):
+        ctx.initial_temporal(g, None, None, res, learned, st)
+
+    def ris_plain(k):
+        ctx.initial_temporal(g, None, None, res, base, st)
+
+    def train(k):
+        learned.frame = 1 + k
+        ctx.proposal_train(g, learned, res.data_ptr(), st)
+
+    infer_ms = timed(infer)
+    learned.frame = 1
+    ctx.proposal_infer(g, learned, st)
+    ris_l = timed(ris_learned)
+    ris_p = timed(ris_plain)
+    train_ms = timed(train)
+    loss, rows = ctx.proposal_last_loss()
+    stats = ctx.stats()
+    ctx.close()
+    # products of one inference: two passes over every pixel, each the three
+    # hidden layers (16x64, 64x64, 64x64) and the 64 x C logit layer
+    flops = 2 * n * 2 * (16 * 64 + 2 * 64 * 64 + 64 * clusters)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak_tf = float(peaks.get("bf16_tflops", 1900.0))
+    tf = flops / (infer_ms / 1000.0) / 1e12
+    return {"workload": f"config 4: {s.width}x{s.height}, {len(s.point_lights):,} point lights in {clusters} k-means "
+                        "clusters, MLP 9-64-64-64-4096 (bf16, FP32 accumulation in tensor memory), mix 0.9",
+            "inference_ms": round(infer_ms, 3), "ris_learned_ms": round(ris_l, 3), "ris_plain_ms": round(ris_p, 3),
+            "train_step_ms": round(train_ms, 3), "train_batch": 65_536, "last_loss": round(loss, 4),
+            "inference_tensor": {"tflops": round(tf, 2), "peak_tflops": peak_tf,
+                                 "peak_source": "measured bf16 burst" if "bf16_tflops" in peaks else "fallback",
+                                 "frac": round(tf / peak_tf, 4), "flops_per_inference": flops},
+            "kmeans_host_seconds": round(kmeans_s, 2), "mma_timeouts": int(stats.mma_timeouts)}
+
+
+# ------------------------------------------------------------------ batched views (config 5 workload)
+def batched_section(dev: int, steps: int = 5, n_views: int = 64) -> dict:
+    """Config 5: n_views views of config 2's scene, sizes log-uniform between
+    320x240 and 1920x1080, seeded poses; config 2's pass sequence (RIS +
+    visibility + temporal, 2 unbiased spatial passes k=5, shading) for every
+    view with one persistent launch per pass, launch shapes from the
+    autotuner, replayed from CUDA graphs.  Per-view frame times of the same
+    views run one by one give the p50/p99."""
+    import torch
+
+    from restir_gb300 import _lib, scenes
+    from restir_gb300.passes import Batch, Context, DeviceGBuffer, reservoirs
+    base, views = scenes.config5(n_views=n_views)
+    ctx = Context(dev)
+    ctx.upload_scene(base)
+    vws = []
+    for v in views:
+        gb = DeviceGBuffer(v.width, v.height)
+        ctx.trace_gbuffer(v.cameras[0], gb)
+        nv = v.width * v.height
+        u = v.uniforms(0)
+        u.flags |= _lib.RG_FLAG_TEMPORAL_REUSE
+        vws.append({"scene": v, "cur": gb, "prev": gb, "res0": reservoirs(nv), "res1": reservoirs(nv),
+                    "tmp": reservoirs(nv), "uniforms": u,
+                    "image": torch.zeros((v.height, v.width, 4), dtype=torch.float32, device="cuda")})
+    fp = base.frame_params(0)
+    pixels = sum(v.width * v.height for v in views)
+    samples = sum(v.width * v.height * (v.candidates + 1 + v.spatial_passes * v.neighbors) for v in views)
+    b = Batch(ctx, vws, fp)
+    t0 = time.perf_counter()
+    tuning, tuned_ms = b.autotune(repeats=1)
+    tune_s = time.perf_counter() - t0
+    b.reset_frames()
+    for vw in vws:
+        for k in ("res0", "res1", "tmp"):
+            vw[k].zero_()
+    torch.cuda.synchronize()
+    stream = torch.cuda.Stream()
+    graphs = []
+    for parity in (0, 1):
+        gr = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(gr, stream=stream):
+            b.run(parity, stream)
+        graphs.append(gr)
+    for k in range(3):
+        graphs[k & 1].replay()
+    torch.cuda.synchronize()
+    cur = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(cur)
+    for k in range(steps):
+        graphs[(3 + k) & 1].replay()
+    e1.record(cur)
+    torch.cuda.synchronize()
+    batched_ms = e0.elapsed_time(e1) / steps
+    # the same views one by one (single-view launches), per-view frame times
+    per_view = []
+    for vw in vws:
+        v = vw["scene"]
+        u = vw["uniforms"]
+        lu = v.lighting_uniforms(0)
+        times = []
+        for k in range(4):
+            uu = _lib.RestirUniforms.from_buffer_copy(bytes(u))
+            uu.frame = u.frame + 100 + k
+            a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(cur)
+            ctx.initial_temporal(vw["cur"], vw["prev"], vw["res1"], vw["res0"], uu, cur)
+            ctx.spatial_unbiased(vw["cur"], vw["res0"], vw["tmp"], uu, v.neighbors, 0, cur)
+            ctx.spatial_unbiased(vw["cur"], vw["tmp"], vw["res0"], uu, v.neighbors, 1, cur)
+            ctx.shade(vw["cur"], vw["res0"], lu, vw["image"], cur)
+            z.record(cur)
+            torch.cuda.synchronize()
+            if k:
+                times.append(a.elapsed_time(z))
+        per_view.append(statistics.median(times))
+    stats = ctx.stats()
+    b.close()
+    ctx.close()
+    pv = np.array(per_view)
+    return {"workload": f"config 5: {n_views} views of config 2's scene ({len(base.triangles):,} triangles, "
+                        f"{len(base.point_lights):,} point lights), sizes log-uniform 320x240..1920x1080, "
+                        f"{pixels:,} pixels; RIS + visibility + temporal, 2 unbiased spatial passes k=5, shading",
+            "batched": {"ms_per_frame": round(batched_ms, 3), "samples_per_s": samples / (batched_ms / 1000.0),
+                        "launches_per_frame": 2 + 2 + 1 + 2, "cuda_graph": True,
+                        "tuning": {"ris_pixels_per_thread": tuning.ris_pixels_per_thread,
+                                   "spatial_tile_width": tuning.spatial_tile_width,
+                                   "ctas_per_sm": tuning.ctas_per_sm},
+                        "autotune_seconds": round(tune_s, 2),
+                        "note": "all views advance together: each view's frame completes within ms_per_frame"},
+            "one_by_one": {"ms_per_frame_all_views": round(float(pv.sum()), 3),
+                           "samples_per_s": samples / (pv.sum() / 1000.0),
+                           "per_view_ms_p50": round(float(np.percentile(pv, 50)), 3),
+                           "per_view_ms_p99": round(float(np.percentile(pv, 99)), 3)},
+            "samples_per_frame": samples, "traversal_errors": int(stats.traversal_errors)}
 
 
 # ------------------------------------------------------------------ reference arm
@@ -442,6 +634,7 @@ def main(argv=None):
     ap.add_argument("--cpu-crop", type=int, default=0, help="0: the whole frame")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the learned-proposal and batched-view sections")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         log("warmup raised to 3 (timing rule)")
