@@ -418,7 +418,7 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
 
 
 # ------------------------------------------------------------------ learned proposal (config 4 workload)
-def learned_section(dev: int, iters: int = 10) -> dict:
+def learned_section(dev: int, iters: int = 10, width: int = 1920, height: int = 1080) -> dict:
     """Live timings of the learned light-cluster proposal on config 4's
     workload (config 2's scene at 1080p, 65,536 lights in 4096 k-means
     clusters): inference over every pixel, RIS with the learned candidates
@@ -428,7 +428,7 @@ def learned_section(dev: int, iters: int = 10) -> dict:
 
     from restir_gb300 import _lib, scenes
     from restir_gb300.passes import Context, DeviceGBuffer, cluster_lights, reservoirs
-    s = scenes.config2(frames=1)
+    s = scenes.config2(width=width, height=height, frames=1)
     clusters = 4096
     t0 = time.perf_counter()
     co, _ = cluster_lights(s.point_lights, clusters, iterations=8, seed=4)
@@ -635,6 +635,8 @@ def main(argv=None):
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the learned-proposal and batched-view sections")
+    ap.add_argument("--section", choices=["all", "learned", "batched"], default="all",
+                    help="learned / batched: run only that section (at --width x --height for learned) and print it")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         log("warmup raised to 3 (timing rule)")
@@ -642,6 +644,14 @@ def main(argv=None):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     dist = None
+    if args.section != "all":
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        if rank == 0:
+            fn = learned_section if args.section == "learned" else batched_section
+            kw = {"width": args.width or 1920, "height": args.height or 1080} if args.section == "learned" else {}
+            print(json.dumps({"section": args.section, **fn(torch.cuda.current_device(), **kw)}), flush=True)
+        return
     if args.impl == "reference":
         line = reference_arm(args, rank, world)
     else:
