@@ -203,6 +203,15 @@ int rg_get_stats(rg_context *ctx, rg_stats *out, int32_t reset);
 /* AabbTree::build on a flat list of n_tris triangles (9 floats each).  Writes
  * n_tris-1 nodes and n_tris triangles; returns the node count or an error. */
 int rg_build_bvh(const float *tri_xyz, int32_t n_tris, rg_aabb_tree_node *out_nodes, rg_triangle *out_tris);
+/* The same tree built on the GPU from device buffers: tri_xyz (9 floats per
+ * triangle) in, n_tris-1 nodes and n_tris triangles out (device), with
+ * contents byte-identical to rg_build_bvh's.  Synchronous on `stream`;
+ * returns the node count; *ref_undefined (host, may be null) is set when a
+ * range took a path the reference leaves undefined (see rg_build_bvh).
+ * At most 4,194,304 triangles; coordinates must be finite.  No counterpart
+ * in the reference, which builds on the host (aabbTreeBuilder.cpp:52-214). */
+int rg_build_bvh_device(rg_context *ctx, const float *tri_xyz, int32_t n_tris, rg_aabb_tree_node *nodes,
+                        rg_triangle *triangles, int32_t *ref_undefined, void *stream);
 /* Depth of the tree (root = 1). */
 int rg_tree_depth(const rg_aabb_tree_node *nodes, int32_t n_nodes);
 /* createAliasTable: point lights if n_point > 0, else triangle lights. */

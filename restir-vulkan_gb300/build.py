@@ -19,7 +19,7 @@ CSRC = HERE / "csrc"
 OUT = HERE / "librestir_gb300.so"
 BUILD = HERE / "_build"
 
-SOURCES = ["kernels.cu", "gbuffer_kernel.cu", "capi.cu", "noalloc.cu", "gemm_tc.cu", "mlp.cu", "proposal.cu", "batch.cu", "host.cpp"]
+SOURCES = ["kernels.cu", "gbuffer_kernel.cu", "capi.cu", "noalloc.cu", "gemm_tc.cu", "mlp.cu", "proposal.cu", "batch.cu", "gpu_bvh.cu", "host.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",

@@ -559,6 +559,13 @@ ProposalState **rg_internal_proposal(rg_context *ctx) {
     return &ctx->proposal;
 }
 
+int rg_internal_device(rg_context *ctx, int *device) {
+    const int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    *device = ctx->device;
+    return RG_OK;
+}
+
 int rg_internal_prepare(rg_context *ctx, const DevScene **scene, int *device) {
     const int rc = check_ctx(ctx, true);
     if (rc) return rc;

@@ -118,6 +118,12 @@ cudaError_t launch_advance_frames(void *initial_params, void *spatial_params, in
 // capi.cu: error reporting and context access for other translation units.
 int rg_internal_fail(int code, const char *msg);
 int rg_internal_prepare(rg_context *ctx, const DevScene **scene, int *device);
+// A valid context (no scene needed); makes its device current.
+int rg_internal_device(rg_context *ctx, int *device);
+
+// gpu_bvh.cu: the reference tree built on the device (node count, or < 0).
+int gpu_build_bvh(const float *xyz, int n, rg_aabb_tree_node *nodes, rg_triangle *tris, int *undefined,
+                  cudaStream_t st);
 
 // proposal.cu: the learned proposal attached to a context.
 struct ProposalState;

@@ -158,6 +158,8 @@ _SIGNATURES = {
                                C.c_int32, C.c_float, C.c_int32, C.c_void_p]),
     "rg_spatial_unbiased_chain_noalloc": (C.c_int, [C.c_void_p, C.POINTER(GBuffer), C.c_void_p, C.c_void_p,
                                                     C.POINTER(RestirUniforms), C.c_int32, C.c_int32, C.c_void_p]),
+    "rg_build_bvh_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
+                                      C.POINTER(C.c_int32), C.c_void_p]),
     "rg_batch_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(FrameParams),
                                   C.POINTER(BatchTuning), C.POINTER(C.c_void_p)]),
     "rg_batch_run": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
