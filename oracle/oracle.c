@@ -479,35 +479,81 @@ void or_build_alias_table(const or_point_light *pl, int32_t n_pl, const or_tri_l
 }
 
 /* ------------------------------------------------------------------ reservoirs (reservoir.glsl:6-76) */
-static inline void update_reservoir(or_reservoir *r, float weight, v3 pos, or_f4 nrm, float lum, int32_t idx,
-                                    float p_hat, float w, pcg_t *rng) { /* :6-26 */
-    r->sum_weights += weight;
-    float replace = weight / r->sum_weights;
+static inline void update_reservoir_at(or_reservoir *r, int i, float weight, v3 pos, or_f4 nrm, float lum,
+                                       int32_t idx, float p_hat, float w, float sum_phat, pcg_t *rng) { /* :6-26 */
+    or_sample *s = &r->s[i];
+    s->sum_weights += weight;
+    float replace = weight / s->sum_weights;
     if (rand_float(rng) < replace) {
-        r->pos_lum.x = pos.x; r->pos_lum.y = pos.y; r->pos_lum.z = pos.z; r->pos_lum.w = lum;
-        r->normal = nrm;
-        r->light_index = idx;
-        r->p_hat = p_hat;
-        r->w = w;
+        s->pos_lum.x = pos.x; s->pos_lum.y = pos.y; s->pos_lum.z = pos.z; s->pos_lum.w = lum;
+        s->normal = nrm;
+        s->light_index = idx;
+        s->p_hat = p_hat;
+        s->w = w;
+#if OR_MIS
+        s->sum_phat += sum_phat;
+#else
+        (void)sum_phat;
+#endif
     }
 }
 static inline void add_sample(or_reservoir *r, v3 pos, or_f4 nrm, float lum, int32_t idx, float p_hat,
                               float sample_p, pcg_t *rng) { /* :28-42 */
     float weight = p_hat / sample_p;
     r->m += 1;
-    float w = (r->sum_weights + weight) / ((float)r->m * p_hat);
-    update_reservoir(r, weight, pos, nrm, lum, idx, p_hat, w, rng);
+    for (int i = 0; i < OR_RS; ++i) {
+        float w = (r->s[i].sum_weights + weight) / ((float)r->m * p_hat);
+        update_reservoir_at(r, i, weight, pos, nrm, lum, idx, p_hat, w, p_hat, rng);
+    }
 }
-static inline void combine_reservoirs(or_reservoir *self, const or_reservoir *other, float p_hat, pcg_t *rng) { /* :44-64 */
+/* :44-64.  With UNBIASED_MIS the reference passes other's sumPHat where
+ * updateReservoirAt takes w and other's w where it takes sumPHat (:55-60);
+ * that is kept unless swap_fix. */
+static inline void combine_reservoirs(or_reservoir *self, const or_reservoir *other, const float *p_hat,
+                                      int swap_fix, pcg_t *rng) {
     self->m += other->m;
-    float weight = p_hat * other->w * (float)other->m;
-    if (weight > 0.0f)
-        update_reservoir(self, weight, f4xyz(other->pos_lum), other->normal, other->pos_lum.w, other->light_index,
-                         p_hat, other->w, rng);
-    if (self->w > 0.0f) self->w = self->sum_weights / ((float)self->m * self->p_hat);
+    for (int i = 0; i < OR_RS; ++i) {
+        const or_sample *o = &other->s[i];
+        float weight = p_hat[i] * o->w * (float)other->m;
+        if (weight > 0.0f) {
+#if OR_MIS
+            const float wv = swap_fix ? o->w : o->sum_phat;
+            const float sp = swap_fix ? o->sum_phat : o->w;
+#else
+            const float wv = o->w, sp = 0.0f;
+            (void)swap_fix;
+#endif
+            update_reservoir_at(self, i, weight, f4xyz(o->pos_lum), o->normal, o->pos_lum.w, o->light_index, p_hat[i],
+                                wv, sp, rng);
+        }
+        if (self->s[i].w > 0.0f) self->s[i].w = self->s[i].sum_weights / ((float)self->m * self->s[i].p_hat);
+    }
 }
 /* :66-76; the fields the reference leaves uninitialised are defined as zero */
 static inline void new_reservoir(or_reservoir *r) { memset(r, 0, sizeof(*r)); }
+
+void or_reservoir_layout(int32_t *rs, int32_t *mis, int32_t *bytes) {
+    if (rs) *rs = OR_RS;
+    if (mis) *mis = OR_MIS;
+    if (bytes) *bytes = (int32_t)sizeof(or_reservoir);
+}
+
+void or_reservoir_script(const float *cand, int32_t n, const or_reservoir *other, const float *other_phat,
+                         uint64_t seed, uint64_t seq, int32_t swap_fix, or_reservoir *out) {
+    pcg_t rng = pcg_seed(seed, seq);
+    or_reservoir r;
+    new_reservoir(&r);
+    for (int32_t k = 0; k < n; ++k) {
+        const float *c = cand + 12 * (size_t)k;
+        or_f4 nrm;
+        nrm.x = c[3]; nrm.y = c[4]; nrm.z = c[5]; nrm.w = c[6];
+        int32_t idx;
+        memcpy(&idx, &c[8], 4);
+        add_sample(&r, V(c[0], c[1], c[2]), nrm, c[7], idx, c[9], c[10], &rng);
+    }
+    if (other) combine_reservoirs(&r, other, other_phat, swap_fix, &rng);
+    *out = r;
+}
 
 static int crop_ok(const int32_t *crop, int W, int H, int *x0, int *y0, int *cw, int *ch) {
     if (!crop) { *x0 = 0; *y0 = 0; *cw = W; *ch = H; return 1; }
@@ -603,17 +649,24 @@ int or_initial_temporal_learned(const or_scene *sc, const or_gbuffer *cur, const
                                          t.roughness, t.metallic);
                     add_sample(&res, lpos, ln, llum, lidx, ph, prob, &rng);
                 }
-                if ((u->flags & OR_FLAG_FINAL_RIS_WEIGHT) && res.sum_weights > 0.0f)
-                    res.w = res.sum_weights / ((float)res.m * res.p_hat);
+                if (u->flags & OR_FLAG_FINAL_RIS_WEIGHT)
+                    for (int i = 0; i < OR_RS; ++i)
+                        if (res.s[i].sum_weights > 0.0f)
+                            res.s[i].w = res.s[i].sum_weights / ((float)res.m * res.s[i].p_hat);
             }
             /* visibility reuse :147-160 -- a background pixel's (zero normal) sample is
              * undefined in the reference; here it is the zero sample, for which zeroing
              * w and sumWeights changes nothing, so no ray is traced for it. */
             if ((u->flags & OR_FLAG_VISIBILITY) && !zero_normal) {
-                ++my_rays;
-                if (test_visibility(sc, t.wpos, f4xyz(res.pos_lum), &tc)) {
-                    res.w = 0.0f;
-                    res.sum_weights = 0.0f;
+                for (int i = 0; i < OR_RS; ++i) {
+                    ++my_rays;
+                    if (test_visibility(sc, t.wpos, f4xyz(res.s[i].pos_lum), &tc)) {
+                        res.s[i].w = 0.0f;
+                        res.s[i].sum_weights = 0.0f;
+#if OR_MIS
+                        res.s[i].sum_phat = 0.0f;
+#endif
+                    }
                 }
             }
             /* temporal reuse :162-209 */
@@ -638,10 +691,12 @@ int or_initial_temporal_learned(const or_scene *sc, const or_gbuffer *cur, const
                                 or_reservoir pr = prev_res[(size_t)fy * u->size[0] + (size_t)fx];
                                 uint32_t cap = u->temporal_mult * res.m;
                                 pr.m = pr.m < cap ? pr.m : cap;
-                                float ph = eval_phat(t.wpos, f4xyz(pr.pos_lum), cam, t.normal, f4xyz(pr.normal),
-                                                     pr.normal.w > 0.5f, albedo_lum, pr.pos_lum.w, t.roughness,
-                                                     t.metallic);
-                                combine_reservoirs(&res, &pr, ph, &rng);
+                                float ph[OR_RS];
+                                for (int i = 0; i < OR_RS; ++i)
+                                    ph[i] = eval_phat(t.wpos, f4xyz(pr.s[i].pos_lum), cam, t.normal,
+                                                      f4xyz(pr.s[i].normal), pr.s[i].normal.w > 0.5f, albedo_lum,
+                                                      pr.s[i].pos_lum.w, t.roughness, t.metallic);
+                                combine_reservoirs(&res, &pr, ph, (u->flags & OR_FLAG_MIS_SWAP_FIX) != 0, &rng);
                             }
                         }
                     }
@@ -693,9 +748,11 @@ int or_spatial_biased(const or_scene *sc, const or_gbuffer *g, const or_reservoi
             v3 nnor = V(or_half_to_float(nn[0]), or_half_to_float(nn[1]), or_half_to_float(nn[2]));
             if (fabsf(nd - t.depth) > u->pos_threshold * fabsf(t.depth) || vdot(nnor, t.normal) < cos_thr) continue;
             const or_reservoir *rr = &in[ni];
-            float ph = eval_phat(t.wpos, f4xyz(rr->pos_lum), cam, t.normal, f4xyz(rr->normal), rr->normal.w > 0.5f,
-                                 albedo_lum, rr->pos_lum.w, t.roughness, t.metallic);
-            combine_reservoirs(&res, rr, ph, &rng);
+            float ph[OR_RS];
+            for (int j = 0; j < OR_RS; ++j)
+                ph[j] = eval_phat(t.wpos, f4xyz(rr->s[j].pos_lum), cam, t.normal, f4xyz(rr->s[j].normal),
+                                  rr->s[j].normal.w > 0.5f, albedo_lum, rr->s[j].pos_lum.w, t.roughness, t.metallic);
+            combine_reservoirs(&res, rr, ph, (u->flags & OR_FLAG_MIS_SWAP_FIX) != 0, &rng);
         }
         out[ri] = res;
     }
@@ -733,7 +790,10 @@ int or_spatial_unbiased(const or_scene *sc, const or_gbuffer *g, const or_reserv
             pcg_t rng = pcg_seed((uint64_t)(u->frame * 17u + (uint32_t)pass_index), (uint64_t)((uint32_t)y * 10007u + (uint32_t)x));
             int npx[64], npy[64];
             uint32_t nm[64];
-            uint32_t orig_m = res.m;
+#if OR_MIS
+            float nsp[OR_RS][64], orig_sp[OR_RS];
+            for (int i = 0; i < OR_RS; ++i) orig_sp[i] = res.s[i].sum_phat;
+#endif
             for (int i = 0; i < num_neighbors; ++i) {
                 float angle = rand_float(&rng) * 2.0f * PI_F;
                 float radius = sqrtf(rand_float(&rng)) * u->spatial_radius;
@@ -744,36 +804,74 @@ int or_spatial_unbiased(const or_scene *sc, const or_gbuffer *g, const or_reserv
                 const or_reservoir *rr = &in[(size_t)ny * (size_t)W + (size_t)nx];
                 npx[i] = nx; npy[i] = ny;
                 nm[i] = rr->m;
+#if OR_MIS
+                for (int j = 0; j < OR_RS; ++j) nsp[j][i] = rr->s[j].sum_phat;
+#endif
                 res.m += rr->m;
-                float ph = eval_phat(t.wpos, f4xyz(rr->pos_lum), cam, t.normal, f4xyz(rr->normal), rr->normal.w > 0.5f,
-                                     albedo_lum, rr->pos_lum.w, t.roughness, t.metallic);
-                float weight = ph * rr->w * (float)rr->m;
-                if (weight > 0.0f)
-                    update_reservoir(&res, weight, f4xyz(rr->pos_lum), rr->normal, rr->pos_lum.w, rr->light_index, ph,
-                                     rr->w, &rng);
+                for (int j = 0; j < OR_RS; ++j) {
+                    const or_sample *o = &rr->s[j];
+                    float ph = eval_phat(t.wpos, f4xyz(o->pos_lum), cam, t.normal, f4xyz(o->normal),
+                                         o->normal.w > 0.5f, albedo_lum, o->pos_lum.w, t.roughness, t.metallic);
+                    float weight = ph * o->w * (float)rr->m;
+#if OR_MIS
+                    const float sp = o->sum_phat;
+#else
+                    const float sp = 0.0f;
+#endif
+                    if (weight > 0.0f)
+                        update_reservoir_at(&res, j, weight, f4xyz(o->pos_lum), o->normal, o->pos_lum.w,
+                                            o->light_index, ph, o->w, sp, &rng);
+                }
             }
-            v3 lpos = f4xyz(res.pos_lum);
-            uint32_t ns = orig_m;
-            for (int j = 0; j < num_neighbors; ++j) {
-                texel_t nt;
-                fetch_texel(g, npx[j], npy[j], &nt);
-                if (vdot(vsub(lpos, nt.wpos), nt.normal) < 0.0f) continue;
+            texel_t nt[64];
+            for (int j = 0; j < num_neighbors; ++j) fetch_texel(g, npx[j], npy[j], &nt[j]);
+            for (int i = 0; i < OR_RS; ++i) {
+                v3 lpos = f4xyz(res.s[i].pos_lum);
+#if OR_MIS
+                float sum_phat = orig_sp[i];
+#else
+                uint32_t ns = in[ri].m;  /* the reservoir's own count before the merges */
+#endif
+                for (int j = 0; j < num_neighbors; ++j) {
+                    if (vdot(vsub(lpos, nt[j].wpos), nt[j].normal) < 0.0f) continue;
+                    if (vis) {
+                        ++my_rays;
+                        if (test_visibility(sc, nt[j].wpos, lpos, &tc)) continue;
+                    }
+#if OR_MIS
+                    sum_phat += nsp[i][j];
+#else
+                    ns += nm[j];
+#endif
+                }
                 if (vis) {
                     ++my_rays;
-                    if (test_visibility(sc, nt.wpos, lpos, &tc)) continue;
+                    if (test_visibility(sc, t.wpos, lpos, &tc)) {
+#if OR_MIS
+                        sum_phat = 0.0f;
+#else
+                        ns = 0;
+#endif
+                    }
                 }
-                ns += nm[j];
+#if OR_MIS
+                if (sum_phat > 0.0f) {
+                    res.s[i].w = res.s[i].sum_weights * res.s[i].p_hat / (sum_phat * res.s[i].p_hat);
+                } else {
+                    res.s[i].w = 0.0f;
+                    res.s[i].sum_weights = 0.0f;
+                    res.s[i].sum_phat = 0.0f;
+                }
+#else
+                if (ns > 0) {
+                    res.s[i].w = res.s[i].sum_weights / ((float)ns * res.s[i].p_hat);
+                } else {
+                    res.s[i].w = 0.0f;
+                    res.s[i].sum_weights = 0.0f;
+                }
+#endif
             }
-            if (vis) {
-                ++my_rays;
-                if (test_visibility(sc, t.wpos, lpos, &tc)) ns = 0;
-            }
-            if (ns > 0) {
-                res.w = res.sum_weights / ((float)ns * res.p_hat);
-            } else {
-                res.w = 0.0f;
-                res.sum_weights = 0.0f;
-            }
+            (void)nm;
             out[ri] = res;
         }
 #pragma omp critical
@@ -804,18 +902,22 @@ int or_shade(const or_scene *sc, const or_gbuffer *g, const or_reservoir *resv, 
         fetch_texel(g, x, y, &t);
         size_t ri = (size_t)y * (size_t)W + (size_t)x;
         const or_reservoir *r = &resv[ri];
-        v3 emission;
-        if (r->light_index < 0) {
-            int k = -1 - r->light_index;
-            emission = (k < sc->n_tri_lights) ? f4xyz(sc->tri_lights[k].emission_lum) : V(0.0f, 0.0f, 0.0f);
-        } else {
-            int k = r->light_index;
-            emission = (k < sc->n_point_lights) ? f4xyz(sc->point_lights[k].color_lum) : V(0.0f, 0.0f, 0.0f);
+        v3 col = V(0.0f, 0.0f, 0.0f);
+        for (int i = 0; i < OR_RS; ++i) {
+            const or_sample *sm = &r->s[i];
+            v3 emission;
+            if (sm->light_index < 0) {
+                int k = -1 - sm->light_index;
+                emission = (k < sc->n_tri_lights) ? f4xyz(sc->tri_lights[k].emission_lum) : V(0.0f, 0.0f, 0.0f);
+            } else {
+                int k = sm->light_index;
+                emission = (k < sc->n_point_lights) ? f4xyz(sc->point_lights[k].color_lum) : V(0.0f, 0.0f, 0.0f);
+            }
+            v3 ph = eval_phat_full(t.wpos, f4xyz(sm->pos_lum), cam, t.normal, f4xyz(sm->normal), sm->normal.w > 0.5f,
+                                   t.albedo, emission, t.roughness, t.metallic);
+            col = V(col.x + ph.x * sm->w, col.y + ph.y * sm->w, col.z + ph.z * sm->w);
         }
-        v3 ph = eval_phat_full(t.wpos, f4xyz(r->pos_lum), cam, t.normal, f4xyz(r->normal), r->normal.w > 0.5f,
-                               t.albedo, emission, t.roughness, t.metallic);
-        v3 col = V(0.0f + ph.x * r->w, 0.0f + ph.y * r->w, 0.0f + ph.z * r->w);
-        col = vdivs(col, 1.0f); /* RESERVOIR_SIZE */
+        col = vdivs(col, (float)OR_RS); /* RESERVOIR_SIZE */
         if (t.albedo_a > 0.5f) col = t.albedo;
         if (u->gamma != 1.0f) col = V(powf(col.x, inv_gamma), powf(col.y, inv_gamma), powf(col.z, inv_gamma));
         rgba[4 * ri] = col.x; rgba[4 * ri + 1] = col.y; rgba[4 * ri + 2] = col.z; rgba[4 * ri + 3] = 1.0f;

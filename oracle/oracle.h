@@ -38,13 +38,32 @@ extern "C" {
 
 typedef struct { float x, y, z, w; } or_f4;
 
-typedef struct {             /* Reservoir with RESERVOIR_SIZE 1: 64 bytes */
+/* Compile-time variants of the reference (restirStructs.glsl:16-17):
+ * OR_RS = RESERVOIR_SIZE, OR_MIS = UNBIASED_MIS.  The default build is the
+ * reference's configuration (1, off); oracle/Makefile builds the others as
+ * separate libraries with the same symbols. */
+#ifndef OR_RS
+#define OR_RS 1
+#endif
+#ifndef OR_MIS
+#define OR_MIS 0
+#endif
+
+typedef struct {             /* LightSample (std430): 48 bytes, 64 with UNBIASED_MIS */
     or_f4 pos_lum;           /* position_emissionLum */
     or_f4 normal;            /* light normal, w>0.5 => use it */
     int32_t light_index;     /* negative: triangle light -1-i */
     float p_hat;
     float sum_weights;
     float w;
+#if OR_MIS
+    float sum_phat;
+    float pad_s[3];
+#endif
+} or_sample;
+
+typedef struct {             /* Reservoir: OR_RS samples + numStreamSamples (64 bytes in the default build) */
+    or_sample s[OR_RS];
     uint32_t m;              /* numStreamSamples */
     uint32_t pad[3];
 } or_reservoir;
@@ -81,6 +100,7 @@ typedef struct {             /* LightingPassUniforms: 96 bytes */
 #define OR_FLAG_VISIBILITY 1
 #define OR_FLAG_TEMPORAL 2
 #define OR_FLAG_FINAL_RIS_WEIGHT 256 /* extension: W = sumWeights / (M * pHat) after RIS */
+#define OR_FLAG_MIS_SWAP_FIX 2048    /* extension (UNBIASED_MIS): combineReservoirs passes (w, sumPHat) in order */
 
 typedef struct {
     const or_node *nodes; int32_t n_nodes;
@@ -172,6 +192,15 @@ void or_mlp_sample(const or_mlp *m, const or_gbuffer *g, const float cam[3], uin
                    int32_t n, const int32_t *rows, int32_t *keys, float *qs);
 double or_mlp_loss_grad(const or_mlp *m, const double *params64, const or_gbuffer *g, const float cam[3], int32_t n,
                         const int32_t *rows, const int32_t *target, int32_t emulate, double *grad);
+
+/* ---- reservoir variants ---- */
+void or_reservoir_layout(int32_t *reservoir_size, int32_t *unbiased_mis, int32_t *bytes);
+/* newReservoir, addSampleToReservoir for each of n candidates (12 floats:
+ * position xyz, normal xyzw, emission luminance, light index (int bits),
+ * p-hat, source pdf, unused), then combineReservoirs(other, other_phat[OR_RS])
+ * when other != NULL; PCG stream (seed, seq). */
+void or_reservoir_script(const float *cand, int32_t n, const or_reservoir *other, const float *other_phat,
+                         uint64_t seed, uint64_t seq, int32_t swap_fix, or_reservoir *out);
 
 int or_max_threads(void);
 void or_set_threads(int32_t n);

@@ -22,9 +22,9 @@ REFERENCE_ROOT = Path(os.environ.get("RESTIR_REFERENCE", "/root/reference"))
 def build(ref: bool | None = None) -> None:
     """Builds liboracle.so and, when the reference sources exist, _ref/libref.so."""
     env = dict(os.environ)
-    r = subprocess.run(["make", "-C", str(HERE), "liboracle.so"], capture_output=True, text=True, env=env)
+    r = subprocess.run(["make", "-C", str(HERE), "all"], capture_output=True, text=True, env=env)
     if r.returncode != 0:  # retry without OpenMP (toolchains without libgomp)
-        r = subprocess.run(["make", "-C", str(HERE), "liboracle.so", "OMP="], capture_output=True, text=True, env=env)
+        r = subprocess.run(["make", "-C", str(HERE), "all", "OMP="], capture_output=True, text=True, env=env)
         if r.returncode != 0:
             raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
     if ref is None:
@@ -259,3 +259,58 @@ def initial_temporal_learned(scene, g_cur, g_prev, prev_res, out, uniforms, cand
                                                P(out), C.byref(uniforms), C.byref(lrn), crop_arg(crop),
                                                C.byref(stats) if stats else None),
           "initial_temporal_learned")
+
+
+# ---------------------------------------------------------------- reservoir variants
+VARIANT_LIBS = {(1, 0): "liboracle.so", (2, 0): "liboracle_rs2.so", (1, 1): "liboracle_mis.so",
+                (2, 1): "liboracle_rs2_mis.so"}
+_variant_handles = {}
+
+
+def reservoir_dtype(rs: int, mis: int) -> np.dtype:
+    """std430 Reservoir with RESERVOIR_SIZE rs and UNBIASED_MIS mis."""
+    sample = [("pos_lum", "<f4", 4), ("normal", "<f4", 4), ("light_index", "<i4"), ("p_hat", "<f4"),
+              ("sum_weights", "<f4"), ("w", "<f4")]
+    if mis:
+        sample += [("sum_phat", "<f4"), ("pad_s", "<f4", 3)]
+    return np.dtype([("s", np.dtype(sample), (rs,)), ("m", "<u4"), ("pad", "<u4", 3)])
+
+
+def oracle_variant(rs: int, mis: int):
+    """The oracle built for RESERVOIR_SIZE rs / UNBIASED_MIS mis (same symbols as oracle())."""
+    key = (rs, mis)
+    if key not in _variant_handles:
+        path = HERE / VARIANT_LIBS[key]
+        if not path.exists():
+            build(ref=False)
+        h = C.CDLL(str(path))
+        for name in ("or_initial_temporal", "or_spatial_biased", "or_spatial_unbiased", "or_shade"):
+            getattr(h, name).restype = C.c_int
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        h.or_reservoir_layout(C.byref(a), C.byref(b), C.byref(c))
+        assert (a.value, b.value) == key and c.value == reservoir_dtype(rs, mis).itemsize
+        _variant_handles[key] = h
+    return _variant_handles[key]
+
+
+def ref_reservoir(rs: int, mis: int):
+    """The reference's own reservoir.glsl compiled for the variant (None if not built)."""
+    p = HERE / "_ref" / f"libref_res_rs{rs}_mis{mis}.so"
+    return C.CDLL(str(p)) if p.exists() else None
+
+
+def to_flat(res: np.ndarray, rs: int) -> np.ndarray:
+    """Reservoirs of a variant dtype -> the interchange layout of the reference bridge."""
+    out = np.zeros((len(res), 16 * rs + 4), np.float32)
+    for i in range(rs):
+        s = res["s"][:, i]
+        out[:, 16 * i:16 * i + 4] = s["pos_lum"]
+        out[:, 16 * i + 4:16 * i + 8] = s["normal"]
+        out[:, 16 * i + 8] = s["light_index"].view(np.float32)
+        out[:, 16 * i + 9] = s["p_hat"]
+        out[:, 16 * i + 10] = s["sum_weights"]
+        out[:, 16 * i + 11] = s["w"]
+        if "sum_phat" in s.dtype.names:
+            out[:, 16 * i + 12] = s["sum_phat"]
+    out[:, 16 * rs] = res["m"].view(np.float32)
+    return out

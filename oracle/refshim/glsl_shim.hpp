@@ -64,6 +64,7 @@ struct vec4 {
     gfloat w;
     vec4() = default;
     constexpr vec4(gfloat a, gfloat b, gfloat c, gfloat d) : xyz(a, b, c), w(d) {}
+    constexpr vec4(vec3 v, gfloat d) : xyz(v), w(d) {}
 };
 
 inline vec3 operator+(vec3 a, vec3 b) { return vec3(a.x + b.x, a.y + b.y, a.z + b.z); }
