@@ -71,6 +71,11 @@ extern "C" {
  * LEARNED_TRAIN adds one training step on the frame's final reservoirs. */
 #define RG_FLAG_LEARNED_PROPOSAL 512
 #define RG_FLAG_LEARNED_TRAIN 1024
+/* Extension for the UNBIASED_MIS format (off by default): combineReservoirs
+ * passes the merged sample's (w, sumPHat) in the order updateReservoirAt
+ * declares them; the reference passes them swapped (reservoir.glsl:55-60),
+ * which is what the passes do without this flag. */
+#define RG_FLAG_MIS_SWAP_FIX 2048
 
 /* Deepest BVH the traversal accepts: its stack holds depth+1 entries. */
 #define RG_MAX_TREE_DEPTH 63
@@ -220,6 +225,20 @@ int rg_build_alias_table(const rg_point_light *point_lights, int32_t n_point, co
 /* CPU primary-ray G-buffer (host planes, same formats as rg_gbuffer). */
 int rg_trace_gbuffer_host(const rg_scene_desc *scene, const rg_camera *cam, int32_t width, int32_t height,
                           uint8_t *albedo, uint16_t *normal, uint16_t *material, float *world_pos, float *depth);
+
+/* ---- reservoir format ----
+ * The reference's compile-time variants (restirStructs.glsl:16-17):
+ * RESERVOIR_SIZE samples per reservoir (1 or 2) and UNBIASED_MIS (0 or 1,
+ * a sumPHat per sample, used by the unbiased pass's normalisation).  The
+ * default is the reference's (1, 0), the rg_reservoir layout.  Otherwise the
+ * reservoir buffers every pass reads and writes hold rg_reservoir_bytes()
+ * bytes per pixel in the std430 layout: `samples` LightSamples of 48 bytes
+ * (64 with MIS: sumPHat, then 12 bytes of padding) followed by
+ * numStreamSamples, padded to 16 bytes.  The frame driver reallocates its
+ * buffers; the batched views, the learned proposal's training and the
+ * allocation-free chain accept only the default format. */
+int rg_set_reservoir_format(rg_context *ctx, int32_t samples, int32_t unbiased_mis);
+int rg_reservoir_bytes(rg_context *ctx);
 
 /* ---- scene upload (host pointers; copied to device, synchronous) ---- */
 int rg_upload_scene(rg_context *ctx, const rg_scene_desc *scene);

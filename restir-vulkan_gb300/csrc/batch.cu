@@ -161,6 +161,7 @@ int rg_batch_create(rg_context *ctx, const rg_view *views, int32_t n_views, cons
     int rc = rg_internal_prepare(ctx, &s, &device);
     if (rc) return rc;
     if (!views || !fp || !out || n_views <= 0 || n_views > 65536) return bfail(RG_ERR_INVALID_ARGUMENT, "bad arguments");
+    if (s->res_samples != 1 || s->res_mis) return bfail(RG_ERR_UNSUPPORTED, "batched views need the default reservoir format");
     *out = nullptr;
     const int passes = fp->spatial_iterations < 0 ? 0 : fp->spatial_iterations;
     if (fp->unbiased && (fp->unbiased_neighbors < 0 || fp->unbiased_neighbors > 16))

@@ -79,6 +79,8 @@ struct rg_context {
     unsigned long long *counters = nullptr;
     int *mma_timeouts = nullptr;
     ProposalState *proposal = nullptr;  // learned proposal (proposal.cu), tied to the uploaded lights
+    int res_samples = 1, res_mis = 0;   // reservoir format (rg_set_reservoir_format)
+    size_t frame_bytes = 0;             // bytes per pixel of the frame driver's reservoir buffers
     // frame driver
     int fw = 0, fh = 0;
     rg_reservoir *res[2] = {nullptr, nullptr};
@@ -326,6 +328,8 @@ int rg_upload_scene(rg_context *ctx, const rg_scene_desc *sc) {
     s.n_materials = sc->n_materials;
     s.counters = ctx->counters;
     s.mma_timeouts = ctx->mma_timeouts;
+    s.res_samples = ctx->res_samples;
+    s.res_mis = ctx->res_mis;
     ctx->has_scene = true;
     return RG_OK;
 }
@@ -428,24 +432,48 @@ int rg_trace_gbuffer(rg_context *ctx, const rg_camera *cam, const rg_gbuffer_out
     return RG_OK;
 }
 
+static size_t reservoir_bytes(int samples, int mis) { return (size_t)samples * (mis ? 64 : 48) + 16; }
+
 static int ensure_frame_buffers(rg_context *ctx, int w, int h, cudaStream_t st) {
-    if (ctx->fw == w && ctx->fh == h && ctx->res[0]) return RG_OK;
+    const size_t rb = reservoir_bytes(ctx->res_samples, ctx->res_mis);
+    if (ctx->fw == w && ctx->fh == h && ctx->res[0] && ctx->frame_bytes == rb) return RG_OK;
     ctx->release_frame();
     const size_t np = (size_t)w * (size_t)h;
-    cudaError_t e = dev_alloc(&ctx->res[0], np);
-    if (e == cudaSuccess) e = dev_alloc(&ctx->res[1], np);
-    if (e == cudaSuccess) e = dev_alloc(&ctx->tmp, np);
+    const size_t units = (np * rb + sizeof(rg_reservoir) - 1) / sizeof(rg_reservoir);
+    cudaError_t e = dev_alloc(&ctx->res[0], units);
+    if (e == cudaSuccess) e = dev_alloc(&ctx->res[1], units);
+    if (e == cudaSuccess) e = dev_alloc(&ctx->tmp, units);
     if (e == cudaSuccess) e = dev_alloc(&ctx->image, np);
     // zero-filled at creation, as the reference's fillBuffer (src/app.h:276,283)
-    for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaMemsetAsync(ctx->res[k], 0, np * sizeof(rg_reservoir), st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->tmp, 0, np * sizeof(rg_reservoir), st);
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaMemsetAsync(ctx->res[k], 0, np * rb, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->tmp, 0, np * rb, st);
     if (e != cudaSuccess) {
         ctx->release_frame();
         return cuda_fail(e, "frame buffers");
     }
     ctx->fw = w;
     ctx->fh = h;
+    ctx->frame_bytes = rb;
     return RG_OK;
+}
+
+int rg_set_reservoir_format(rg_context *ctx, int32_t samples, int32_t unbiased_mis) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if ((samples != 1 && samples != 2) || (unbiased_mis != 0 && unbiased_mis != 1))
+        return fail(RG_ERR_INVALID_ARGUMENT, "reservoir format: samples 1 or 2, unbiased_mis 0 or 1");
+    RG_CUDA(cudaDeviceSynchronize(), "rg_set_reservoir_format");
+    ctx->res_samples = samples;
+    ctx->res_mis = unbiased_mis;
+    ctx->scene.res_samples = samples;
+    ctx->scene.res_mis = unbiased_mis;
+    return RG_OK;
+}
+
+int rg_reservoir_bytes(rg_context *ctx) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    return (int)reservoir_bytes(ctx->res_samples, ctx->res_mis);
 }
 
 int rg_render_frame(rg_context *ctx, const rg_gbuffer *cur, const rg_gbuffer *prev, int32_t slot,

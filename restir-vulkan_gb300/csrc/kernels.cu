@@ -63,73 +63,126 @@ __device__ __forceinline__ void load_texel(const GBufView &g, size_t i, Texel &t
     t.wpos = load_wpos(g, i);
 }
 
+template <int R_, bool MIS_>
+struct FormatTag {
+    static constexpr int R = R_;
+    static constexpr bool MIS = MIS_;
+};
+
 // ---------------------------------------------------------------- reservoirs
-struct Res {
-    float4 pos_lum;
-    float4 nrm;
-    int32_t idx;
-    float p_hat, sum_w, w;
+// Reservoir with R samples (RESERVOIR_SIZE) and, with MIS (UNBIASED_MIS), a
+// sumPHat per sample (restirStructs.glsl:16-34).  In memory: the std430
+// layout, R LightSamples of 48 bytes (64 with MIS) then numStreamSamples,
+// padded to 16 bytes; R = 1 without MIS is rg_reservoir (64 bytes).
+template <int R, bool MIS>
+struct ResV {
+    float4 pos_lum[R];
+    float4 nrm[R];
+    int32_t idx[R];
+    float p_hat[R], sum_w[R], w[R];
+    float sum_phat[MIS ? R : 1];
     uint32_t m;
 };
-__device__ __forceinline__ Res load_res(const rg_reservoir *base, size_t i) {
-    const float4 *p = reinterpret_cast<const float4 *>(base + i);
-    Res r;
-    r.pos_lum = __ldg(p);
-    r.nrm = __ldg(p + 1);
-    const float4 c = __ldg(p + 2);
-    const float4 d = __ldg(p + 3);
-    r.idx = __float_as_int(c.x);
-    r.p_hat = c.y;
-    r.sum_w = c.z;
-    r.w = c.w;
-    r.m = __float_as_uint(d.x);
+template <int R, bool MIS>
+struct ResLayout {
+    static constexpr int kSample4 = MIS ? 4 : 3;          // float4 words per sample
+    static constexpr int kWords = R * kSample4 + 1;       // float4 words per reservoir
+};
+
+template <int R, bool MIS>
+__device__ __forceinline__ ResV<R, MIS> load_resv(const rg_reservoir *base, size_t i) {
+    using L = ResLayout<R, MIS>;
+    const float4 *p = reinterpret_cast<const float4 *>(base) + i * L::kWords;
+    ResV<R, MIS> r;
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        r.pos_lum[j] = __ldg(p + j * L::kSample4);
+        r.nrm[j] = __ldg(p + j * L::kSample4 + 1);
+        const float4 c = __ldg(p + j * L::kSample4 + 2);
+        r.idx[j] = __float_as_int(c.x);
+        r.p_hat[j] = c.y;
+        r.sum_w[j] = c.z;
+        r.w[j] = c.w;
+        if (MIS) r.sum_phat[j] = __ldg(p + j * L::kSample4 + 3).x;
+    }
+    r.m = __float_as_uint(__ldg(p + R * L::kSample4).x);
     return r;
 }
-__device__ __forceinline__ void store_res(rg_reservoir *base, size_t i, const Res &r) {
-    float4 *p = reinterpret_cast<float4 *>(base + i);
-    p[0] = r.pos_lum;
-    p[1] = r.nrm;
-    p[2] = make_float4(__int_as_float(r.idx), r.p_hat, r.sum_w, r.w);
-    p[3] = make_float4(__uint_as_float(r.m), 0.0f, 0.0f, 0.0f);
+template <int R, bool MIS>
+__device__ __forceinline__ void store_resv(rg_reservoir *base, size_t i, const ResV<R, MIS> &r) {
+    using L = ResLayout<R, MIS>;
+    float4 *p = reinterpret_cast<float4 *>(base) + i * L::kWords;
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        p[j * L::kSample4] = r.pos_lum[j];
+        p[j * L::kSample4 + 1] = r.nrm[j];
+        p[j * L::kSample4 + 2] = make_float4(__int_as_float(r.idx[j]), r.p_hat[j], r.sum_w[j], r.w[j]);
+        if (MIS) p[j * L::kSample4 + 3] = make_float4(r.sum_phat[j], 0.0f, 0.0f, 0.0f);
+    }
+    p[R * L::kSample4] = make_float4(__uint_as_float(r.m), 0.0f, 0.0f, 0.0f);
 }
-__device__ __forceinline__ Res empty_res() {
-    Res r;
-    r.pos_lum = make_float4(0.f, 0.f, 0.f, 0.f);
-    r.nrm = make_float4(0.f, 0.f, 0.f, 0.f);
-    r.idx = 0;
-    r.p_hat = 0.f;
-    r.sum_w = 0.f;
-    r.w = 0.f;
+
+template <int R, bool MIS>
+__device__ __forceinline__ ResV<R, MIS> empty_resv() {
+    ResV<R, MIS> r;
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        r.pos_lum[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        r.nrm[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        r.idx[j] = 0;
+        r.p_hat[j] = 0.f;
+        r.sum_w[j] = 0.f;
+        r.w[j] = 0.f;
+        if (MIS) r.sum_phat[j] = 0.f;
+    }
     r.m = 0u;
     return r;
 }
 // reservoir.glsl:6-26
-__device__ __forceinline__ void update_res(Res &r, float weight, float4 pos_lum, float4 nrm, int32_t idx, float p_hat,
-                                           float w, Pcg &rng) {
-    r.sum_w += weight;
-    const float replace = weight / r.sum_w;
+template <int R, bool MIS>
+__device__ __forceinline__ void update_at(ResV<R, MIS> &r, int j, float weight, float4 pos_lum, float4 nrm,
+                                          int32_t idx, float p_hat, float w, float sum_phat, Pcg &rng) {
+    r.sum_w[j] += weight;
+    const float replace = weight / r.sum_w[j];
     if (rand_float(rng) < replace) {
-        r.pos_lum = pos_lum;
-        r.nrm = nrm;
-        r.idx = idx;
-        r.p_hat = p_hat;
-        r.w = w;
+        r.pos_lum[j] = pos_lum;
+        r.nrm[j] = nrm;
+        r.idx[j] = idx;
+        r.p_hat[j] = p_hat;
+        r.w[j] = w;
+        if (MIS) r.sum_phat[j] += sum_phat;
     }
 }
 // reservoir.glsl:28-42
-__device__ __forceinline__ void add_sample(Res &r, float4 pos_lum, float4 nrm, int32_t idx, float p_hat, float sample_p,
-                                           Pcg &rng) {
+template <int R, bool MIS>
+__device__ __forceinline__ void add_sample(ResV<R, MIS> &r, float4 pos_lum, float4 nrm, int32_t idx, float p_hat,
+                                           float sample_p, Pcg &rng) {
     const float weight = p_hat / sample_p;
     r.m += 1u;
-    const float w = (r.sum_w + weight) / ((float)r.m * p_hat);
-    update_res(r, weight, pos_lum, nrm, idx, p_hat, w, rng);
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        const float w = (r.sum_w[j] + weight) / ((float)r.m * p_hat);
+        update_at(r, j, weight, pos_lum, nrm, idx, p_hat, w, p_hat, rng);
+    }
 }
-// reservoir.glsl:44-64
-__device__ __forceinline__ void combine_res(Res &self, const Res &other, float p_hat, Pcg &rng) {
+// reservoir.glsl:44-64.  With MIS the reference passes other's sumPHat where
+// updateReservoirAt takes w and other's w where it takes sumPHat (:55-60);
+// RG_FLAG_MIS_SWAP_FIX passes them in the declared order instead.
+template <int R, bool MIS>
+__device__ __forceinline__ void combine_res(ResV<R, MIS> &self, const ResV<R, MIS> &other, const float (&p_hat)[R],
+                                            bool swap_fix, Pcg &rng) {
     self.m += other.m;
-    const float weight = p_hat * other.w * (float)other.m;
-    if (weight > 0.0f) update_res(self, weight, other.pos_lum, other.nrm, other.idx, p_hat, other.w, rng);
-    if (self.w > 0.0f) self.w = self.sum_w / ((float)self.m * self.p_hat);
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        const float weight = p_hat[j] * other.w[j] * (float)other.m;
+        if (weight > 0.0f) {
+            const float osp = MIS ? other.sum_phat[j] : 0.0f;
+            const float wv = (MIS && !swap_fix) ? osp : other.w[j];
+            const float sp = (MIS && !swap_fix) ? other.w[j] : osp;
+            update_at(self, j, weight, other.pos_lum[j], other.nrm[j], other.idx[j], p_hat[j], wv, sp, rng);
+        }
+        if (self.w[j] > 0.0f) self.w[j] = self.sum_w[j] / ((float)self.m * self.p_hat[j]);
+    }
 }
 
 __device__ __forceinline__ f3 xyz(float4 v) { return mk(v.x, v.y, v.z); }
@@ -181,9 +234,11 @@ struct InitialParams {
 // drawn uniformly; either way the source pdf is the mixture density
 // mix * q(cluster) * p(light | cluster) + (1 - mix) / N.  The RIS stream keeps
 // the shape of the plain path (two uniforms per candidate).
-__device__ __forceinline__ Res ris(const DevScene &s, const Texel &t, float albedo_lum, f3 cam, uint32_t count_c,
-                                   bool zero_normal, int flags, const mlp::LearnedRis &lr, size_t px, Pcg &rng) {
-    Res r = empty_res();
+template <int R, bool MIS>
+__device__ __forceinline__ ResV<R, MIS> ris(const DevScene &s, const Texel &t, float albedo_lum, f3 cam,
+                                            uint32_t count_c, bool zero_normal, int flags, const mlp::LearnedRis &lr,
+                                            size_t px, Pcg &rng) {
+    ResV<R, MIS> r = empty_resv<R, MIS>();
     if (zero_normal) return r;
     const f3 wo = view_dir(cam, t.wpos);
     const int count = s.n_alias;
@@ -244,22 +299,27 @@ __device__ __forceinline__ Res ris(const DevScene &s, const Texel &t, float albe
                                       pos_lum.w, t.roughness, t.metallic);
         add_sample(r, pos_lum, nrm, lidx, ph, prob, rng);
     }
-    if ((flags & RG_FLAG_FINAL_RIS_WEIGHT) && r.sum_w > 0.0f) r.w = r.sum_w / ((float)r.m * r.p_hat);
+    if (flags & RG_FLAG_FINAL_RIS_WEIGHT) {
+#pragma unroll
+        for (int j = 0; j < R; ++j)
+            if (r.sum_w[j] > 0.0f) r.w[j] = r.sum_w[j] / ((float)r.m * r.p_hat[j]);
+    }
     return r;
 }
 
 #ifndef RG_RIS_MIN_BLOCKS
 #define RG_RIS_MIN_BLOCKS 8
 #endif
-// The pass over one 32 x (4*PPT) pixel tile (tile coordinates bx, by).
-template <int PPT>
+// The pass over one 32 x (4*PPT) pixel tile (tile coordinates bx, by); with
+// R samples per reservoir each pixel traces R visibility segments.
+template <int PPT, int R, bool MIS>
 __device__ __forceinline__ void initial_temporal_tile(const InitialParams &p, int bx, int by) {
     constexpr int kTile = 128 * PPT;
     extern __shared__ __align__(16) unsigned char smem[];
     rgpool::Ray *pool = reinterpret_cast<rgpool::Ray *>(smem);
-    float4 *endp = reinterpret_cast<float4 *>(pool + kTile);  // sample position per pixel slot
-    uint8_t *shadow = reinterpret_cast<uint8_t *>(endp + kTile);
-    int *stack = reinterpret_cast<int *>(shadow + kTile);
+    float4 *endp = reinterpret_cast<float4 *>(pool + kTile * R);  // sample position per (pixel slot, sample)
+    uint8_t *shadow = reinterpret_cast<uint8_t *>(endp + kTile * R);
+    int *stack = reinterpret_cast<int *>(shadow + kTile * R);
     __shared__ int s_count, s_next;
     const int tid = threadIdx.x + threadIdx.y * 32;
     if (tid == 0) { s_count = 0; s_next = 0; }
@@ -270,13 +330,17 @@ __device__ __forceinline__ void initial_temporal_tile(const InitialParams &p, in
     const int y0 = by * (4 * PPT) + threadIdx.y;
     const f3 cam = mk(p.u.camera_pos[0], p.u.camera_pos[1], p.u.camera_pos[2]);
     const bool vis = (p.u.flags & RG_FLAG_VISIBILITY_REUSE) != 0;
+    const bool swap_fix = (p.u.flags & RG_FLAG_MIS_SWAP_FIX) != 0;
     uint64_t rng_state[PPT];
 #pragma unroll
     for (int j = 0; j < PPT; ++j) {
         const int y = y0 + 4 * j;
         const bool valid = x < W && y < H;
         bool want = false;
-        f3 wpos = mk(0.f, 0.f, 0.f), lpos = wpos;
+        f3 wpos = mk(0.f, 0.f, 0.f);
+        float4 lpos[R];
+#pragma unroll
+        for (int q = 0; q < R; ++q) lpos[q] = make_float4(0.f, 0.f, 0.f, 0.f);
         rng_state[j] = 0;
         if (valid) {
             const size_t i = (size_t)y * (size_t)W + (size_t)x;
@@ -285,20 +349,25 @@ __device__ __forceinline__ void initial_temporal_tile(const InitialParams &p, in
             const float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
             Pcg rng = pcg_seed((uint64_t)p.u.frame, (uint64_t)((uint32_t)y * 10007u + (uint32_t)x));
             const bool zero_normal = !(dot(t.normal, t.normal) != 0.0f);
-            const Res r = ris(s, t, albedo_lum, cam, p.u.initial_light_sample_count, zero_normal, p.u.flags,
-                              p.learned, i, rng);
-            store_res(p.out, i, r);
+            const ResV<R, MIS> r = ris<R, MIS>(s, t, albedo_lum, cam, p.u.initial_light_sample_count, zero_normal,
+                                               p.u.flags, p.learned, i, rng);
+            store_resv(p.out, i, r);
             rng_state[j] = rng.state;
             // visibility reuse :147-160; a background pixel's (zero normal) sample is the
             // zero sample, for which zeroing w and sumWeights changes nothing: no ray
             want = vis && !zero_normal;
             wpos = t.wpos;
-            lpos = xyz(r.pos_lum);
+#pragma unroll
+            for (int q = 0; q < R; ++q) lpos[q] = make_float4(r.pos_lum[q].x, r.pos_lum[q].y, r.pos_lum[q].z, 0.0f);
         }
-        shadow[j * 128 + tid] = 0;
-        endp[j * 128 + tid] = make_float4(lpos.x, lpos.y, lpos.z, 0.0f);
-        const int slot = rgpool::append_slot(&s_count, want);
-        if (want) rgpool::put_ray(pool, slot, wpos, j * 128 + tid);
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            const int owner = (j * 128 + tid) * R + q;
+            shadow[owner] = 0;
+            endp[owner] = lpos[q];
+            const int slot = rgpool::append_slot(&s_count, want);
+            if (want) rgpool::put_ray(pool, slot, wpos, owner);
+        }
     }
     __syncthreads();
     rgpool::TraceStats ts;
@@ -312,10 +381,14 @@ __device__ __forceinline__ void initial_temporal_tile(const InitialParams &p, in
         const int y = y0 + 4 * j;
         if (x >= W || y >= H) continue;
         const size_t i = (size_t)y * (size_t)W + (size_t)x;
-        Res r = load_res(p.out, i);
-        if (shadow[j * 128 + tid]) {
-            r.w = 0.0f;
-            r.sum_w = 0.0f;
+        ResV<R, MIS> r = load_resv<R, MIS>(p.out, i);
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            if (shadow[(j * 128 + tid) * R + q]) {
+                r.w[q] = 0.0f;
+                r.sum_w[q] = 0.0f;
+                if (MIS) r.sum_phat[q] = 0.0f;
+            }
         }
         if ((p.u.flags & RG_FLAG_TEMPORAL_REUSE) && p.has_prev) {
             Texel t;
@@ -340,26 +413,30 @@ __device__ __forceinline__ void initial_temporal_tile(const InitialParams &p, in
                     const f3 da = t.albedo - load_albedo(p.prev, pi, nullptr);
                     if (dot(da, da) < 0.01f) {
                         if (dot(t.normal, load_normal(p.prev, pi)) > 0.5f) {
-                            Res pr = load_res(p.prev_res, pi);
+                            ResV<R, MIS> pr = load_resv<R, MIS>(p.prev_res, pi);
                             const uint32_t cap = p.u.temporal_sample_count_multiplier * r.m;
                             pr.m = pr.m < cap ? pr.m : cap;
-                            const float ph = eval_phat_wo(t.wpos, xyz(pr.pos_lum), view_dir(cam, t.wpos), t.normal,
-                                                          xyz(pr.nrm), pr.nrm.w > 0.5f, albedo_lum, pr.pos_lum.w,
-                                                          t.roughness, t.metallic);
-                            combine_res(r, pr, ph, rng);
+                            const f3 wo = view_dir(cam, t.wpos);
+                            float ph[R];
+#pragma unroll
+                            for (int q = 0; q < R; ++q)
+                                ph[q] = eval_phat_wo(t.wpos, xyz(pr.pos_lum[q]), wo, t.normal, xyz(pr.nrm[q]),
+                                                     pr.nrm[q].w > 0.5f, albedo_lum, pr.pos_lum[q].w, t.roughness,
+                                                     t.metallic);
+                            combine_res(r, pr, ph, swap_fix, rng);
                         }
                     }
                 }
             }
         }
-        store_res(p.out, i, r);
+        store_resv(p.out, i, r);
     }
     count_block_rays(s, tid == 0 ? s_count : 0, ts);
 }
 
-template <int PPT>
+template <int PPT, int R, bool MIS>
 __global__ void __launch_bounds__(128, RG_RIS_MIN_BLOCKS) k_initial_temporal(const InitialParams p) {
-    initial_temporal_tile<PPT>(p, blockIdx.x, blockIdx.y);
+    initial_temporal_tile<PPT, R, MIS>(p, blockIdx.x, blockIdx.y);
 }
 
 // ---------------------------------------------------------------- biased spatial (spatialReuse.comp:30-86)
@@ -375,6 +452,7 @@ struct SpatialParams {
 };
 
 // One 32 x 4 pixel tile.
+template <int R, bool MIS>
 __device__ __forceinline__ void spatial_biased_tile(const SpatialParams &p, int bx, int by) {
     const int x = bx * 32 + threadIdx.x;
     const int y = by * 4 + threadIdx.y;
@@ -387,7 +465,8 @@ __device__ __forceinline__ void spatial_biased_tile(const SpatialParams &p, int 
     const float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
     const f3 cam = mk(p.u.camera_pos[0], p.u.camera_pos[1], p.u.camera_pos[2]);
     const f3 wo = view_dir(cam, t.wpos);
-    Res r = load_res(p.in, i);
+    ResV<R, MIS> r = load_resv<R, MIS>(p.in, i);
+    const bool swap_fix = (p.u.flags & RG_FLAG_MIS_SWAP_FIX) != 0;
     Pcg rng = pcg_seed((uint64_t)(p.u.frame * 31u + (uint32_t)p.iter), (uint64_t)((uint32_t)y * 10007u + (uint32_t)x));
     for (uint32_t k = 0; k < p.u.spatial_neighbors; ++k) {
         const float angle = rand_float(rng) * 2.0f * kPi;
@@ -400,16 +479,20 @@ __device__ __forceinline__ void spatial_biased_tile(const SpatialParams &p, int 
         const float nd = __ldg(p.g.depth + ni);
         const f3 nn = load_normal(p.g, ni);
         if (fabsf(nd - depth) > p.u.spatial_pos_threshold * fabsf(depth) || dot(nn, t.normal) < p.cos_thr) continue;
-        const Res rr = load_res(p.in, ni);
-        const float ph = eval_phat_wo(t.wpos, xyz(rr.pos_lum), wo, t.normal, xyz(rr.nrm), rr.nrm.w > 0.5f, albedo_lum,
-                                      rr.pos_lum.w, t.roughness, t.metallic);
-        combine_res(r, rr, ph, rng);
+        const ResV<R, MIS> rr = load_resv<R, MIS>(p.in, ni);
+        float ph[R];
+#pragma unroll
+        for (int q = 0; q < R; ++q)
+            ph[q] = eval_phat_wo(t.wpos, xyz(rr.pos_lum[q]), wo, t.normal, xyz(rr.nrm[q]), rr.nrm[q].w > 0.5f,
+                                 albedo_lum, rr.pos_lum[q].w, t.roughness, t.metallic);
+        combine_res(r, rr, ph, swap_fix, rng);
     }
-    store_res(p.out, i, r);
+    store_resv(p.out, i, r);
 }
 
+template <int R, bool MIS>
 __global__ void __launch_bounds__(128) k_spatial_biased(const SpatialParams p) {
-    spatial_biased_tile(p, blockIdx.x, blockIdx.y);
+    spatial_biased_tile<R, MIS>(p, blockIdx.x, blockIdx.y);
 }
 
 // ---------------------------------------------------------------- unbiased spatial (unbiasedReuse.glsl:50-185)
@@ -419,17 +502,20 @@ __global__ void __launch_bounds__(128) k_spatial_biased(const SpatialParams p) {
 //      visibility segment goes to the block's ray pool (:132-166);
 //   2. the block traces its pool;
 //   3. the normalisation count and the final W (:168-182).
-// Shared memory: ray pool [128*(K+1)], sample position per pixel [128],
-// neighbour index and M [K][128], not-counted flags [(K+1)][128], stacks.
-// The merged reservoir is parked in `out` between steps 1 and 3.
+// Shared memory (R samples per reservoir): ray pool [128*(K+1)*R], light
+// position per sample and pixel [R][128], neighbour index [K][128], neighbour
+// M [K][128] (with MIS: neighbour sumPHat [R][K][128]), not-counted flags
+// [R][(K+1)][128], stacks.  The merged reservoir is parked in `out` between
+// steps 1 and 3.
 constexpr int kMaxNeighbors = 16;
 
-__host__ __device__ inline size_t unbiased_smem_bytes(int K, int depth) {
-    const size_t slots = (size_t)K + 1;
-    size_t b = 128 * slots * sizeof(rgpool::Ray);
-    b += 128 * sizeof(float4);
-    b += 2 * 128 * (size_t)(K > 0 ? K : 1) * sizeof(uint32_t);
-    b += (128 * slots + 15) & ~(size_t)15;
+__host__ __device__ inline size_t unbiased_smem_bytes(int K, int depth, int R = 1, bool mis = false) {
+    const size_t slots = (size_t)K + 1, kp = (size_t)(K > 0 ? K : 1);
+    size_t b = 128 * slots * (size_t)R * sizeof(rgpool::Ray);
+    b += 128 * (size_t)R * sizeof(float4);
+    b += 128 * kp * sizeof(uint32_t);
+    b += 128 * kp * (mis ? (size_t)R : 1) * sizeof(uint32_t);
+    b += (128 * slots * (size_t)R + 15) & ~(size_t)15;
     b += 128 * (size_t)depth * sizeof(int);
     return b;
 }
@@ -439,17 +525,18 @@ __host__ __device__ inline size_t unbiased_smem_bytes(int K, int depth) {
 #endif
 // One TW x (128/TW) pixel tile; the tile shape changes which pixels share a
 // ray pool, never a result.
-template <int TW>
+template <int TW, int R, bool MIS>
 __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, int bx, int by) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int K = p.num_neighbors;
-    const int slots = K + 1;
+    const int slots = K + 1, kp = K > 0 ? K : 1;
     rgpool::Ray *pool = reinterpret_cast<rgpool::Ray *>(smem);
-    float4 *endp = reinterpret_cast<float4 *>(pool + 128 * slots);              // [128]
-    uint32_t *nidx = reinterpret_cast<uint32_t *>(endp + 128);                   // [K][128]
-    uint32_t *nm = nidx + 128 * (K > 0 ? K : 1);                                  // [K][128]
-    uint8_t *flag = reinterpret_cast<uint8_t *>(nm + 128 * (K > 0 ? K : 1));      // [slots][128]
-    int *stack = reinterpret_cast<int *>(flag + ((128 * slots + 15) & ~15));
+    float4 *endp = reinterpret_cast<float4 *>(pool + 128 * slots * R);             // [R][128]
+    uint32_t *nidx = reinterpret_cast<uint32_t *>(endp + 128 * R);                  // [K][128]
+    uint32_t *nm = nidx + 128 * kp;                                                 // [K][128]
+    float *nsp = reinterpret_cast<float *>(nm);                                     // MIS: [R][K][128]
+    uint8_t *flag = reinterpret_cast<uint8_t *>(nm + 128 * kp * (MIS ? R : 1));     // [R][K+1][128]
+    int *stack = reinterpret_cast<int *>(flag + ((128 * slots * R + 15) & ~15));
     __shared__ int s_count, s_next;
     const int tid = threadIdx.x + threadIdx.y * 32;
     if (tid == 0) { s_count = 0; s_next = 0; }
@@ -461,8 +548,14 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
     const bool valid = x < W && y < H;
     const bool vis = (p.u.flags & RG_FLAG_VISIBILITY_REUSE) != 0;
     const size_t i = valid ? (size_t)y * (size_t)W + (size_t)x : 0;
-    f3 wpos = mk(0.f, 0.f, 0.f), lpos = wpos;
+    f3 wpos = mk(0.f, 0.f, 0.f);
+    f3 lpos[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) lpos[q] = wpos;
     uint32_t orig_m = 0;
+    float orig_sp[MIS ? R : 1];
+#pragma unroll
+    for (int q = 0; q < (MIS ? R : 1); ++q) orig_sp[q] = 0.0f;
     if (valid) {
         Texel t;
         load_texel(p.g, i, t);
@@ -470,8 +563,12 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
         const float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
         const f3 cam = mk(p.u.camera_pos[0], p.u.camera_pos[1], p.u.camera_pos[2]);
         const f3 wo = view_dir(cam, t.wpos);
-        Res r = load_res(p.in, i);
+        ResV<R, MIS> r = load_resv<R, MIS>(p.in, i);
         orig_m = r.m;
+        if (MIS) {
+#pragma unroll
+            for (int q = 0; q < R; ++q) orig_sp[q] = r.sum_phat[q];
+        }
         Pcg rng = pcg_seed((uint64_t)(p.u.frame * 17u + (uint32_t)p.iter),
                            (uint64_t)((uint32_t)y * 10007u + (uint32_t)x));
         for (int k = 0; k < K; ++k) {
@@ -482,66 +579,104 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
             const int nx = iclamp(x + (int)roundf(cs * radius), 0, (int)(p.u.screen_size[0] - 1u));
             const int ny = iclamp(y + (int)roundf(sn * radius), 0, (int)(p.u.screen_size[1] - 1u));
             const size_t ni = (size_t)ny * (size_t)W + (size_t)nx;
-            const Res rr = load_res(p.in, ni);
+            const ResV<R, MIS> rr = load_resv<R, MIS>(p.in, ni);
             nidx[k * 128 + tid] = (uint32_t)ni;
-            nm[k * 128 + tid] = rr.m;
+            if (MIS) {
+#pragma unroll
+                for (int q = 0; q < R; ++q) nsp[(q * kp + k) * 128 + tid] = rr.sum_phat[q];
+            } else {
+                nm[k * 128 + tid] = rr.m;
+            }
             r.m += rr.m;
-            const float ph = eval_phat_wo(t.wpos, xyz(rr.pos_lum), wo, t.normal, xyz(rr.nrm), rr.nrm.w > 0.5f,
-                                          albedo_lum, rr.pos_lum.w, t.roughness, t.metallic);
-            const float weight = ph * rr.w * (float)rr.m;
-            if (weight > 0.0f) update_res(r, weight, rr.pos_lum, rr.nrm, rr.idx, ph, rr.w, rng);
+#pragma unroll
+            for (int q = 0; q < R; ++q) {
+                const float ph = eval_phat_wo(t.wpos, xyz(rr.pos_lum[q]), wo, t.normal, xyz(rr.nrm[q]),
+                                              rr.nrm[q].w > 0.5f, albedo_lum, rr.pos_lum[q].w, t.roughness,
+                                              t.metallic);
+                const float weight = ph * rr.w[q] * (float)rr.m;
+                if (weight > 0.0f)
+                    update_at(r, q, weight, rr.pos_lum[q], rr.nrm[q], rr.idx[q], ph, rr.w[q],
+                              MIS ? rr.sum_phat[q] : 0.0f, rng);
+            }
         }
-        lpos = xyz(r.pos_lum);
-        store_res(p.out, i, r);
+#pragma unroll
+        for (int q = 0; q < R; ++q) lpos[q] = xyz(r.pos_lum[q]);
+        store_resv(p.out, i, r);
     }
-    endp[tid] = make_float4(lpos.x, lpos.y, lpos.z, 0.0f);
-    for (int k = 0; k < K; ++k) {
-        bool want = false, excluded = true;
-        f3 nw = mk(0.f, 0.f, 0.f);
-        if (valid) {
-            const uint32_t ni = nidx[k * 128 + tid];
-            nw = load_wpos(p.g, ni);
-            const f3 nn = load_normal(p.g, ni);
-            excluded = dot(lpos - nw, nn) < 0.0f;
-            want = !excluded && vis;
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+        endp[q * 128 + tid] = make_float4(lpos[q].x, lpos[q].y, lpos[q].z, 0.0f);
+        for (int k = 0; k < K; ++k) {
+            bool want = false, excluded = true;
+            f3 nw = mk(0.f, 0.f, 0.f);
+            if (valid) {
+                const uint32_t ni = nidx[k * 128 + tid];
+                nw = load_wpos(p.g, ni);
+                const f3 nn = load_normal(p.g, ni);
+                excluded = dot(lpos[q] - nw, nn) < 0.0f;
+                want = !excluded && vis;
+            }
+            const int owner = (q * slots + k) * 128 + tid;
+            flag[owner] = excluded ? 1 : 0;
+            const int slot = rgpool::append_slot(&s_count, want);
+            if (want) rgpool::put_ray(pool, slot, nw, owner);
         }
-        flag[k * 128 + tid] = excluded ? 1 : 0;
-        const int slot = rgpool::append_slot(&s_count, want);
-        if (want) rgpool::put_ray(pool, slot, nw, k * 128 + tid);
-    }
-    {
-        const bool want = valid && vis;
-        flag[K * 128 + tid] = 0;
-        const int slot = rgpool::append_slot(&s_count, want);
-        if (want) rgpool::put_ray(pool, slot, wpos, K * 128 + tid);
+        {
+            const bool want = valid && vis;
+            const int owner = (q * slots + K) * 128 + tid;
+            flag[owner] = 0;
+            const int slot = rgpool::append_slot(&s_count, want);
+            if (want) rgpool::put_ray(pool, slot, wpos, owner);
+        }
     }
     __syncthreads();
     rgpool::TraceStats ts;
     rgpool::trace_pool(
         s, pool, s_count, &s_next, stack, s.depth, ts,
-        [&](int owner) { const float4 e = endp[owner & 127]; return mk(e.x, e.y, e.z); },
+        [&](int owner) {
+            const float4 e = endp[(owner / (slots * 128)) * 128 + (owner & 127)];
+            return mk(e.x, e.y, e.z);
+        },
         [&](int owner, bool hit) { if (hit) flag[owner] = 1; });
     __syncthreads();
     if (valid) {
-        uint32_t ns = orig_m;
-        for (int k = 0; k < K; ++k)
-            if (!flag[k * 128 + tid]) ns += nm[k * 128 + tid];
-        if (vis && flag[K * 128 + tid]) ns = 0;
-        Res r = load_res(p.out, i);
-        if (ns > 0) {
-            r.w = r.sum_w / ((float)ns * r.p_hat);
-        } else {
-            r.w = 0.0f;
-            r.sum_w = 0.0f;
+        ResV<R, MIS> r = load_resv<R, MIS>(p.out, i);
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            const uint8_t *fq = flag + q * slots * 128;
+            if (MIS) {
+                float sp = orig_sp[q];
+                for (int k = 0; k < K; ++k)
+                    if (!fq[k * 128 + tid]) sp += nsp[(q * kp + k) * 128 + tid];
+                if (vis && fq[K * 128 + tid]) sp = 0.0f;
+                if (sp > 0.0f) {
+                    r.w[q] = r.sum_w[q] * r.p_hat[q] / (sp * r.p_hat[q]);
+                } else {
+                    r.w[q] = 0.0f;
+                    r.sum_w[q] = 0.0f;
+                    r.sum_phat[q] = 0.0f;
+                }
+            } else {
+                uint32_t ns = orig_m;
+                for (int k = 0; k < K; ++k)
+                    if (!fq[k * 128 + tid]) ns += nm[k * 128 + tid];
+                if (vis && fq[K * 128 + tid]) ns = 0;
+                if (ns > 0) {
+                    r.w[q] = r.sum_w[q] / ((float)ns * r.p_hat[q]);
+                } else {
+                    r.w[q] = 0.0f;
+                    r.sum_w[q] = 0.0f;
+                }
+            }
         }
-        store_res(p.out, i, r);
+        store_resv(p.out, i, r);
     }
     count_block_rays(s, tid == 0 ? s_count : 0, ts);
 }
 
-template <int TW>
+template <int TW, int R, bool MIS>
 __global__ void __launch_bounds__(128, RG_UNBIASED_MIN_BLOCKS) k_spatial_unbiased(const SpatialParams p) {
-    spatial_unbiased_tile<TW>(p, blockIdx.x, blockIdx.y);
+    spatial_unbiased_tile<TW, R, MIS>(p, blockIdx.x, blockIdx.y);
 }
 
 // ---------------------------------------------------------------- shading (lighting.frag:43-71,103)
@@ -554,6 +689,7 @@ struct ShadeParams {
 };
 
 // One 32 x 4 pixel tile.
+template <int R, bool MIS>
 __device__ __forceinline__ void shade_tile(const ShadeParams &p, int bx, int by) {
     const int x = bx * 32 + threadIdx.x;
     const int y = by * 4 + threadIdx.y;
@@ -562,23 +698,27 @@ __device__ __forceinline__ void shade_tile(const ShadeParams &p, int bx, int by)
     const size_t i = (size_t)y * (size_t)W + (size_t)x;
     Texel t;
     load_texel(p.g, i, t);
-    const Res r = load_res(p.res, i);
-    f3 emission = mk(0.f, 0.f, 0.f);
-    if (r.idx < 0) {
-        const int k = -1 - r.idx;
-        if (k < p.s.n_tri_lights) {
-            const rg_tri_light &L = p.s.tri_lights[k];
-            emission = mk(L.emission_luminance[0], L.emission_luminance[1], L.emission_luminance[2]);
-        }
-    } else if (r.idx < p.s.n_point_lights) {
-        const float4 c = __ldg(p.s.pl_color + r.idx);
-        emission = mk(c.x, c.y, c.z);
-    }
+    const ResV<R, MIS> r = load_resv<R, MIS>(p.res, i);
     const f3 cam = mk(p.u.camera_pos[0], p.u.camera_pos[1], p.u.camera_pos[2]);
-    const f3 ph = eval_phat_full(t.wpos, xyz(r.pos_lum), cam, t.normal, xyz(r.nrm), r.nrm.w > 0.5f, t.albedo, emission,
-                                 t.roughness, t.metallic);
-    f3 col = mk(0.0f + ph.x * r.w, 0.0f + ph.y * r.w, 0.0f + ph.z * r.w);
-    col = divs(col, 1.0f);  // RESERVOIR_SIZE
+    f3 col = mk(0.0f, 0.0f, 0.0f);
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+        f3 emission = mk(0.f, 0.f, 0.f);
+        if (r.idx[q] < 0) {
+            const int k = -1 - r.idx[q];
+            if (k < p.s.n_tri_lights) {
+                const rg_tri_light &L = p.s.tri_lights[k];
+                emission = mk(L.emission_luminance[0], L.emission_luminance[1], L.emission_luminance[2]);
+            }
+        } else if (r.idx[q] < p.s.n_point_lights) {
+            const float4 c = __ldg(p.s.pl_color + r.idx[q]);
+            emission = mk(c.x, c.y, c.z);
+        }
+        const f3 ph = eval_phat_full(t.wpos, xyz(r.pos_lum[q]), cam, t.normal, xyz(r.nrm[q]), r.nrm[q].w > 0.5f,
+                                     t.albedo, emission, t.roughness, t.metallic);
+        col = mk(col.x + ph.x * r.w[q], col.y + ph.y * r.w[q], col.z + ph.z * r.w[q]);
+    }
+    col = divs(col, (float)R);  // RESERVOIR_SIZE
     if (t.albedo_a > 0.5f) col = t.albedo;
     if (p.u.gamma != 1.0f) {
         const float ig = 1.0f / p.u.gamma;
@@ -587,7 +727,8 @@ __device__ __forceinline__ void shade_tile(const ShadeParams &p, int bx, int by)
     p.out[i] = make_float4(col.x, col.y, col.z, 1.0f);
 }
 
-__global__ void __launch_bounds__(128) k_shade(const ShadeParams p) { shade_tile(p, blockIdx.x, blockIdx.y); }
+template <int R, bool MIS>
+__global__ void __launch_bounds__(128) k_shade(const ShadeParams p) { shade_tile<R, MIS>(p, blockIdx.x, blockIdx.y); }
 
 // ---------------------------------------------------------------- visibility batch (testVisibility)
 // 128 threads take a chunk of 512 segments into the pool and trace it.
@@ -649,18 +790,21 @@ __device__ __forceinline__ void for_each_view_tile(const P *views, const ViewTil
 template <int PPT>
 __global__ void __launch_bounds__(128, RG_RIS_MIN_BLOCKS) k_initial_temporal_views(const InitialParams *views,
                                                                                      const ViewTiles vt) {
-    for_each_view_tile(views, vt, [](const InitialParams &p, int bx, int by) { initial_temporal_tile<PPT>(p, bx, by); });
+    for_each_view_tile(views, vt,
+                       [](const InitialParams &p, int bx, int by) { initial_temporal_tile<PPT, 1, false>(p, bx, by); });
 }
 template <int TW>
 __global__ void __launch_bounds__(128, RG_UNBIASED_MIN_BLOCKS) k_spatial_unbiased_views(const SpatialParams *views,
                                                                                           const ViewTiles vt) {
-    for_each_view_tile(views, vt, [](const SpatialParams &p, int bx, int by) { spatial_unbiased_tile<TW>(p, bx, by); });
+    for_each_view_tile(views, vt,
+                       [](const SpatialParams &p, int bx, int by) { spatial_unbiased_tile<TW, 1, false>(p, bx, by); });
 }
 __global__ void __launch_bounds__(128) k_spatial_biased_views(const SpatialParams *views, const ViewTiles vt) {
-    for_each_view_tile(views, vt, [](const SpatialParams &p, int bx, int by) { spatial_biased_tile(p, bx, by); });
+    for_each_view_tile(views, vt,
+                       [](const SpatialParams &p, int bx, int by) { spatial_biased_tile<1, false>(p, bx, by); });
 }
 __global__ void __launch_bounds__(128) k_shade_views(const ShadeParams *views, const ViewTiles vt) {
-    for_each_view_tile(views, vt, [](const ShadeParams &p, int bx, int by) { shade_tile(p, bx, by); });
+    for_each_view_tile(views, vt, [](const ShadeParams &p, int bx, int by) { shade_tile<1, false>(p, bx, by); });
 }
 
 // frame index of every view for the next run: start + (number of runs so far)
@@ -676,9 +820,16 @@ __global__ void k_advance_frames(InitialParams *ip, SpatialParams *sp, int n_vie
 }
 __global__ void k_count_run(uint32_t *runs) { *runs += 1u; }
 
-size_t ris_smem_bytes(int ppt, int depth) {
-    return (size_t)128 * ppt * (sizeof(rgpool::Ray) + sizeof(float4) + 1) +
+size_t ris_smem_bytes(int ppt, int depth, int samples = 1) {
+    return (size_t)128 * ppt * samples * (sizeof(rgpool::Ray) + sizeof(float4) + 1) +
            128 * (size_t)(RG_STACK_LOCAL ? 0 : depth) * sizeof(int);
+}
+
+// Calls f.template operator()<R, MIS>() for the scene's reservoir format.
+template <typename F>
+cudaError_t with_format(const DevScene &s, F &&f) {
+    if (s.res_samples == 2) return s.res_mis ? f(FormatTag<2, true>{}) : f(FormatTag<2, false>{});
+    return s.res_mis ? f(FormatTag<1, true>{}) : f(FormatTag<1, false>{});
 }
 
 dim3 pixel_grid(int w, int h, dim3 block) {
@@ -711,14 +862,19 @@ cudaError_t launch_initial_temporal(const DevScene &s, const GBufView &cur, cons
     p.prev_res = prev_res;
     p.out = out;
     p.u = u;
-    const dim3 block(32, 4);
-    const dim3 grid((u.screen_size[0] + 31u) / 32u, (u.screen_size[1] + 4u * kRisPpt - 1u) / (4u * kRisPpt));
-    const size_t smem = ris_smem_bytes(kRisPpt, s.depth);
-    cudaError_t e = cudaFuncSetAttribute(k_initial_temporal<kRisPpt>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    k_initial_temporal<kRisPpt><<<grid, block, smem, st>>>(p);
-    return cudaGetLastError();
+    return with_format(s, [&](auto tag) {
+        constexpr int R = decltype(tag)::R;
+        constexpr bool MIS = decltype(tag)::MIS;
+        constexpr int ppt = R == 1 ? kRisPpt : 2;  // pool size per block kept near the single-sample one
+        const dim3 block(32, 4);
+        const dim3 grid((u.screen_size[0] + 31u) / 32u, (u.screen_size[1] + 4u * ppt - 1u) / (4u * ppt));
+        const size_t smem = ris_smem_bytes(ppt, s.depth, R);
+        cudaError_t e = cudaFuncSetAttribute(k_initial_temporal<ppt, R, MIS>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_initial_temporal<ppt, R, MIS><<<grid, block, smem, st>>>(p);
+        return cudaGetLastError();
+    });
 }
 
 cudaError_t launch_spatial_biased(const DevScene &s, const GBufView &g, const rg_reservoir *in, rg_reservoir *out,
@@ -732,9 +888,12 @@ cudaError_t launch_spatial_biased(const DevScene &s, const GBufView &g, const rg
     p.iter = iter;
     p.num_neighbors = 0;
     p.cos_thr = cos_cw(u.spatial_normal_threshold * kDeg2Rad);
-    const dim3 block(32, 4);
-    k_spatial_biased<<<pixel_grid((int)u.screen_size[0], (int)u.screen_size[1], block), block, 0, st>>>(p);
-    return cudaGetLastError();
+    return with_format(s, [&](auto tag) {
+        const dim3 block(32, 4);
+        k_spatial_biased<decltype(tag)::R, decltype(tag)::MIS>
+            <<<pixel_grid((int)u.screen_size[0], (int)u.screen_size[1], block), block, 0, st>>>(p);
+        return cudaGetLastError();
+    });
 }
 
 cudaError_t launch_spatial_unbiased(const DevScene &s, const GBufView &g, const rg_reservoir *in, rg_reservoir *out,
@@ -749,17 +908,23 @@ cudaError_t launch_spatial_unbiased(const DevScene &s, const GBufView &g, const 
     p.iter = pass_index;
     p.num_neighbors = num_neighbors;
     p.cos_thr = 0.0f;
-    const dim3 block(32, 4);
-    const size_t smem = unbiased_smem_bytes(num_neighbors, RG_STACK_LOCAL ? 0 : s.depth);
-    cudaError_t e = cudaFuncSetAttribute(k_spatial_unbiased<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    if (RG_SMEM_CARVEOUT >= 0) {
-        e = cudaFuncSetAttribute(k_spatial_unbiased<32>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 RG_SMEM_CARVEOUT);
+    return with_format(s, [&](auto tag) {
+        constexpr int R = decltype(tag)::R;
+        constexpr bool MIS = decltype(tag)::MIS;
+        const dim3 block(32, 4);
+        const size_t smem = unbiased_smem_bytes(num_neighbors, RG_STACK_LOCAL ? 0 : s.depth, R, MIS);
+        cudaError_t e = cudaFuncSetAttribute(k_spatial_unbiased<32, R, MIS>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-    }
-    k_spatial_unbiased<32><<<pixel_grid((int)u.screen_size[0], (int)u.screen_size[1], block), block, smem, st>>>(p);
-    return cudaGetLastError();
+        if (RG_SMEM_CARVEOUT >= 0) {
+            e = cudaFuncSetAttribute(k_spatial_unbiased<32, R, MIS>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     RG_SMEM_CARVEOUT);
+            if (e != cudaSuccess) return e;
+        }
+        k_spatial_unbiased<32, R, MIS>
+            <<<pixel_grid((int)u.screen_size[0], (int)u.screen_size[1], block), block, smem, st>>>(p);
+        return cudaGetLastError();
+    });
 }
 
 cudaError_t launch_shade(const DevScene &s, const GBufView &g, const rg_reservoir *res, const rg_lighting_uniforms &u,
@@ -770,9 +935,12 @@ cudaError_t launch_shade(const DevScene &s, const GBufView &g, const rg_reservoi
     p.res = res;
     p.out = out;
     p.u = u;
-    const dim3 block(32, 4);
-    k_shade<<<pixel_grid((int)u.buffer_size[0], (int)u.buffer_size[1], block), block, 0, st>>>(p);
-    return cudaGetLastError();
+    return with_format(s, [&](auto tag) {
+        const dim3 block(32, 4);
+        k_shade<decltype(tag)::R, decltype(tag)::MIS>
+            <<<pixel_grid((int)u.buffer_size[0], (int)u.buffer_size[1], block), block, 0, st>>>(p);
+        return cudaGetLastError();
+    });
 }
 
 cudaError_t launch_visibility_batch(const DevScene &s, const float4 *p1, const float4 *p2, uint8_t *out, int n,

@@ -65,6 +65,9 @@ extern "C" int rg_spatial_unbiased_chain_noalloc(rg_context *ctx, const rg_gbuff
     if (rc) return rc;
     if (!u || !gbuf || !in || !out)
         return rg_internal_fail(RG_ERR_INVALID_ARGUMENT, "rg_spatial_unbiased_chain_noalloc: null argument");
+    if (scene->res_samples != 1 || scene->res_mis)
+        return rg_internal_fail(RG_ERR_UNSUPPORTED,
+                                "rg_spatial_unbiased_chain_noalloc: its scratch holds the default reservoir format");
     const size_t w = u->screen_size[0], h = u->screen_size[1];
     if (w == 0 || h == 0 || (uint32_t)gbuf->width != w || (uint32_t)gbuf->height != h)
         return rg_internal_fail(RG_ERR_INVALID_ARGUMENT,

@@ -474,8 +474,11 @@ int rg_proposal_gradients(rg_context *ctx, const rg_gbuffer *g, const float cam[
 int rg_proposal_train(rg_context *ctx, const rg_gbuffer *g, const rg_restir_uniforms *u, const rg_reservoir *res,
                       void *stream) {
     ProposalState *ps = nullptr;
-    int rc = get_state(ctx, &ps);
+    const DevScene *scene = nullptr;
+    int rc = get_state(ctx, &ps, &scene);
     if (rc) return rc;
+    if (scene->res_samples != 1 || scene->res_mis)
+        return pfail(RG_ERR_UNSUPPORTED, "training reads the default reservoir format");
     if (!u || !res || ((uintptr_t)res & 15u)) return pfail(RG_ERR_INVALID_ARGUMENT, "bad arguments");
     if ((rc = check_gbuf(g))) return rc;
     if ((uint32_t)g->width != u->screen_size[0] || (uint32_t)g->height != u->screen_size[1])

@@ -49,6 +49,8 @@ struct DevScene {
     int32_t n_materials;
     unsigned long long *counters; // [0] rays traced, [1] traversal errors, [2] node visits, [3] triangle tests
     int *mma_timeouts;            // tensor-core kernels whose bounded mbarrier wait ran out
+    int32_t res_samples;          // reservoir format: RESERVOIR_SIZE (1 or 2)
+    int32_t res_mis;              // and UNBIASED_MIS (0 or 1)
 };
 
 struct GBufView {

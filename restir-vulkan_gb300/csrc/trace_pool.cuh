@@ -152,7 +152,6 @@ template <typename Endpoint, typename Emit>
 __device__ void trace_pool(const DevScene &s, const Ray *pool, int n, int *next, int *stack, int depth,
                            TraceStats &ts, Endpoint endpoint, Emit emit) {
     constexpr unsigned kFull = 0xffffffffu;
-    const int tid = threadIdx.x + threadIdx.y * blockDim.x;
 #if RG_STACK_LOCAL
     int local_stack[RG_MAX_TREE_DEPTH + 1];
     int *my_stack = local_stack;
@@ -160,7 +159,7 @@ __device__ void trace_pool(const DevScene &s, const Ray *pool, int n, int *next,
     (void)stack;
 #else
     const int nthreads = blockDim.x * blockDim.y;
-    int *my_stack = stack + tid;
+    int *my_stack = stack + threadIdx.x + threadIdx.y * blockDim.x;
 #endif
     int cur = -1;          // pool index of this lane's segment, -1: none
     bool retired = false;  // the pool has no segment left for this lane

@@ -24,6 +24,7 @@ RG_FLAG_TEMPORAL_REUSE = 2
 RG_FLAG_FINAL_RIS_WEIGHT = 256
 RG_FLAG_LEARNED_PROPOSAL = 512
 RG_FLAG_LEARNED_TRAIN = 1024
+RG_FLAG_MIS_SWAP_FIX = 2048
 RG_MAX_TREE_DEPTH = 63
 
 F4 = C.c_float * 4
@@ -158,6 +159,8 @@ _SIGNATURES = {
                                C.c_int32, C.c_float, C.c_int32, C.c_void_p]),
     "rg_spatial_unbiased_chain_noalloc": (C.c_int, [C.c_void_p, C.POINTER(GBuffer), C.c_void_p, C.c_void_p,
                                                     C.POINTER(RestirUniforms), C.c_int32, C.c_int32, C.c_void_p]),
+    "rg_set_reservoir_format": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "rg_reservoir_bytes": (C.c_int, [C.c_void_p]),
     "rg_build_bvh_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
                                       C.POINTER(C.c_int32), C.c_void_p]),
     "rg_batch_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(FrameParams),

@@ -86,9 +86,10 @@ class DeviceGBuffer:
                                p["material"].data_ptr(), p["world_pos"].data_ptr(), p["depth"].data_ptr())
 
 
-def reservoirs(n: int, device="cuda"):
-    """Zero-filled device reservoir buffer (64 bytes per pixel)."""
-    return _torch().zeros((n, 16), dtype=_torch().int32, device=device)
+def reservoirs(n: int, device="cuda", nbytes: int = 64):
+    """Zero-filled device reservoir buffer (nbytes per pixel: 64 for the
+    default format, Context.reservoir_bytes() for the others)."""
+    return _torch().zeros((n, nbytes // 4), dtype=_torch().int32, device=device)
 
 
 class _DeviceSpan:
@@ -183,6 +184,12 @@ class Context:
         check(lib().rg_render_frame_host(self._h, w, h, _lib.ptr(g["albedo"]), _lib.ptr(g["normal"]),
                                          _lib.ptr(g["material"]), _lib.ptr(g["world_pos"]), _lib.ptr(g["depth"]),
                                          C.byref(params), _lib.ptr(out_rgba), _stream_handle(stream)))
+
+    def set_reservoir_format(self, samples: int, unbiased_mis: int):
+        check(lib().rg_set_reservoir_format(self._h, samples, unbiased_mis))
+
+    def reservoir_bytes(self) -> int:
+        return check(lib().rg_reservoir_bytes(self._h))
 
     def stats(self, reset: bool = False) -> _lib.Stats:
         s = _lib.Stats()
