@@ -498,37 +498,30 @@ def learned_section(dev: int, iters: int = 10, width: int = 1920, height: int = 
 
 
 # ------------------------------------------------------------------ batched views (config 5 workload)
-def batched_section(dev: int, steps: int = 5, n_views: int = 64) -> dict:
-    """Config 5: n_views views of config 2's scene, sizes log-uniform between
-    320x240 and 1920x1080, seeded poses; config 2's pass sequence (RIS +
-    visibility + temporal, 2 unbiased spatial passes k=5, shading) for every
-    view with one persistent launch per pass, launch shapes from the
-    autotuner, replayed from CUDA graphs.  Per-view frame times of the same
-    views run one by one give the p50/p99."""
+def _batched_arm(ctx, vws, fp, samples, steps, learned, tuning=None):
+    """One proposal form of the batched views: autotuned (or given) launch
+    shapes, CUDA-graph replays timed with events, then the views one by one
+    for the per-view frame times.  The learned form's run includes the
+    proposal's inference over all views; one Adam step on one view (rotating)
+    follows each run and is timed separately."""
     import torch
 
-    from restir_gb300 import _lib, scenes
-    from restir_gb300.passes import Batch, Context, DeviceGBuffer, reservoirs
-    base, views = scenes.config5(n_views=n_views)
-    ctx = Context(dev)
-    ctx.upload_scene(base)
-    vws = []
-    for v in views:
-        gb = DeviceGBuffer(v.width, v.height)
-        ctx.trace_gbuffer(v.cameras[0], gb)
-        nv = v.width * v.height
-        u = v.uniforms(0)
-        u.flags |= _lib.RG_FLAG_TEMPORAL_REUSE
-        vws.append({"scene": v, "cur": gb, "prev": gb, "res0": reservoirs(nv), "res1": reservoirs(nv),
-                    "tmp": reservoirs(nv), "uniforms": u,
-                    "image": torch.zeros((v.height, v.width, 4), dtype=torch.float32, device="cuda")})
-    fp = base.frame_params(0)
-    pixels = sum(v.width * v.height for v in views)
-    samples = sum(v.width * v.height * (v.candidates + 1 + v.spatial_passes * v.neighbors) for v in views)
+    from restir_gb300 import _lib
+    from restir_gb300.passes import Batch
+    for vw in vws:
+        if learned:
+            vw["uniforms"].flags |= _lib.RG_FLAG_LEARNED_PROPOSAL
+        else:
+            vw["uniforms"].flags &= ~_lib.RG_FLAG_LEARNED_PROPOSAL
     b = Batch(ctx, vws, fp)
-    t0 = time.perf_counter()
-    tuning, tuned_ms = b.autotune(repeats=1)
-    tune_s = time.perf_counter() - t0
+    tune_s = 0.0
+    if tuning is None:
+        t0 = time.perf_counter()
+        tuning, _ = b.autotune(repeats=1)
+        tune_s = time.perf_counter() - t0
+    else:
+        b.set_tuning(tuning.ris_pixels_per_thread, tuning.spatial_tile_width, tuning.ctas_per_sm)
+        b.run(0)  # outside capture
     b.reset_frames()
     for vw in vws:
         for k in ("res0", "res1", "tmp"):
@@ -552,6 +545,19 @@ def batched_section(dev: int, steps: int = 5, n_views: int = 64) -> dict:
     e1.record(cur)
     torch.cuda.synchronize()
     batched_ms = e0.elapsed_time(e1) / steps
+    train_ms = None
+    if learned:
+        tt = []
+        for k in range(steps):
+            vw = vws[k % len(vws)]
+            parity = (3 + k) & 1
+            a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(cur)
+            ctx.proposal_train(vw["cur"], vw["uniforms"], vw[f"res{parity}"].data_ptr(), cur)
+            z.record(cur)
+            torch.cuda.synchronize()
+            tt.append(a.elapsed_time(z))
+        train_ms = statistics.median(tt)
     # the same views one by one (single-view launches), per-view frame times
     per_view = []
     for vw in vws:
@@ -564,6 +570,8 @@ def batched_section(dev: int, steps: int = 5, n_views: int = 64) -> dict:
             uu.frame = u.frame + 100 + k
             a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(cur)
+            if learned:
+                ctx.proposal_infer(vw["cur"], uu, cur)
             ctx.initial_temporal(vw["cur"], vw["prev"], vw["res1"], vw["res0"], uu, cur)
             ctx.spatial_unbiased(vw["cur"], vw["res0"], vw["tmp"], uu, v.neighbors, 0, cur)
             ctx.spatial_unbiased(vw["cur"], vw["tmp"], vw["res0"], uu, v.neighbors, 1, cur)
@@ -573,25 +581,69 @@ def batched_section(dev: int, steps: int = 5, n_views: int = 64) -> dict:
             if k:
                 times.append(a.elapsed_time(z))
         per_view.append(statistics.median(times))
-    stats = ctx.stats()
     b.close()
-    ctx.close()
     pv = np.array(per_view)
-    return {"workload": f"config 5: {n_views} views of config 2's scene ({len(base.triangles):,} triangles, "
-                        f"{len(base.point_lights):,} point lights), sizes log-uniform 320x240..1920x1080, "
-                        f"{pixels:,} pixels; RIS + visibility + temporal, 2 unbiased spatial passes k=5, shading",
-            "batched": {"ms_per_frame": round(batched_ms, 3), "samples_per_s": samples / (batched_ms / 1000.0),
-                        "launches_per_frame": 2 + 2 + 1 + 2, "cuda_graph": True,
-                        "tuning": {"ris_pixels_per_thread": tuning.ris_pixels_per_thread,
-                                   "spatial_tile_width": tuning.spatial_tile_width,
-                                   "ctas_per_sm": tuning.ctas_per_sm},
-                        "autotune_seconds": round(tune_s, 2),
-                        "note": "all views advance together: each view's frame completes within ms_per_frame"},
-            "one_by_one": {"ms_per_frame_all_views": round(float(pv.sum()), 3),
-                           "samples_per_s": samples / (pv.sum() / 1000.0),
-                           "per_view_ms_p50": round(float(np.percentile(pv, 50)), 3),
-                           "per_view_ms_p99": round(float(np.percentile(pv, 99)), 3)},
-            "samples_per_frame": samples, "traversal_errors": int(stats.traversal_errors)}
+    out = {"batched": {"ms_per_frame": round(batched_ms, 3), "samples_per_s": samples / (batched_ms / 1000.0),
+                       "launches_per_frame": 2 + (2 if learned else 0) + 2 + 1 + 2, "cuda_graph": True,
+                       "tuning": {"ris_pixels_per_thread": tuning.ris_pixels_per_thread,
+                                  "spatial_tile_width": tuning.spatial_tile_width,
+                                  "ctas_per_sm": tuning.ctas_per_sm},
+                       "autotune_seconds": round(tune_s, 2),
+                       "note": "all views advance together: each view's frame completes within ms_per_frame"},
+           "one_by_one": {"ms_per_frame_all_views": round(float(pv.sum()), 3),
+                          "samples_per_s": samples / (pv.sum() / 1000.0),
+                          "per_view_ms_p50": round(float(np.percentile(pv, 50)), 3),
+                          "per_view_ms_p99": round(float(np.percentile(pv, 99)), 3)}}
+    if learned:
+        out["batched"]["tuning_from"] = "the plain form's autotuned shapes (the inference launches are not tuned)"
+        out["train_ms_per_adam_step"] = round(train_ms, 3)
+    return out, tuning
+
+
+def batched_section(dev: int, steps: int = 5, n_views: int = 64, clusters: int = 4096) -> dict:
+    """Config 5: n_views views of config 2's scene, sizes log-uniform between
+    320x240 and 1920x1080, seeded poses; config 2's pass sequence (RIS +
+    visibility + temporal, 2 unbiased spatial passes k=5, shading) for every
+    view with one persistent launch per pass, launch shapes from the
+    autotuner, replayed from CUDA graphs; with the plain alias-table proposal
+    and with the learned proposal (config 4's network over 4096 clusters,
+    inferred over all views by one launch per inference pass).  Per-view frame
+    times of the same views run one by one give the p50/p99."""
+    import torch
+
+    from restir_gb300 import _lib, scenes
+    from restir_gb300.passes import Context, DeviceGBuffer, cluster_lights, reservoirs
+    base, views = scenes.config5(n_views=n_views)
+    ctx = Context(dev)
+    ctx.upload_scene(base)
+    vws = []
+    for v in views:
+        gb = DeviceGBuffer(v.width, v.height)
+        ctx.trace_gbuffer(v.cameras[0], gb)
+        nv = v.width * v.height
+        u = v.uniforms(0)
+        u.flags |= _lib.RG_FLAG_TEMPORAL_REUSE
+        vws.append({"scene": v, "cur": gb, "prev": gb, "res0": reservoirs(nv), "res1": reservoirs(nv),
+                    "tmp": reservoirs(nv), "uniforms": u,
+                    "image": torch.zeros((v.height, v.width, 4), dtype=torch.float32, device="cuda")})
+    fp = base.frame_params(0)
+    pixels = sum(v.width * v.height for v in views)
+    samples = sum(v.width * v.height * (v.candidates + 1 + v.spatial_passes * v.neighbors) for v in views)
+    plain, tuning = _batched_arm(ctx, vws, fp, samples, steps, learned=False)
+    co, _ = cluster_lights(base.point_lights, clusters, iterations=8, seed=4)
+    ctx.create_proposal(co, clusters, mix=0.9, batch=65_536, learning_rate=1e-2, seed=1)
+    learned, _ = _batched_arm(ctx, vws, fp, samples, steps, learned=True, tuning=tuning)
+    stats = ctx.stats()
+    ctx.close()
+    out = {"workload": f"config 5: {n_views} views of config 2's scene ({len(base.triangles):,} triangles, "
+                       f"{len(base.point_lights):,} point lights), sizes log-uniform 320x240..1920x1080, "
+                       f"{pixels:,} pixels; RIS + visibility + temporal, 2 unbiased spatial passes k=5, shading",
+           "samples_per_frame": samples, "traversal_errors": int(stats.traversal_errors),
+           "mma_timeouts": int(stats.mma_timeouts)}
+    out.update(plain)
+    out["learned"] = learned
+    out["learned"]["proposal"] = f"MLP 9-64-64-64-{clusters}, mix 0.9, inference over all {pixels:,} pixels per run"
+    return out
 
 
 # ------------------------------------------------------------------ reference arm

@@ -335,7 +335,16 @@ typedef struct rg_batch_tuning {
 
 typedef struct rg_batch rg_batch;
 /* params: unbiased, spatial_iterations, unbiased_neighbors and gamma as for
- * rg_render_frame (its uniforms are not used); tuning may be null. */
+ * rg_render_frame (its uniforms are not used); tuning may be null.
+ * RG_FLAG_LEARNED_PROPOSAL on the views (all or none; 1..32 candidates each)
+ * batches the context's learned proposal too: each run first infers it over
+ * the pixels of every view (one launch per inference pass) into the batch's
+ * own candidate buffer, so each view's results equal rg_proposal_infer
+ * followed by rg_render_frame's passes for that view.  The batch uses the
+ * proposal's weights as they are at each run (training between runs is
+ * fine); once the proposal is re-created, rg_batch_run fails and a captured
+ * graph of the batch must not be replayed.  Training stays a separate call
+ * (rg_proposal_train on a view's G-buffer and reservoirs). */
 int rg_batch_create(rg_context *ctx, const rg_view *views, int32_t n_views, const rg_frame_params *params,
                     const rg_batch_tuning *tuning, rg_batch **out);
 /* One frame of every view on `stream`. */

@@ -8,6 +8,12 @@
 // device, and launch RIS, the spatial passes and shading once each over all
 // views.  Nothing is copied from the host and nothing is allocated, so a run
 // can be captured into a CUDA graph once per parity and replayed.
+//
+// With the learned proposal (RG_FLAG_LEARNED_PROPOSAL on the views), a run
+// first infers the proposal over all views' pixels (the two k_mlp_fused
+// passes, each one launch over the concatenated pixels of every view) into
+// the batch's own candidate buffer, whose slice of a view its RIS records
+// point at.
 #include <cuda_runtime.h>
 #include <stdarg.h>
 #include <stdio.h>
@@ -63,6 +69,16 @@ struct rg_batch {
     uint32_t *start_frame = nullptr, *runs = nullptr;
     unsigned *counters = nullptr;  // 2 + spatial
     TileMap maps[3];               // RIS, spatial, shade (for the current tuning)
+    // learned proposal
+    bool learned = false;
+    uint64_t proposal_generation = 0;
+    mlp::ProposalDev pd{};
+    int *err = nullptr;            // the context's tensor-core timeout counter
+    int64_t rows = 0;              // pixels of all views
+    mlp::ViewRows *mlp_views = nullptr;
+    uint32_t *view_frame = nullptr;
+    float4 *stat = nullptr;
+    mlp::Candidate *cand = nullptr;
 
     void release_maps() {
         for (auto &m : maps) {
@@ -81,8 +97,15 @@ struct rg_batch {
         if (start_frame) cudaFree(start_frame);
         if (runs) cudaFree(runs);
         if (counters) cudaFree(counters);
-        start_frame = runs = nullptr;
+        if (mlp_views) cudaFree(mlp_views);
+        if (view_frame) cudaFree(view_frame);
+        if (stat) cudaFree(stat);
+        if (cand) cudaFree(cand);
+        start_frame = runs = view_frame = nullptr;
         counters = nullptr;
+        mlp_views = nullptr;
+        stat = nullptr;
+        cand = nullptr;
         release_maps();
     }
 };
@@ -131,8 +154,16 @@ int enqueue_run(rg_batch *b, int parity, cudaStream_t st) {
     const int nl = 2 + b->spatial;
     B_CUDA(cudaMemsetAsync(b->counters, 0, (size_t)nl * sizeof(unsigned), st), "rg_batch_run");
     B_CUDA(launch_advance_frames(b->initial[parity], b->spatial_p[parity], b->n, b->spatial, b->start_frame, b->runs,
-                                 st),
+                                 b->view_frame, st),
            "frame advance");
+    if (b->learned) {
+        int *err = b->err;
+        B_CUDA(mlp::forward_lse_views(b->pd, b->mlp_views, b->n, b->view_frame, (int)b->rows, b->stat, b->cand, err, st),
+               "proposal lse over views");
+        B_CUDA(mlp::forward_sample_views(b->pd, b->mlp_views, b->n, b->view_frame, (int)b->rows, b->stat, b->cand, err,
+                                         st),
+               "proposal sampling over views");
+    }
     ViewTiles vt{b->maps[0].view_start, b->maps[0].tiles_x, b->n, b->maps[0].total, b->counters};
     B_CUDA(launch_views_pass(0, b->tuning.ris_pixels_per_thread, b->unbiased, b->neighbors, b->depth, b->initial[parity],
                              vt, b->maps[0].grid, st),
@@ -182,8 +213,37 @@ int rg_batch_create(rg_context *ctx, const rg_view *views, int32_t n_views, cons
         if (!w.reservoirs[0] || !w.reservoirs[1] || !w.tmp || !w.rgba_out || ((uintptr_t)w.reservoirs[0] & 15u) ||
             ((uintptr_t)w.reservoirs[1] & 15u) || ((uintptr_t)w.tmp & 15u) || ((uintptr_t)w.rgba_out & 15u))
             return bfail(RG_ERR_INVALID_ARGUMENT, "view %d: null or misaligned buffer", v);
-        if (w.uniforms.flags & RG_FLAG_LEARNED_PROPOSAL)
-            return bfail(RG_ERR_UNSUPPORTED, "view %d: the learned proposal is not batched", v);
+        if (((w.uniforms.flags ^ views[0].uniforms.flags) & RG_FLAG_LEARNED_PROPOSAL) != 0)
+            return bfail(RG_ERR_INVALID_ARGUMENT, "view %d: RG_FLAG_LEARNED_PROPOSAL must be set on all views or none", v);
+        if ((w.uniforms.flags & RG_FLAG_LEARNED_PROPOSAL) &&
+            (w.uniforms.initial_light_sample_count < 1 || w.uniforms.initial_light_sample_count > (uint32_t)mlp::kCand))
+            return bfail(RG_ERR_INVALID_ARGUMENT, "view %d: the learned proposal draws 1..%d candidates per pixel", v,
+                         mlp::kCand);
+    }
+    const bool learned = (views[0].uniforms.flags & RG_FLAG_LEARNED_PROPOSAL) != 0;
+    ProposalState *ps = learned ? *rg_internal_proposal(ctx) : nullptr;
+    if (learned && !ps) return bfail(RG_ERR_INVALID_ARGUMENT, "RG_FLAG_LEARNED_PROPOSAL without a proposal");
+    std::vector<int64_t> first_row((size_t)n_views + 1, 0);
+    for (int v = 0; v < n_views; ++v)
+        first_row[(size_t)v + 1] = first_row[(size_t)v] + (int64_t)views[v].uniforms.screen_size[0] *
+                                                              (int64_t)views[v].uniforms.screen_size[1];
+    if (learned && first_row[(size_t)n_views] > 0x7fffffff)
+        return bfail(RG_ERR_INVALID_ARGUMENT, "the learned proposal batches at most 2^31 - 1 pixels");
+    mlp::LearnedRis lr{};
+    std::vector<mlp::ViewRows> vrows;
+    uint64_t generation = 0;
+    mlp::ProposalDev pd{};
+    if (learned) {
+        generation = proposal_batch_tables(ps, &pd, &lr);
+        vrows.resize((size_t)n_views);
+        for (int v = 0; v < n_views; ++v) {
+            const rg_view &w = views[v];
+            vrows[(size_t)v].g = make_view(&w.cur);
+            for (int d = 0; d < 3; ++d) vrows[(size_t)v].cam[d] = w.uniforms.camera_pos[d];
+            vrows[(size_t)v].first_row = (uint32_t)first_row[(size_t)v];
+            vrows[(size_t)v].n_cand = (int32_t)w.uniforms.initial_light_sample_count;
+        }
+        B_CUDA(mlp::prepare_views(), "proposal kernel attributes");
     }
     rg_batch *b = new rg_batch();
     b->ctx = ctx;
@@ -194,6 +254,24 @@ int rg_batch_create(rg_context *ctx, const rg_view *views, int32_t n_views, cons
     b->neighbors = fp->unbiased_neighbors;
     b->depth = s->depth;
     b->views.assign(views, views + n_views);
+    b->learned = learned;
+    b->proposal_generation = generation;
+    b->pd = pd;
+    b->err = s->mma_timeouts;
+    b->rows = first_row[(size_t)n_views];
+    if (learned) {
+        cudaError_t ea = cudaMalloc(&b->mlp_views, (size_t)n_views * sizeof(mlp::ViewRows));
+        if (ea == cudaSuccess)
+            ea = cudaMemcpy(b->mlp_views, vrows.data(), (size_t)n_views * sizeof(mlp::ViewRows), cudaMemcpyHostToDevice);
+        if (ea == cudaSuccess) ea = cudaMalloc(&b->view_frame, (size_t)n_views * 4);
+        if (ea == cudaSuccess) ea = cudaMalloc(&b->stat, (size_t)b->rows * sizeof(float4));
+        if (ea == cudaSuccess) ea = cudaMalloc(&b->cand, (size_t)b->rows * mlp::kCand * sizeof(mlp::Candidate));
+        if (ea != cudaSuccess) {
+            b->release();
+            delete b;
+            return bcuda(ea, "learned proposal buffers");
+        }
+    }
     if (tuning) {
         if ((rc = check_tuning(*tuning))) {
             delete b;
@@ -217,8 +295,10 @@ int rg_batch_create(rg_context *ctx, const rg_view *views, int32_t n_views, cons
             const bool temporal = (u.flags & RG_FLAG_TEMPORAL_REUSE) != 0;
             rg_reservoir *first = cur_res;
             if (b->unbiased && passes % 2 == 1) first = w.tmp;
+            mlp::LearnedRis vlr = lr;
+            if (learned) vlr.cand = b->cand + (size_t)first_row[(size_t)v] * mlp::kCand;
             make_initial_params(hi.data() + ri * v, *s, cur, temporal ? &prev : nullptr, temporal ? prev_res : nullptr,
-                                first, u, nullptr);
+                                first, u, learned ? &vlr : nullptr);
             if (b->unbiased) {
                 rg_reservoir *src = first;
                 for (int k = 0; k < passes; ++k) {
@@ -271,6 +351,13 @@ int rg_batch_create(rg_context *ctx, const rg_view *views, int32_t n_views, cons
 
 int rg_batch_run(rg_batch *b, int32_t parity, void *stream) {
     if (!b || (parity != 0 && parity != 1)) return bfail(RG_ERR_INVALID_ARGUMENT, "bad arguments");
+    if (b->learned) {
+        ProposalState *ps = *rg_internal_proposal(b->ctx);
+        mlp::ProposalDev pd;
+        mlp::LearnedRis lr;
+        if (!ps || proposal_batch_tables(ps, &pd, &lr) != b->proposal_generation)
+            return bfail(RG_ERR_INVALID_ARGUMENT, "the context's proposal changed since rg_batch_create");
+    }
     int cur = -1;
     B_CUDA(cudaGetDevice(&cur), "cudaGetDevice");
     if (cur != b->device) B_CUDA(cudaSetDevice(b->device), "cudaSetDevice");

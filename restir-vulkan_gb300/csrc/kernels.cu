@@ -809,13 +809,14 @@ __global__ void __launch_bounds__(128) k_shade_views(const ShadeParams *views, c
 
 // frame index of every view for the next run: start + (number of runs so far)
 __global__ void k_advance_frames(InitialParams *ip, SpatialParams *sp, int n_views, int n_spatial,
-                                 const uint32_t *start_frame, uint32_t *runs) {
+                                 const uint32_t *start_frame, uint32_t *runs, uint32_t *frame_out) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t r = *runs;  // read by every thread before thread 0's increment becomes visible to a later launch
+    const uint32_t r = *runs;  // the increment is a later launch (k_count_run)
     if (v < n_views) {
         const uint32_t f = start_frame[v] + r;
         ip[v].u.frame = f;
         for (int k = 0; k < n_spatial; ++k) sp[(size_t)k * n_views + v].u.frame = f;
+        if (frame_out) frame_out[v] = f;
     }
 }
 __global__ void k_count_run(uint32_t *runs) { *runs += 1u; }
@@ -1068,10 +1069,10 @@ cudaError_t launch_views_pass(int kind, int variant, bool unbiased, int num_neig
 }
 
 cudaError_t launch_advance_frames(void *initial_params, void *spatial_params, int n_views, int n_spatial,
-                                  const uint32_t *start_frame, uint32_t *runs, cudaStream_t st) {
+                                  const uint32_t *start_frame, uint32_t *runs, uint32_t *frame_out, cudaStream_t st) {
     k_advance_frames<<<(n_views + 127) / 128, 128, 0, st>>>(static_cast<InitialParams *>(initial_params),
                                                              static_cast<SpatialParams *>(spatial_params), n_views,
-                                                             n_spatial, start_frame, runs);
+                                                             n_spatial, start_frame, runs, frame_out);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_count_run<<<1, 1, 0, st>>>(runs);

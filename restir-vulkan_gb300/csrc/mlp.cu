@@ -145,20 +145,25 @@ struct FusedParams {
     uint32_t frame;
     int n_cand;
     int *err;
+    // batched views (kViews): row -> view by binary search over first_row
+    const mlp::ViewRows *views;
+    int n_views;
+    const uint32_t *frames;    // per view
 };
 
 // Features of one pixel (mlp.cuh), each rounded to bf16; non-finite values
 // (a pixel at the camera position) become 0.
-__device__ __forceinline__ void features(const FusedParams &p, size_t px, float x[mlp::kIn]) {
-    const float4 wp = __ldg(p.g.wpos + px);
-    const uint2 nb = __ldg(p.g.normal + px);
+__device__ __forceinline__ void features(const mlp::ProposalDev &pd, const float4 *wpos_plane, const uint2 *normal_plane,
+                                         float cx, float cy, float cz, size_t px, float x[mlp::kIn]) {
+    const float4 wp = __ldg(wpos_plane + px);
+    const uint2 nb = __ldg(normal_plane + px);
     const f3 wpos = mk(wp.x, wp.y, wp.z);
     const f3 n = mk(half_bits_to_float((uint16_t)(nb.x & 0xffffu)), half_bits_to_float((uint16_t)(nb.x >> 16)),
                     half_bits_to_float((uint16_t)(nb.y & 0xffffu)));
-    const f3 v = normalize(mk(p.cam[0], p.cam[1], p.cam[2]) - wpos);
-    x[0] = (wpos.x - p.pd.box_center.x) * p.pd.box_inv_half.x;
-    x[1] = (wpos.y - p.pd.box_center.y) * p.pd.box_inv_half.y;
-    x[2] = (wpos.z - p.pd.box_center.z) * p.pd.box_inv_half.z;
+    const f3 v = normalize(mk(cx, cy, cz) - wpos);
+    x[0] = (wpos.x - pd.box_center.x) * pd.box_inv_half.x;
+    x[1] = (wpos.y - pd.box_center.y) * pd.box_inv_half.y;
+    x[2] = (wpos.z - pd.box_center.z) * pd.box_inv_half.z;
     x[3] = n.x; x[4] = n.y; x[5] = n.z;
     x[6] = v.x; x[7] = v.y; x[8] = v.z;
 #pragma unroll
@@ -189,7 +194,7 @@ __device__ __forceinline__ bool mma_wait(uint64_t *mbar, uint32_t parity) {
     return __all_sync(0xffffffffu, w);
 }
 
-template <int kMode>
+template <int kMode, bool kViews>
 __global__ void __launch_bounds__(128, 4) k_mlp_fused(const FusedParams p) {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ uint64_t mbar_layer, mbar_chunk[2], mbar_dh;
@@ -198,7 +203,33 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fused(const FusedParams p) {
     const int tid = threadIdx.x, warp = tid >> 5;
     const int row = blockIdx.x * kRows + tid;
     const bool valid = row < p.n;
-    const size_t px = valid ? (p.rows ? (size_t)p.rows[row] : (size_t)row) : 0;
+    size_t px;
+    uint32_t frame = p.frame;
+    int n_cand = p.n_cand;
+    const float4 *wpos_plane = p.g.wpos;
+    const uint2 *normal_plane = p.g.normal;
+    float cx = p.cam[0], cy = p.cam[1], cz = p.cam[2];
+    if constexpr (kViews) {
+        // the view holding this row: the last one whose first row is <= row
+        const uint32_t r = valid ? (uint32_t)row : 0u;
+        int lo = 0, hi = p.n_views - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(&p.views[mid].first_row) <= r) lo = mid;
+            else hi = mid - 1;
+        }
+        const mlp::ViewRows &vr = p.views[lo];
+        px = (size_t)(r - vr.first_row);
+        frame = __ldg(p.frames + lo);
+        n_cand = vr.n_cand;
+        wpos_plane = vr.g.wpos;
+        normal_plane = vr.g.normal;
+        cx = vr.cam[0];
+        cy = vr.cam[1];
+        cz = vr.cam[2];
+    } else {
+        px = valid ? (p.rows ? (size_t)p.rows[row] : (size_t)row) : 0;
+    }
     const int nch = p.pd.c / kChunkN;
     const mlp::Layout L(p.pd.c);
     unsigned char *xtile = smem + kOffX, *htile = smem + kOffH;
@@ -234,7 +265,7 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fused(const FusedParams p) {
     {
         float x[mlp::kIn];
         if (valid) {
-            features(p, px, x);
+            features(p.pd, wpos_plane, normal_plane, cx, cy, cz, px, x);
         } else {
 #pragma unroll
             for (int i = 0; i < mlp::kIn; ++i) x[i] = 0.0f;
@@ -256,8 +287,8 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fused(const FusedParams p) {
     float u_prev = 0.0f;
     Pcg rng{};
     if (kMode == kSample && valid) {
-        rng = pcg_seed((uint64_t)p.frame * mlp::kSeedMul + mlp::kSeedAdd, (uint64_t)px);
-        for (int j = 0; j < p.n_cand; ++j) {
+        rng = pcg_seed((uint64_t)frame * mlp::kSeedMul + mlp::kSeedAdd, (uint64_t)px);
+        for (int j = 0; j < n_cand; ++j) {
             const float u0 = rand_float(rng);
             rand_float(rng);
             if (u0 < p.pd.mix) lmask |= 1u << j;
@@ -504,9 +535,9 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fused(const FusedParams p) {
                         h[j + 2 * i + 1] = f.y;
                     }
                 }
-                Pcg r2 = pcg_seed((uint64_t)p.frame * mlp::kSeedMul + mlp::kSeedAdd, (uint64_t)px);
+                Pcg r2 = pcg_seed((uint64_t)frame * mlp::kSeedMul + mlp::kSeedAdd, (uint64_t)px);
                 const float nl = -lse_row * kLog2e;
-                for (int j = 0; j < p.n_cand; ++j) {
+                for (int j = 0; j < n_cand; ++j) {
                     const float u0 = rand_float(r2);
                     const float u1 = rand_float(r2);
                     if (u0 < p.pd.mix) continue;
@@ -834,13 +865,22 @@ __global__ void k_batch_rows(int32_t *rows, int n, uint32_t pixels, uint32_t off
 }
 
 template <int kMode>
-cudaError_t launch_fused(const FusedParams &p, cudaStream_t st) {
+constexpr int fused_smem() {
+    return (kMode == kGrad ? kSmemGrad : kSmemUsed) < kSmemMin ? kSmemMin : (kMode == kGrad ? kSmemGrad : kSmemUsed);
+}
+
+// set_attr: set the shared-memory attribute first (the batched launches set it
+// once, before any stream capture, in prepare_views)
+template <int kMode, bool kViews = false>
+cudaError_t launch_fused(const FusedParams &p, cudaStream_t st, bool set_attr = true) {
     if (p.pd.c % kChunkN != 0 || p.pd.c < kChunkN) return cudaErrorInvalidValue;
-    int smem = kMode == kGrad ? kSmemGrad : kSmemUsed;
-    if (smem < kSmemMin) smem = kSmemMin;
-    cudaError_t e = cudaFuncSetAttribute(k_mlp_fused<kMode>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    if (p.n > 0) k_mlp_fused<kMode><<<(p.n + kRows - 1) / kRows, kRows, smem, st>>>(p);
+    constexpr int smem = fused_smem<kMode>();
+    if (set_attr) {
+        cudaError_t e =
+            cudaFuncSetAttribute(k_mlp_fused<kMode, kViews>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+    }
+    if (p.n > 0) k_mlp_fused<kMode, kViews><<<(p.n + kRows - 1) / kRows, kRows, smem, st>>>(p);
     return cudaGetLastError();
 }
 
@@ -870,6 +910,33 @@ cudaError_t forward_sample(const ProposalDev &pd, const GBufView &g, const float
     p.pd = pd; p.g = g; p.cam[0] = cam[0]; p.cam[1] = cam[1]; p.cam[2] = cam[2];
     p.n = n; p.stat = const_cast<float4 *>(stat); p.frame = frame; p.n_cand = n_cand; p.cand = cand; p.err = err;
     return launch_fused<kSample>(p, st);
+}
+
+cudaError_t prepare_views() {
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_fused<kLse, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         fused_smem<kLse>());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_mlp_fused<kSample, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 fused_smem<kSample>());
+    return e;
+}
+
+cudaError_t forward_lse_views(const ProposalDev &pd, const ViewRows *views, int n_views, const uint32_t *frames,
+                              int total, float4 *stat, Candidate *cand, int *err, cudaStream_t st) {
+    if (!views || n_views < 1 || !frames || !cand) return cudaErrorInvalidValue;
+    FusedParams p{};
+    p.pd = pd; p.n = total; p.stat = stat; p.err = err; p.cand = cand;
+    p.views = views; p.n_views = n_views; p.frames = frames;
+    return launch_fused<kLse, true>(p, st, false);
+}
+
+cudaError_t forward_sample_views(const ProposalDev &pd, const ViewRows *views, int n_views, const uint32_t *frames,
+                                 int total, const float4 *stat, Candidate *cand, int *err, cudaStream_t st) {
+    if (!views || n_views < 1 || !frames || !cand) return cudaErrorInvalidValue;
+    FusedParams p{};
+    p.pd = pd; p.n = total; p.stat = const_cast<float4 *>(stat); p.err = err; p.cand = cand;
+    p.views = views; p.n_views = n_views; p.frames = frames;
+    return launch_fused<kSample, true>(p, st, false);
 }
 
 cudaError_t forward_grad(const ProposalDev &pd, const GBufView &g, const float cam[3], const int32_t *rows, int n,

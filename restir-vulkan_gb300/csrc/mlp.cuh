@@ -101,6 +101,16 @@ struct TrainBuffers {
     __nv_bfloat16 *x, *h1, *h2, *h3;
 };
 
+// One view of a batched inference.  The views' pixels are concatenated into
+// one row space: view v owns rows first_row .. first_row + w*h - 1 (ascending
+// first_row), row first_row + px being its pixel px.
+struct ViewRows {
+    GBufView g;
+    float cam[3];
+    uint32_t first_row;
+    int32_t n_cand;            // candidates per pixel (1..kCand)
+};
+
 size_t weight_image_bytes();
 // cand != nullptr (inference): also writes the uniform-branch candidates of frame `frame`
 cudaError_t forward_lse(const ProposalDev &pd, const GBufView &g, const float cam[3], const int32_t *rows, int n,
@@ -108,6 +118,14 @@ cudaError_t forward_lse(const ProposalDev &pd, const GBufView &g, const float ca
                         cudaStream_t st);
 cudaError_t forward_sample(const ProposalDev &pd, const GBufView &g, const float cam[3], int n, const float4 *stat,
                            uint32_t frame, int n_cand, Candidate *cand, int *err, cudaStream_t st);
+// Both inference passes over all rows of a batch of views in one launch each;
+// frames[v] is view v's frame index (device memory, read at run time).  The
+// kernels' attributes are set by prepare_views, outside any stream capture.
+cudaError_t prepare_views();
+cudaError_t forward_lse_views(const ProposalDev &pd, const ViewRows *views, int n_views, const uint32_t *frames,
+                              int total, float4 *stat, Candidate *cand, int *err, cudaStream_t st);
+cudaError_t forward_sample_views(const ProposalDev &pd, const ViewRows *views, int n_views, const uint32_t *frames,
+                                 int total, const float4 *stat, Candidate *cand, int *err, cudaStream_t st);
 cudaError_t forward_grad(const ProposalDev &pd, const GBufView &g, const float cam[3], const int32_t *rows, int n,
                          const float4 *stat, const int32_t *target, float inv_n, float *dh3, float *loss_sum,
                          int *err, cudaStream_t st);

@@ -55,6 +55,7 @@ double unit(uint64_t &s) { return (double)(splitmix(s) >> 11) * (1.0 / 900719925
 }  // namespace
 
 struct ProposalState {
+    uint64_t generation = 0;  // distinct for every proposal created in the process
     int c = 0, n_lights = 0, batch = 0;
     float mix = 0.9f, lr = 1e-3f;
     float3 box_center{}, box_inv_half{};
@@ -216,13 +217,21 @@ int proposal_learned_ris(ProposalState *ps, int w, int h, uint32_t frame, uint32
                      "learned candidates are for %dx%d frame %u (%u per pixel), not %dx%d frame %u (%u): "
                      "run rg_proposal_infer first",
                      ps->cand_w, ps->cand_h, ps->cand_frame, ps->cand_count, w, h, frame, count);
+    mlp::ProposalDev dev;
+    proposal_batch_tables(ps, &dev, out);
     out->cand = ps->cand;
+    return RG_OK;
+}
+
+uint64_t proposal_batch_tables(ProposalState *ps, mlp::ProposalDev *dev, mlp::LearnedRis *out) {
+    *dev = ps->dev();
+    out->cand = nullptr;
     out->offset = ps->offset;
     out->lcol = ps->lcol;
     out->within = ps->within;
     out->mix = ps->mix;
     out->uniform_pdf = (1.0f - ps->mix) / (float)ps->n_lights;
-    return RG_OK;
+    return ps->generation;
 }
 
 extern "C" {
@@ -300,7 +309,9 @@ int rg_proposal_create(rg_context *ctx, const rg_proposal_config *cfg, const rg_
     ProposalState **slot = rg_internal_proposal(ctx);
     proposal_release(*slot);
     *slot = nullptr;
+    static uint64_t generations = 0;
     ProposalState *ps = new ProposalState();
+    ps->generation = ++generations;
     ps->c = C;
     ps->n_lights = n;
     ps->batch = cfg->batch;

@@ -65,7 +65,7 @@ struct GBufView {
 GBufView make_view(const rg_gbuffer *g);
 
 // launchers (kernels.cu); return cudaGetLastError()
-namespace mlp { struct LearnedRis; }
+namespace mlp { struct LearnedRis; struct ProposalDev; }
 cudaError_t launch_initial_temporal(const DevScene &s, const GBufView &cur, const GBufView *prev,
                                     const rg_reservoir *prev_res, rg_reservoir *out, const rg_restir_uniforms &u,
                                     const mlp::LearnedRis *learned, cudaStream_t st);
@@ -113,9 +113,10 @@ cudaError_t views_pass_grid(int kind, int variant, bool unbiased, int num_neighb
                             int ctas_per_sm, int *grid);
 cudaError_t launch_views_pass(int kind, int variant, bool unbiased, int num_neighbors, int depth, const void *params,
                               const ViewTiles &vt, int grid, cudaStream_t st);
-// Sets every view's frame index to start_frame[v] + *runs, then adds one to *runs.
+// Sets every view's frame index to start_frame[v] + *runs (also into
+// frame_out[v] when frame_out is not null), then adds one to *runs.
 cudaError_t launch_advance_frames(void *initial_params, void *spatial_params, int n_views, int n_spatial,
-                                  const uint32_t *start_frame, uint32_t *runs, cudaStream_t st);
+                                  const uint32_t *start_frame, uint32_t *runs, uint32_t *frame_out, cudaStream_t st);
 
 // capi.cu: error reporting and context access for other translation units.
 int rg_internal_fail(int code, const char *msg);
@@ -134,3 +135,6 @@ void proposal_release(ProposalState *ps);
 // Learned RIS inputs for a frame of w x h with `count` candidates, or an
 // RG_ERR_* code when the context's candidates do not match that frame.
 int proposal_learned_ris(ProposalState *ps, int w, int h, uint32_t frame, uint32_t count, mlp::LearnedRis *out);
+// The network and the learned RIS tables (cand left null) for batched views,
+// and the proposal's identity: a number no other proposal of the process has.
+uint64_t proposal_batch_tables(ProposalState *ps, mlp::ProposalDev *dev, mlp::LearnedRis *out);

@@ -207,6 +207,10 @@ class Context:
         check(lib().rg_proposal_create(self._h, C.byref(cfg), _lib.ptr(pl), len(pl), _lib.ptr(co)))
         self.proposal_clusters = clusters
 
+    def destroy_proposal(self):
+        check(lib().rg_proposal_destroy(self._h))
+        self.proposal_clusters = 0
+
     def proposal_params(self) -> np.ndarray:
         n = lib().rg_proposal_param_count(self.proposal_clusters)
         out = np.empty(n, np.float32)

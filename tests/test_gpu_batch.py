@@ -23,17 +23,21 @@ def views5(restir_lib):
     return base, views
 
 
-def _make(ctx, cuda, base, views, unbiased=True):
+def _make(ctx, cuda, base, views, unbiased=True, learned=False):
+    from restir_gb300 import _lib
     from restir_gb300.passes import DeviceGBuffer, reservoirs
     ctx.upload_scene(base)
     out = []
-    for v in views:
+    for i, v in enumerate(views):
         g = DeviceGBuffer(v.width, v.height)
         ctx.trace_gbuffer(v.cameras[0], g)
         n = v.width * v.height
         u = v.uniforms(0)
         u.flags |= 2  # temporal reuse (static camera: the previous G-buffer is the current one)
         u.frame = 7
+        if learned:
+            u.flags |= _lib.RG_FLAG_LEARNED_PROPOSAL
+            u.initial_light_sample_count = (32, 16, 8)[i % 3]
         out.append({"scene": v, "cur": g, "prev": g, "res0": reservoirs(n), "res1": reservoirs(n),
                     "tmp": reservoirs(n),
                     "image": cuda.zeros((v.height, v.width, 4), dtype=cuda.float32, device="cuda"), "uniforms": u})
@@ -55,6 +59,9 @@ def _single(ctx, cuda, vw, fp, parity, frame):
     uu.frame = frame
     cur, prev = vw[f"s{parity}"], vw[f"s{1 - parity}"]
     passes = fp.spatial_iterations
+    from restir_gb300 import _lib
+    if uu.flags & _lib.RG_FLAG_LEARNED_PROPOSAL:
+        ctx.proposal_infer(vw["cur"], uu)
     if fp.unbiased:
         first = vw["stmp"] if passes % 2 == 1 else cur
         ctx.initial_temporal(vw["cur"], vw["prev"], prev, first, uu)
@@ -150,4 +157,46 @@ def test_autotune_keeps_results(ctx, cuda, views5):
         for k in ("res0", "res1", "tmp"):
             vw[k].zero_()
     _compare(ctx, cuda, vws, fp, b, runs=2)
+    b.close()
+
+
+def test_batch_learned_proposal_equals_single_views(ctx, cuda, views5):
+    """Learned proposal: one inference launch pair over all views' pixels,
+    then the batched passes; every view equals rg_proposal_infer +
+    rg_render_frame's sequence for that view (views draw 32, 16 or 8
+    candidates), also from a captured graph."""
+    from restir_gb300.passes import Batch, cluster_lights
+    base, views = views5
+    vws, fp = _make(ctx, cuda, base, views, unbiased=True, learned=True)
+    cluster_of, _ = cluster_lights(base.point_lights, 256, iterations=4, seed=3)
+    ctx.create_proposal(cluster_of, 256, seed=5)
+    b = Batch(ctx, vws, fp)
+    _compare(ctx, cuda, vws, fp, b, runs=2)
+    b.run(0)
+    cuda.cuda.synchronize()
+    _compare(ctx, cuda, vws, fp, b, runs=2, graph=True)
+    b.close()
+    assert ctx.stats().mma_timeouts == 0
+    assert ctx.stats().traversal_errors == 0
+
+
+def test_batch_learned_guards(ctx, cuda, views5):
+    from restir_gb300 import _lib
+    from restir_gb300._lib import RestirError
+    from restir_gb300.passes import Batch, cluster_lights
+    base, views = views5
+    vws, fp = _make(ctx, cuda, base, views[:2], unbiased=True, learned=True)
+    ctx.destroy_proposal()
+    with pytest.raises(RestirError, match="without a proposal"):
+        Batch(ctx, vws, fp)
+    cluster_of, _ = cluster_lights(base.point_lights, 256, iterations=2, seed=3)
+    ctx.create_proposal(cluster_of, 256, seed=5)
+    vws[1]["uniforms"].flags &= ~_lib.RG_FLAG_LEARNED_PROPOSAL
+    with pytest.raises(RestirError, match="all views or none"):
+        Batch(ctx, vws, fp)
+    vws[1]["uniforms"].flags |= _lib.RG_FLAG_LEARNED_PROPOSAL
+    b = Batch(ctx, vws, fp)
+    ctx.create_proposal(cluster_of, 256, seed=6)  # a new proposal: the batch's tables are stale
+    with pytest.raises(RestirError, match="proposal changed"):
+        b.run(0)
     b.close()
