@@ -12,9 +12,11 @@
 // one FMA per logit.
 //   kSample  the learned-branch candidates: each row walks its softmax CDF
 //            once with its uniforms drawn as ascending order statistics; a
-//            uniform's column is found by a branch-free count inside the
-//            32-column piece that holds it.  (The uniform-branch candidates,
-//            a light and q of its cluster, are written at the end of kLse.)
+//            uniform's column inside the 32-column piece that holds it is
+//            found by binary search over the piece's running sums, and its
+//            probability is the width of its interval.  (The uniform-branch
+//            candidates, a light and q of its cluster, are written at the
+//            end of kLse.)
 //   kGrad    for training: dz = d(loss)/d(logits) = (softmax - onehot) / n
 //            per chunk into a bf16 tile, then dh3 += dz W4^T on the tensor
 //            cores (accumulated in tensor memory over the chunks), and the
@@ -73,27 +75,60 @@ __device__ __forceinline__ float ex2(float x) {
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
-__device__ __forceinline__ float max32(const float (&v)[32]) {
-    float a[16];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) a[i] = fmaxf(v[2 * i], v[2 * i + 1]);
-#pragma unroll
-    for (int w = 8; w >= 1; w >>= 1)
-#pragma unroll
-        for (int i = 0; i < w; ++i) a[i] = fmaxf(a[i], a[i + w]);
-    return a[0];
+// A 32-column piece of one row is held as 16 float2 pairs (columns 2k, 2k+1),
+// so that adds and FMAs run as packed FP32x2 operations (each lane of a
+// packed op rounds exactly like the scalar op).
+__device__ __forceinline__ float col(const float2 (&v)[16], int i) { return (i & 1) ? v[i >> 1].y : v[i >> 1].x; }
+// max of three (IEEE maxNum, like fmaxf)
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float y;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(y) : "f"(a), "f"(b), "f"(c));
+    return y;
 }
-__device__ __forceinline__ float sum32(const float (&v)[32]) {
-    float a[8];
+__device__ __forceinline__ float max32(const float2 (&v)[16]) {
+    float a[11];
 #pragma unroll
-    for (int i = 0; i < 8; ++i) a[i] = (v[i] + v[i + 8]) + (v[i + 16] + v[i + 24]);
-    return ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+    for (int k = 0; k < 10; ++k) a[k] = max3f(col(v, 3 * k), col(v, 3 * k + 1), col(v, 3 * k + 2));
+    a[10] = fmaxf(col(v, 30), col(v, 31));
+    const float b0 = max3f(a[0], a[1], a[2]), b1 = max3f(a[3], a[4], a[5]), b2 = max3f(a[6], a[7], a[8]);
+    return fmaxf(max3f(b0, b1, b2), fmaxf(a[9], a[10]));
+}
+__device__ __forceinline__ float sum32(const float2 (&v)[16]) {
+    float2 t[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) t[k] = __fadd2_rn(v[k], v[k + 8]);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) t[k] = __fadd2_rn(t[k], t[k + 4]);
+    t[0] = __fadd2_rn(t[0], t[2]);
+    t[1] = __fadd2_rn(t[1], t[3]);
+    t[0] = __fadd2_rn(t[0], t[1]);
+    return t[0].x + t[0].y;
+}
+// v[k] = 2^(v[k] * log2(e) + off), both columns of every pair
+__device__ __forceinline__ void exp_piece(float2 (&v)[16], float off) {
+    const float2 l2 = make_float2(kLog2e, kLog2e), o2 = make_float2(off, off);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        const float2 t = __ffma2_rn(v[k], l2, o2);
+        v[k] = make_float2(ex2(t.x), ex2(t.y));
+    }
+}
+__device__ __forceinline__ float lg2(float x) {
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
 }
 // Next of n ascending order statistics of U(0,1) given the previous one:
-// 1 - (1 - prev) * V^(1/remaining), V uniform.
+// 1 - (1 - prev) * V^(1/remaining), V uniform; the power as 2^(log2(V) / n)
+// on the MUFU unit (V = 0 gives 1: beyond every CDF total).
 __device__ __forceinline__ float next_order_stat(Pcg &rng, float prev, int remaining) {
     const float v = rand_float(rng);
-    return 1.0f - (1.0f - prev) * powf(v, 1.0f / (float)remaining);
+    return 1.0f - (1.0f - prev) * ex2(lg2(v) * rcp((float)remaining));
 }
 // z of cluster cl for the row whose h3 is h: FP32 dot with the bf16 W4^T
 // image (chunk tiles in the MMA operand layout) plus b4.
@@ -426,15 +461,17 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fused(const FusedParams p) {
             umma::tmem_ld32_wait(raw[piece & 1]);
             // the next piece's load runs under this piece's arithmetic
             if (piece + 1 < kChunkN / 32) umma::tmem_ld32_issue(half, warp, (piece + 1) * 32, raw[(piece + 1) & 1]);
-            float v[32];
-#pragma unroll
-            for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(raw[piece & 1][i]);
+            const uint32_t(&rw)[32] = raw[piece & 1];
             const int col0 = c * kChunkN + piece * 32;
             const float4 *be = reinterpret_cast<const float4 *>(p.pd.b4e + col0);
+            float2 v[16];  // logits z = MMA result + b4
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
                 const float4 b = __ldg(be + q);
-                v[4 * q] += b.x; v[4 * q + 1] += b.y; v[4 * q + 2] += b.z; v[4 * q + 3] += b.w;
+                v[2 * q] = __fadd2_rn(make_float2(__uint_as_float(rw[4 * q]), __uint_as_float(rw[4 * q + 1])),
+                                      make_float2(b.x, b.y));
+                v[2 * q + 1] = __fadd2_rn(make_float2(__uint_as_float(rw[4 * q + 2]), __uint_as_float(rw[4 * q + 3])),
+                                          make_float2(b.z, b.w));
             }
             if (kMode == kLse) {
                 const float mp = max32(v);
@@ -442,11 +479,9 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fused(const FusedParams p) {
                 if (mp > m) {
 #pragma unroll
                     for (int i = 31; i >= 0; --i)
-                        if (v[i] == mp) amax = col0 + i;
+                        if (col(v, i) == mp) amax = col0 + i;
                 }
-                const float nm = -mp * kLog2e;
-#pragma unroll
-                for (int i = 0; i < 32; ++i) v[i] = ex2(__fmaf_rn(v[i], kLog2e, nm));
+                exp_piece(v, -mp * kLog2e);
                 const float sp = sum32(v);
                 if (mp > m) {
                     s = (m == -INFINITY) ? sp : __fmaf_rn(s, ex2((m - mp) * kLog2e), sp);
@@ -455,32 +490,50 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fused(const FusedParams p) {
                     s = __fmaf_rn(sp, ex2((mp - m) * kLog2e), s);
                 }
             } else if (kMode == kSample) {
-                if (!valid) continue;
-#pragma unroll
-                for (int i = 0; i < 32; ++i) v[i] = ex2(__fmaf_rn(v[i], kLog2e, nl2));
+                exp_piece(v, nl2);
                 const float end = cum + sum32(v);
-                // each uniform below `end` belongs to this piece: its column is
-                // the first whose running sum exceeds it (at most the last)
-                while (next_u < end) {
-                    float c = cum, q = v[0];
-                    int idx = 0;
+                // the uniforms below `end` belong to this piece
+                if (valid && next_u < end) {
+                    // running sums within the piece, left to right
+                    float r[32];
+                    r[0] = v[0].x;
 #pragma unroll
-                    for (int i = 0; i < 31; ++i) {
-                        c += v[i];
-                        const bool past = c <= next_u;
-                        idx += past ? 1 : 0;
-                        q = past ? v[i + 1] : q;
-                    }
-                    take(col0 + idx, q);
+                    for (int i = 1; i < 32; ++i) r[i] = r[i - 1] + col(v, i);
+                    do {
+                        // the column is the first whose running sum exceeds the
+                        // uniform (at most the last), by binary search; its
+                        // probability is the width of its interval
+                        const float ul = next_u - cum;
+                        float a[16];
+                        int idx = 0;
+                        float lo = 0.0f;
+                        {
+                            const bool b = r[15] <= ul;
+                            lo = b ? r[15] : lo;
+                            idx += b ? 16 : 0;
+#pragma unroll
+                            for (int j = 0; j < 16; ++j) a[j] = b ? r[16 + j] : r[j];
+                        }
+#pragma unroll
+                        for (int h = 8; h >= 1; h >>= 1) {
+                            const bool b = a[h - 1] <= ul;
+                            lo = b ? a[h - 1] : lo;
+                            idx += b ? h : 0;
+#pragma unroll
+                            for (int j = 0; j < h; ++j) a[j] = b ? a[h + j] : a[j];
+                        }
+                        take(col0 + idx, a[0] - lo);
+                    } while (next_u < end);
                 }
                 cum = end;
             } else {  // kGrad: the gradient rows go to the dz tile (bf16)
                 float d[32];
 #pragma unroll
                 for (int i = 0; i < 32; ++i) {
-                    const float pr = ex2(__fmaf_rn(v[i], kLog2e, nl2));
+                    const float z = col(v, i);
+                    const float pr = ex2(__fmaf_rn(z, kLog2e, nl2));
                     const bool hit = (col0 + i) == target;
-                    if (hit) zt = v[i];
+                    if (hit) zt = z;
                     d[i] = target < 0 ? 0.0f : (pr - (hit ? 1.0f : 0.0f)) * p.inv_n;
                 }
 #pragma unroll
