@@ -130,23 +130,21 @@ __device__ __forceinline__ float next_order_stat(Pcg &rng, float prev, int remai
     const float v = rand_float(rng);
     return 1.0f - (1.0f - prev) * ex2(lg2(v) * rcp((float)remaining));
 }
-// z of cluster cl for the row whose h3 is h: FP32 dot with the bf16 W4^T
-// image (chunk tiles in the MMA operand layout) plus b4.
+// z of cluster cl for the row whose h3 is h: FP32 dot (even and odd terms
+// in two packed FMA chains) with the bf16 W4^T image (chunk tiles in the MMA
+// operand layout) plus b4.
 __device__ __forceinline__ float logit_of(const mlp::ProposalDev &pd, const float (&h)[64], int cl) {
     const unsigned char *tile = reinterpret_cast<const unsigned char *>(pd.w4t) + (size_t)(cl / kChunkN) * kChunkBytes;
-    float z = 0.0f;
+    float2 z = make_float2(0.0f, 0.0f);
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         const uint4 w = __ldg(reinterpret_cast<const uint4 *>(tile + umma::kmajor_offset(cl % kChunkN, 8 * j, mlp::kH)));
         const __nv_bfloat162 *b = reinterpret_cast<const __nv_bfloat162 *>(&w);
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const float2 f = __bfloat1622float2(b[i]);
-            z += h[8 * j + 2 * i] * f.x;
-            z += h[8 * j + 2 * i + 1] * f.y;
-        }
+        for (int i = 0; i < 4; ++i)
+            z = __ffma2_rn(make_float2(h[8 * j + 2 * i], h[8 * j + 2 * i + 1]), __bfloat1622float2(b[i]), z);
     }
-    return z + __ldg(pd.b4e + cl);
+    return (z.x + z.y) + __ldg(pd.b4e + cl);
 }
 
 __device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
@@ -590,10 +588,30 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fused(const FusedParams p) {
                 }
                 Pcg r2 = pcg_seed((uint64_t)frame * mlp::kSeedMul + mlp::kSeedAdd, (uint64_t)px);
                 const float nl = -lse_row * kLog2e;
-                for (int j = 0; j < n_cand; ++j) {
-                    const float u0 = rand_float(r2);
+                // first the slots that take the uniform branch (about 1 in 10),
+                // then one loop iteration per such slot of this row: the warp
+                // runs as many dot products as its busiest row has slots, not
+                // one per slot index that any row uses
+                uint32_t umask = 0;
+                {
+                    Pcg r1 = r2;
+                    for (int j = 0; j < n_cand; ++j) {
+                        const float u0 = rand_float(r1);
+                        rand_float(r1);
+                        if (!(u0 < p.pd.mix)) umask |= 1u << j;
+                    }
+                }
+                int pos = 0;  // slots of r2's stream consumed
+                while (umask) {
+                    const int j = __ffs(umask) - 1;
+                    umask &= umask - 1;
+                    for (; pos < j; ++pos) {
+                        rand_float(r2);
+                        rand_float(r2);
+                    }
+                    rand_float(r2);
                     const float u1 = rand_float(r2);
-                    if (u0 < p.pd.mix) continue;
+                    ++pos;
                     const int l = imin((int)((float)p.pd.n_lights * u1), p.pd.n_lights - 1);
                     const float z = logit_of(p.pd, h, __ldg(p.pd.cluster_of + l));
                     p.cand[(size_t)row * mlp::kCand + j] = mlp::Candidate{l, ex2(__fmaf_rn(z, kLog2e, nl))};
