@@ -360,6 +360,9 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
         "clocks": clock_rec,
     }
 
+    # the passes that HBM bandwidth bounds, timed alone on this frame size
+    line["hbm_passes"] = hbm_passes(ctx, s, dgs, res + [tmp], image, stream, peaks)
+
     # e2e through the host-buffer C ABI call
     if not args.no_e2e:
         host_frames = []
@@ -415,6 +418,53 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
                                 "full_frame_seconds_estimate": round(cb["frame_seconds_estimate"], 2)}
     ctx.close()
     return line
+
+
+def hbm_passes(ctx, s, dgs, bufs, image, stream, peaks, iters: int = 12) -> dict:
+    """The reservoir passes whose bound is HBM bandwidth (biased spatial reuse:
+    no rays; shading), each timed alone with CUDA events over `iters`
+    launches.  Launches cycle over the configuration's pre-traced frames and
+    four reservoir buffers (a launch reads the buffer written two launches
+    earlier), so every launch's inputs come from HBM, not L2."""
+    import torch
+
+    from restir_gb300.passes import reservoirs
+    n = s.width * s.height
+    extra = reservoirs(n)
+    bufs = list(bufs) + [extra]
+    bufs[3].copy_(bufs[0])
+    out = {}
+
+    def timed(fn):
+        for k in range(3):
+            fn(k)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(iters):
+            fn(3 + k)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / iters
+
+    def biased(k):
+        f = k % s.frames
+        ctx.spatial_biased(dgs[f], bufs[k % 4], bufs[(k + 2) % 4], s.uniforms(f), k & 1, stream)
+
+    def shade(k):
+        f = k % s.frames
+        ctx.shade(dgs[f], bufs[k % 4], s.lighting_uniforms(f), image, stream)
+
+    for name, fn in (("spatial_biased", biased), ("shade", shade)):
+        ms = timed(fn)
+        gbs = BYTES_PER_PX[name] * n / (ms / 1000.0) / 1e9
+        out[name] = {"mean_launch_ms": round(ms, 4), "algorithmic_bytes_per_px": BYTES_PER_PX[name],
+                     "achieved_gbs": round(gbs, 1), "frac": round(gbs / peaks["hbm_gbs"], 4)}
+    out["peak_gbs"] = peaks["hbm_gbs"]
+    out["note"] = ("frac = algorithmic bytes (reference layouts, 52 useful bytes per reservoir) per launch over the "
+                   "launch time, against the measured copy peak")
+    del extra
+    return out
 
 
 # ------------------------------------------------------------------ learned proposal (config 4 workload)

@@ -603,30 +603,31 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
         for (int q = 0; q < R; ++q) lpos[q] = xyz(r.pos_lum[q]);
         store_resv(p.out, i, r);
     }
+    // A pixel's segments (one per neighbour whose hemisphere holds the sample,
+    // and its own) share the sample's light as their end point: they go to the
+    // pool consecutively, so the lanes that take them trace similar paths.
 #pragma unroll
     for (int q = 0; q < R; ++q) {
         endp[q * 128 + tid] = make_float4(lpos[q].x, lpos[q].y, lpos[q].z, 0.0f);
+        uint32_t wantm = 0;  // bit k: neighbour k's segment; bit K: the pixel's own
         for (int k = 0; k < K; ++k) {
-            bool want = false, excluded = true;
-            f3 nw = mk(0.f, 0.f, 0.f);
+            bool excluded = true;
             if (valid) {
                 const uint32_t ni = nidx[k * 128 + tid];
-                nw = load_wpos(p.g, ni);
+                const f3 nw = load_wpos(p.g, ni);
                 const f3 nn = load_normal(p.g, ni);
                 excluded = dot(lpos[q] - nw, nn) < 0.0f;
-                want = !excluded && vis;
+                if (!excluded && vis) wantm |= 1u << k;
             }
-            const int owner = (q * slots + k) * 128 + tid;
-            flag[owner] = excluded ? 1 : 0;
-            const int slot = rgpool::append_slot(&s_count, want);
-            if (want) rgpool::put_ray(pool, slot, nw, owner);
+            flag[(q * slots + k) * 128 + tid] = excluded ? 1 : 0;
         }
-        {
-            const bool want = valid && vis;
-            const int owner = (q * slots + K) * 128 + tid;
-            flag[owner] = 0;
-            const int slot = rgpool::append_slot(&s_count, want);
-            if (want) rgpool::put_ray(pool, slot, wpos, owner);
+        flag[(q * slots + K) * 128 + tid] = 0;
+        if (valid && vis) wantm |= 1u << K;
+        int slot = rgpool::append_range(&s_count, __popc(wantm));
+        for (uint32_t m = wantm; m != 0u; m &= m - 1u) {
+            const int k = __ffs(m) - 1;
+            const f3 start = k < K ? load_wpos(p.g, nidx[k * 128 + tid]) : wpos;
+            rgpool::put_ray(pool, slot++, start, (q * slots + k) * 128 + tid);
         }
     }
     __syncthreads();

@@ -47,6 +47,23 @@ __device__ __forceinline__ int append_slot(int *counter, bool want) {
     return base + __popc(mask & ((1u << lane) - 1u));
 }
 
+// Warp-aggregated append of `count` consecutive slots per lane (every lane of
+// the warp calls it): returns this lane's first slot.
+__device__ __forceinline__ int append_range(int *counter, int count) {
+    const int lane = (threadIdx.x + threadIdx.y * blockDim.x) & 31;
+    int inc = count;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, inc, 31);
+    int base = 0;
+    if (lane == 0 && total > 0) base = atomicAdd(counter, total);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    return base + inc - count;
+}
+
 // Slab test of one child box (softwareRaytracing.glsl:9-14); also returns the
 // entry distance, used only to order the walk.
 __device__ __forceinline__ bool box_hit(f3 o, f3 d, f3 bmin, f3 bmax, float &rmin_out) {

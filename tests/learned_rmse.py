@@ -35,7 +35,7 @@ for p in (ROOT / "restir-vulkan_gb300", ROOT / "oracle", ROOT / "tests"):
         sys.path.insert(0, str(p))
 
 
-def _arm(ctx, s, dg, res, image, crop, judge, frames, learned, steps_per_frame):
+def _arm(ctx, s, dg, res, image, crop, judge, frames, learned, steps_per_frame, candidates=32):
     import torch
     from restir_gb300 import _lib
     x0, y0, cw, ch = crop
@@ -51,6 +51,7 @@ def _arm(ctx, s, dg, res, image, crop, judge, frames, learned, steps_per_frame):
         u.flags = _lib.RG_FLAG_VISIBILITY_REUSE | _lib.RG_FLAG_FINAL_RIS_WEIGHT
         if learned:
             u.flags |= _lib.RG_FLAG_LEARNED_PROPOSAL
+            u.initial_light_sample_count = candidates
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -76,7 +77,7 @@ def _arm(ctx, s, dg, res, image, crop, judge, frames, learned, steps_per_frame):
 
 
 def run(width=1920, height=1080, frames=64, clusters=4096, n_tris=100_000, n_lights=65_536, crop_size=64,
-        lr=3e-3, steps_per_frame=1, batch=65_536, kmeans_iters=8, seed=4, log=print):
+        lr=3e-3, steps_per_frame=1, batch=65_536, kmeans_iters=8, seed=4, log=print, learned_candidates=32):
     import torch
 
     import oracle_binding as ob
@@ -105,7 +106,8 @@ def run(width=1920, height=1080, frames=64, clusters=4096, n_tris=100_000, n_lig
     _arm(ctx, s, dg, res, image, crop, judge, 2, False, 1)
     plain_ms, plain_rmse, _ = _arm(ctx, s, dg, res, image, crop, judge, frames, False, 1)
     ctx.create_proposal(cluster_of, clusters, mix=0.9, learning_rate=lr, batch=batch, seed=seed)
-    lrn_ms, lrn_rmse, loss = _arm(ctx, s, dg, res, image, crop, judge, frames, True, steps_per_frame)
+    lrn_ms, lrn_rmse, loss = _arm(ctx, s, dg, res, image, crop, judge, frames, True, steps_per_frame,
+                                  learned_candidates)
     st = ctx.stats()
     ctx.close()
     target = plain_rmse[-1]
@@ -116,7 +118,8 @@ def run(width=1920, height=1080, frames=64, clusters=4096, n_tris=100_000, n_lig
     return {
         "workload": f"config 4: config 2 scene {width}x{height}, {n_tris} random triangles, {n_lights} point lights, "
                     f"{clusters} k-means clusters, static camera, {frames} frames",
-        "estimator": "RIS 32 candidates + visibility reuse + final RIS weight, shaded; running mean of frames",
+        "estimator": f"RIS (plain 32, learned {learned_candidates} candidates) + visibility reuse + final RIS weight, "
+                     "shaded; running mean of frames",
         "judge": f"FP64 brute force (every light, exact visibility) on a {crop_size}x{crop_size} crop at {crop[:2]}",
         "judge_mean_radiance": judge_mean,
         "plain": {"ms_per_frame": plain_ms[-1] / frames, "final_rmse": target,
@@ -148,10 +151,11 @@ def main(argv=None):
     ap.add_argument("--lr", type=float, default=3e-3)
     ap.add_argument("--steps-per-frame", type=int, default=1)
     ap.add_argument("--batch", type=int, default=65_536)
+    ap.add_argument("--learned-candidates", type=int, default=32, help="RIS candidates of the learned arm")
     ap.add_argument("--out", default=None, help="also write the JSON here")
     a = ap.parse_args(argv)
     r = run(a.width, a.height, a.frames, a.clusters, a.tris, a.lights, a.crop, a.lr, a.steps_per_frame, a.batch,
-            log=lambda *x: print(*x, file=sys.stderr, flush=True))
+            log=lambda *x: print(*x, file=sys.stderr, flush=True), learned_candidates=a.learned_candidates)
     txt = json.dumps(r)
     print(txt, flush=True)
     if a.out:
