@@ -282,15 +282,18 @@ int host_build_alias_table(const rg_point_light *pl, int32_t n_pl, const rg_tri_
     return RG_OK;
 }
 
-// GNode: a = lmin.xyz lmax.x, b = lmax.yz rmin.xy, c = rmin.z rmax.xyz, d = left right.
+// GNode: per axis (a = x, b = y, c = z) left min, right min, left max, right
+// max; d = left right.
 void host_pack_nodes(const rg_aabb_tree_node *src, int32_t n, float *dst16) {
     for (int32_t i = 0; i < n; ++i) {
         const rg_aabb_tree_node &s = src[i];
         float *d = dst16 + 16 * (size_t)i;
-        d[0] = s.left_aabb_min[0]; d[1] = s.left_aabb_min[1]; d[2] = s.left_aabb_min[2];
-        d[3] = s.left_aabb_max[0]; d[4] = s.left_aabb_max[1]; d[5] = s.left_aabb_max[2];
-        d[6] = s.right_aabb_min[0]; d[7] = s.right_aabb_min[1]; d[8] = s.right_aabb_min[2];
-        d[9] = s.right_aabb_max[0]; d[10] = s.right_aabb_max[1]; d[11] = s.right_aabb_max[2];
+        for (int a = 0; a < 3; ++a) {  // per axis: left min, right min, left max, right max
+            d[4 * a] = s.left_aabb_min[a];
+            d[4 * a + 1] = s.right_aabb_min[a];
+            d[4 * a + 2] = s.left_aabb_max[a];
+            d[4 * a + 3] = s.right_aabb_max[a];
+        }
         memcpy(&d[12], &s.left_child, 4);
         memcpy(&d[13], &s.right_child, 4);
         d[14] = 0.0f;

@@ -65,8 +65,8 @@ RG_HD Hit closest_hit(const TraceScene &s, f3 o, f3 d) {
         const float *n = s.nodes + 16 * (size_t)node;
         const int left = ((const int *)n)[12], right = ((const int *)n)[13];
         float tl, tr;
-        const bool hl = slab(o, inv, mk(n[0], n[1], n[2]), mk(n[3], n[4], n[5]), h.t, tl);
-        const bool hr = slab(o, inv, mk(n[6], n[7], n[8]), mk(n[9], n[10], n[11]), h.t, tr);
+        const bool hl = slab(o, inv, mk(n[0], n[4], n[8]), mk(n[2], n[6], n[10]), h.t, tl);
+        const bool hr = slab(o, inv, mk(n[1], n[5], n[9]), mk(n[3], n[7], n[11]), h.t, tr);
         int first = -1, second = -1;
         if (hl) {
             if (left < 0) {

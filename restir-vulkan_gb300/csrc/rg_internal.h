@@ -3,8 +3,9 @@
 // The reference's buffers are repacked once at upload into layouts a GB300
 // reads with 128-bit loads; the repacking copies values, it never recomputes
 // them, so every test the kernels evaluate sees the reference's floats.
-//   GNode      64 B: both child boxes + child links of one AabbTreeNode
-//              (80 B in the reference: the vec4 w lanes are dropped).
+//   GNode      64 B: both child boxes (interleaved per axis) + child links
+//              of one AabbTreeNode (80 B in the reference: the vec4 w lanes
+//              are dropped).
 //   GTri       48 B: p1, e1 = p2-p1, e2 = p3-p1 (the same subtractions the
 //              reference's rayTriangleIntersection performs per test).
 //   AliasLight 48 B: one alias-table column plus the position/luminance of
@@ -16,9 +17,9 @@
 #include "../../include/restir_gb300.h"
 
 struct GNode {
-    float4 a;  // lmin.x lmin.y lmin.z lmax.x
-    float4 b;  // lmax.y lmax.z rmin.x rmin.y
-    float4 c;  // rmin.z rmax.x rmax.y rmax.z
+    float4 a;  // lmin.x rmin.x lmax.x rmax.x  (per axis, so that a pair of lanes
+    float4 b;  // lmin.y rmin.y lmax.y rmax.y   holds the same bound of both
+    float4 c;  // lmin.z rmin.z lmax.z rmax.z   children: packed FP32x2 slab math)
     int4 d;    // left right 0 0
 };
 struct GTri {

@@ -88,32 +88,64 @@ __device__ __forceinline__ bool box_hit(f3 o, f3 d, f3 bmin, f3 bmax, float &rmi
 // otherwise the function returns -1 and the caller repeats the test with
 // exact division.  NaN slabs (b == o and d == 0) arise at the same positions
 // in both computations and propagate the same way through min/max.
-// Returns 1 hit, 0 miss, -1 undecided.
+// Decisions: 1 hit, 0 miss, -1 undecided.
 //
 // The fast path only runs for rays whose direction components are all
 // nonzero, finite and within [2^-100, 2^100] in magnitude (ray_inverse), so
 // no slab value is NaN or infinite and IEEE fminf/fmaxf select the same
 // values as the GLSL min/max definitions (a +-0 result fails the 2^-90 test
 // and is decided exactly).
-__device__ __forceinline__ int box_filtered(f3 o, f3 inv, f3 bmin, f3 bmax, float &rmin_out) {
-    const float t0x = (bmin.x - o.x) * inv.x, t1x = (bmax.x - o.x) * inv.x;
-    const float t0y = (bmin.y - o.y) * inv.y, t1y = (bmax.y - o.y) * inv.y;
-    const float t0z = (bmin.z - o.z) * inv.z, t1z = (bmax.z - o.z) * inv.z;
-    const float rmin = fmaxf(fminf(t0x, t1x), fmaxf(fminf(t0y, t1y), fminf(t0z, t1z)));
-    const float rmax = fminf(fmaxf(t0x, t1x), fminf(fmaxf(t0y, t1y), fmaxf(t0z, t1z)));
-    rmin_out = rmin;
+
+// max/min of three (IEEE maxNum/minNum, as fmaxf/fminf)
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float y;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(y) : "f"(a), "f"(b), "f"(c));
+    return y;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float y;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(y) : "f"(a), "f"(b), "f"(c));
+    return y;
+}
+
+// The decision of box_filtered from a box's slab distances.
+__device__ __forceinline__ int filtered_decision(float rmin, float rmax) {
     constexpr float kEps = 1.9073486328125e-6f;     // 2^-19
     constexpr float kTiny = 8.0779356694631609e-28f; // 2^-90
     constexpr float kBig = 1.0e38f;
     const float ar = fabsf(rmin), ax = fabsf(rmax);
     if (!(ar >= kTiny && ar <= kBig && ax >= kTiny && ax <= kBig)) return -1;
-    if (rmax < 0.0f) return 0;                               // rmax > 0 fails
+    if (rmax < 0.0f) return 0;
     const float m1 = kEps * ar;
-    if (rmin > 1.0f + m1) return 0;                          // rmin < 1 fails
+    if (rmin > 1.0f + m1) return 0;
     const float m2 = kEps * (ar + ax);
-    if (rmin - rmax > m2) return 0;                          // rmax >= rmin fails
-    if (rmin < 1.0f - m1 && rmax - rmin > m2) return 1;      // all three hold
+    if (rmin - rmax > m2) return 0;
+    if (rmin < 1.0f - m1 && rmax - rmin > m2) return 1;
     return -1;
+}
+
+// The filtered test of both children of a node at once: lane .x of every
+// packed pair is the left box, lane .y the right box; each lane rounds
+// exactly like the scalar t~ = RN((b - o) * RN(1/d)) (b - o is b + (-o)),
+// and min/max of three is the nested min/max.
+__device__ __forceinline__ void boxes_filtered(f3 o, f3 inv, const float4 &na, const float4 &nb, const float4 &nc,
+                                               int &fl, int &fr, float &tl, float &tr) {
+    const float2 nox = make_float2(-o.x, -o.x), noy = make_float2(-o.y, -o.y), noz = make_float2(-o.z, -o.z);
+    const float2 ix = make_float2(inv.x, inv.x), iy = make_float2(inv.y, inv.y), iz = make_float2(inv.z, inv.z);
+    const float2 t0x = __fmul2_rn(__fadd2_rn(make_float2(na.x, na.y), nox), ix);
+    const float2 t1x = __fmul2_rn(__fadd2_rn(make_float2(na.z, na.w), nox), ix);
+    const float2 t0y = __fmul2_rn(__fadd2_rn(make_float2(nb.x, nb.y), noy), iy);
+    const float2 t1y = __fmul2_rn(__fadd2_rn(make_float2(nb.z, nb.w), noy), iy);
+    const float2 t0z = __fmul2_rn(__fadd2_rn(make_float2(nc.x, nc.y), noz), iz);
+    const float2 t1z = __fmul2_rn(__fadd2_rn(make_float2(nc.z, nc.w), noz), iz);
+    const float rminl = max3f(fminf(t0x.x, t1x.x), fminf(t0y.x, t1y.x), fminf(t0z.x, t1z.x));
+    const float rmaxl = min3f(fmaxf(t0x.x, t1x.x), fmaxf(t0y.x, t1y.x), fmaxf(t0z.x, t1z.x));
+    const float rminr = max3f(fminf(t0x.y, t1x.y), fminf(t0y.y, t1y.y), fminf(t0z.y, t1z.y));
+    const float rmaxr = min3f(fmaxf(t0x.y, t1x.y), fmaxf(t0y.y, t1y.y), fmaxf(t0z.y, t1z.y));
+    tl = rminl;
+    tr = rminr;
+    fl = filtered_decision(rminl, rmaxl);
+    fr = filtered_decision(rminr, rmaxr);
 }
 
 // Per-ray reciprocal of the direction; false when a component is zero,
@@ -248,14 +280,11 @@ __device__ void trace_pool(const DevScene &s, const Ray *pool, int n, int *next,
             const float4 na = __ldg(&np->a), nb = __ldg(&np->b), nc = __ldg(&np->c);
             const int4 ch = __ldg(&np->d);
             float tl, tr;
-            const f3 lmin = mk(na.x, na.y, na.z), lmax = mk(na.w, nb.x, nb.y);
-            const f3 rmin = mk(nb.z, nb.w, nc.x), rmax = mk(nc.y, nc.z, nc.w);
-            // both filtered tests first (independent, so they overlap), then
-            // the rare exact retests
-            int fl = fast ? box_filtered(o, inv, lmin, lmax, tl) : -1;
-            int fr = fast ? box_filtered(o, inv, rmin, rmax, tr) : -1;
-            if (fl < 0) fl = box_hit(o, d, lmin, lmax, tl) ? 1 : 0;
-            if (fr < 0) fr = box_hit(o, d, rmin, rmax, tr) ? 1 : 0;
+            // both filtered tests at once, then the rare exact retests
+            int fl = -1, fr = -1;
+            if (fast) boxes_filtered(o, inv, na, nb, nc, fl, fr, tl, tr);
+            if (fl < 0) fl = box_hit(o, d, mk(na.x, nb.x, nc.x), mk(na.z, nb.z, nc.z), tl) ? 1 : 0;
+            if (fr < 0) fr = box_hit(o, d, mk(na.y, nb.y, nc.y), mk(na.w, nb.w, nc.w), tr) ? 1 : 0;
             const bool hl = fl != 0, hr = fr != 0;
             if (hl && ch.x < 0) leaf0 = ~ch.x;
             if (hr && ch.y < 0) {
