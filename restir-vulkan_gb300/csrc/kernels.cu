@@ -490,8 +490,11 @@ __device__ __forceinline__ void spatial_biased_tile(const SpatialParams &p, int 
     store_resv(p.out, i, r);
 }
 
+#ifndef RG_BIASED_MIN_BLOCKS
+#define RG_BIASED_MIN_BLOCKS 8
+#endif
 template <int R, bool MIS>
-__global__ void __launch_bounds__(128) k_spatial_biased(const SpatialParams p) {
+__global__ void __launch_bounds__(128, RG_BIASED_MIN_BLOCKS) k_spatial_biased(const SpatialParams p) {
     spatial_biased_tile<R, MIS>(p, blockIdx.x, blockIdx.y);
 }
 

@@ -808,56 +808,171 @@ __global__ void __launch_bounds__(128) k_mlp_dw4(const Dw4Params p) {
 }
 
 // ---------------------------------------------------------------- training helpers
-// Column sums of a row-major [n x c] matrix (bf16 or FP32), added into out[c].
-template <typename T>
-__global__ void k_colsum(const T *a, int n, int c, float *out) {
-    const int col = blockIdx.x * blockDim.x + threadIdx.x;
-    if (col >= c) return;
-    const int r0 = blockIdx.y * 512, r1 = min(n, r0 + 512);
-    float s = 0.0f;
-    for (int r = r0; r < r1; ++r) {
-        if constexpr (sizeof(T) == 2) s += __bfloat162float(a[(size_t)r * c + col]);
-        else s += a[(size_t)r * c + col];
-    }
-    atomicAdd(out + col, s);
-}
-
 struct BackParams {
-    const __nv_bfloat16 *w123;
-    const __nv_bfloat16 *h1, *h2, *h3;
+    const __nv_bfloat16 *w123;        // bf16 W1 | W2 | W3, row-major (row = input)
+    const __nv_bfloat16 *x, *h1, *h2, *h3;
     const float *dh3;
-    float *da1, *da2, *da3;
+    float *gw1, *gw2, *gw3;           // weight gradients (16 x 64, 64 x 64, 64 x 64), added
+    float *gb1, *gb2, *gb3;           // bias gradients, added
     int n;
 };
 
-// dh3 -> da3 -> dh2 -> da2 -> dh1 -> da1, one row per thread, FP32 with the
-// bf16 weights of the forward pass.
-__global__ void __launch_bounds__(128) k_mlp_backward_rows(const BackParams p) {
-    __shared__ float w[2 * mlp::kH * mlp::kH];
-    for (int i = threadIdx.x; i < 2 * mlp::kH * mlp::kH; i += blockDim.x)
-        w[i] = __bfloat162float(p.w123[mlp::kIn * mlp::kH + i]);
-    __syncthreads();
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= p.n) return;
-    const float *w2 = w, *w3 = w + mlp::kH * mlp::kH;
-    float da[mlp::kH], db[mlp::kH];
-    for (int j = 0; j < mlp::kH; ++j) {
-        const size_t i = (size_t)r * mlp::kH + j;
-        da[j] = __bfloat162float(p.h3[i]) > 0.0f ? p.dh3[i] : 0.0f;
-        p.da3[i] = da[j];
+constexpr int kTileStride = 68;  // floats per row of the row tiles (16-byte rows, conflict-free)
+// W2^T, W3^T, the da tile and the layer-input tile (128 rows each)
+constexpr int kBackSmem = (2 * mlp::kH * mlp::kH + 2 * 128 * kTileStride) * 4;
+
+// One row per thread: dh_{l-1} = W_l da_l for 16 outputs at a time, the
+// weights W_l^T in shared memory (row k: W_l[0..63][k]) read as broadcast
+// float4s, the products as packed FP32x2 FMAs.
+__device__ __forceinline__ void back_matvec(const float *wt, const float (&da)[mlp::kH], int i0, float (&o)[16]) {
+    float2 acc[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[j] = make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int k = 0; k < mlp::kH; ++k) {
+        const float2 d = make_float2(da[k], da[k]);
+        const float4 *w = reinterpret_cast<const float4 *>(wt + k * mlp::kH + i0);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float4 w4 = w[j];
+            acc[2 * j] = __ffma2_rn(make_float2(w4.x, w4.y), d, acc[2 * j]);
+            acc[2 * j + 1] = __ffma2_rn(make_float2(w4.z, w4.w), d, acc[2 * j + 1]);
+        }
     }
-    for (int i = 0; i < mlp::kH; ++i) {  // dh2_i = sum_k W3[i][k] da3_k
-        float acc = 0.0f;
-#pragma unroll 16
-        for (int k = 0; k < mlp::kH; ++k) acc += w3[i * mlp::kH + k] * da[k];
-        db[i] = __bfloat162float(p.h2[(size_t)r * mlp::kH + i]) > 0.0f ? acc : 0.0f;
-        p.da2[(size_t)r * mlp::kH + i] = db[i];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        o[2 * j] = acc[j].x;
+        o[2 * j + 1] = acc[j].y;
     }
-    for (int i = 0; i < mlp::kH; ++i) {
-        float acc = 0.0f;
-#pragma unroll 16
-        for (int k = 0; k < mlp::kH; ++k) acc += w2[i * mlp::kH + k] * db[k];
-        p.da1[(size_t)r * mlp::kH + i] = __bfloat162float(p.h1[(size_t)r * mlp::kH + i]) > 0.0f ? acc : 0.0f;
+}
+
+template <int W>
+__device__ __forceinline__ void load_bf16_row(const __nv_bfloat16 *src, float (&v)[W]) {
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+#pragma unroll
+    for (int j = 0; j < W / 8; ++j) {
+        const uint4 w = s4[j];
+        const __nv_bfloat162 *b = reinterpret_cast<const __nv_bfloat162 *>(&w);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const float2 f = __bfloat1622float2(b[i]);
+            v[8 * j + 2 * i] = f.x;
+            v[8 * j + 2 * i + 1] = f.y;
+        }
+    }
+}
+
+// gW[i][k0 .. k0 + 2*NP) += sum over the tile's rows of in[r][i] * da[r][k]
+template <int NP>
+__device__ __forceinline__ void tile_outer(const float *in_t, const float *da_t, int i, int k0, float *gw) {
+    float2 acc[NP];
+#pragma unroll
+    for (int j = 0; j < NP; ++j) acc[j] = make_float2(0.0f, 0.0f);
+#pragma unroll 4
+    for (int r = 0; r < 128; ++r) {
+        const float a = in_t[r * kTileStride + i];
+        const float2 a2 = make_float2(a, a);
+        const float4 *d = reinterpret_cast<const float4 *>(da_t + r * kTileStride + k0);
+#pragma unroll
+        for (int j = 0; j < NP / 2; ++j) {
+            const float4 d4 = d[j];
+            acc[2 * j] = __ffma2_rn(a2, make_float2(d4.x, d4.y), acc[2 * j]);
+            acc[2 * j + 1] = __ffma2_rn(a2, make_float2(d4.z, d4.w), acc[2 * j + 1]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NP; ++j) {
+        atomicAdd(gw + i * mlp::kH + k0 + 2 * j, acc[j].x);
+        atomicAdd(gw + i * mlp::kH + k0 + 2 * j + 1, acc[j].y);
+    }
+}
+
+// The hidden layers' backward pass for 128 rows per block, one row per
+// thread: da3 = dh3 relu'(h3); for l = 3, 2, 1: db_l += column sums of da_l,
+// dW_l += in_l^T da_l (in_3 = h2, in_2 = h1, in_1 = x; from tiles of the
+// block's rows in shared memory), and da_{l-1} = (W_l da_l) relu'(h_{l-1}),
+// FP32 with the bf16 weights of the forward pass.  The weight and bias
+// gradients are added to the output with atomics, once per block.
+__global__ void __launch_bounds__(128, 2) k_mlp_backward_rows(const BackParams p) {
+    extern __shared__ __align__(16) float bsm[];
+    float *wt2 = bsm, *wt3 = bsm + mlp::kH * mlp::kH;
+    float *dt = bsm + 2 * mlp::kH * mlp::kH, *it = dt + 128 * kTileStride;  // da tile, layer-input tile
+    for (int e = threadIdx.x; e < 2 * mlp::kH * mlp::kH; e += blockDim.x) {
+        const int layer = e / (mlp::kH * mlp::kH), f = e % (mlp::kH * mlp::kH);
+        const int i = f / mlp::kH, k = f % mlp::kH;  // W[i][k]
+        (layer ? wt3 : wt2)[k * mlp::kH + i] = __bfloat162float(p.w123[mlp::kIn * mlp::kH + e]);
+    }
+    const int t = threadIdx.x;
+    const int r = blockIdx.x * blockDim.x + t;
+    const bool valid = r < p.n;
+    const size_t ro = (size_t)(valid ? r : 0) * mlp::kH;
+    float da[mlp::kH];
+    if (valid) {
+        float h[mlp::kH];
+        load_bf16_row(p.h3 + ro, h);
+        const float4 *g = reinterpret_cast<const float4 *>(p.dh3 + ro);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const float4 v = g[j];
+            da[4 * j] = h[4 * j] > 0.0f ? v.x : 0.0f;
+            da[4 * j + 1] = h[4 * j + 1] > 0.0f ? v.y : 0.0f;
+            da[4 * j + 2] = h[4 * j + 2] > 0.0f ? v.z : 0.0f;
+            da[4 * j + 3] = h[4 * j + 3] > 0.0f ? v.w : 0.0f;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < mlp::kH; ++j) da[j] = 0.0f;
+    }
+#pragma unroll 1
+    for (int layer = 3; layer >= 1; --layer) {
+        float hin[mlp::kH];  // this layer's input row (x uses the first 16)
+        if (layer > 1) {
+            if (valid) load_bf16_row(layer == 3 ? p.h2 + ro : p.h1 + ro, hin);
+            else
+#pragma unroll
+                for (int j = 0; j < mlp::kH; ++j) hin[j] = 0.0f;
+        } else {
+            float x[mlp::kIn];
+            if (valid) load_bf16_row(p.x + (size_t)r * mlp::kIn, x);
+            else
+#pragma unroll
+                for (int j = 0; j < mlp::kIn; ++j) x[j] = 0.0f;
+#pragma unroll
+            for (int j = 0; j < mlp::kH; ++j) hin[j] = j < mlp::kIn ? x[j] : 0.0f;
+        }
+        __syncthreads();  // the previous layer's tiles are no longer read (first pass: the weights are in)
+        float4 *drow = reinterpret_cast<float4 *>(dt + t * kTileStride);
+        float4 *irow = reinterpret_cast<float4 *>(it + t * kTileStride);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            drow[j] = make_float4(da[4 * j], da[4 * j + 1], da[4 * j + 2], da[4 * j + 3]);
+            irow[j] = make_float4(hin[4 * j], hin[4 * j + 1], hin[4 * j + 2], hin[4 * j + 3]);
+        }
+        __syncthreads();
+        {  // db_l: thread t sums half the rows of column t % 64
+            const int col = t & 63, half = t >> 6;
+            float sum = 0.0f;
+#pragma unroll 8
+            for (int q = 0; q < 64; ++q) sum += dt[(half * 64 + q) * kTileStride + col];
+            atomicAdd((layer == 3 ? p.gb3 : layer == 2 ? p.gb2 : p.gb1) + col, sum);
+        }
+        if (layer > 1) {
+            tile_outer<16>(it, dt, t >> 1, (t & 1) * 32, layer == 3 ? p.gw3 : p.gw2);
+            float nx[mlp::kH];
+            const float *wt = layer == 3 ? wt3 : wt2;
+            const float *own = it + t * kTileStride;  // this row's input: the ReLU mask
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                float o[16];
+                back_matvec(wt, da, 16 * c, o);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) nx[16 * c + j] = own[16 * c + j] > 0.0f ? o[j] : 0.0f;
+            }
+#pragma unroll
+            for (int j = 0; j < mlp::kH; ++j) da[j] = nx[j];
+        } else {
+            tile_outer<4>(it, dt, t >> 3, (t & 7) * 8, p.gw1);
+        }
     }
 }
 
@@ -1037,19 +1152,12 @@ cudaError_t dw4(const ProposalDev &pd, const __nv_bfloat16 *h3, const float4 *st
     return cudaGetLastError();
 }
 
-cudaError_t colsum_bf16(const __nv_bfloat16 *a, int n, int c, float *out, cudaStream_t st) {
-    if (n > 0) k_colsum<__nv_bfloat16><<<dim3((c + 127) / 128, (n + 511) / 512), 128, 0, st>>>(a, n, c, out);
-    return cudaGetLastError();
-}
-cudaError_t colsum_f32(const float *a, int n, int c, float *out, cudaStream_t st) {
-    if (n > 0) k_colsum<float><<<dim3((c + 127) / 128, (n + 511) / 512), 128, 0, st>>>(a, n, c, out);
-    return cudaGetLastError();
-}
-
-cudaError_t backward_rows(const __nv_bfloat16 *w123, const TrainBuffers &t, const float *dh3, float *da1, float *da2,
-                          float *da3, int n, cudaStream_t st) {
-    BackParams p{w123, t.h1, t.h2, t.h3, dh3, da1, da2, da3, n};
-    if (n > 0) k_mlp_backward_rows<<<(n + 127) / 128, 128, 0, st>>>(p);
+cudaError_t backward_rows(const __nv_bfloat16 *w123, const TrainBuffers &t, const float *dh3, float *gw1, float *gw2,
+                          float *gw3, float *gb1, float *gb2, float *gb3, int n, cudaStream_t st) {
+    BackParams p{w123, t.x, t.h1, t.h2, t.h3, dh3, gw1, gw2, gw3, gb1, gb2, gb3, n};
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_backward_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, kBackSmem);
+    if (e != cudaSuccess) return e;
+    if (n > 0) k_mlp_backward_rows<<<(n + 127) / 128, 128, kBackSmem, st>>>(p);
     return cudaGetLastError();
 }
 

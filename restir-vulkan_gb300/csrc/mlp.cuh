@@ -132,10 +132,10 @@ cudaError_t forward_grad(const ProposalDev &pd, const GBufView &g, const float c
 // Adds dW4 (64 x C) and db4 of the mean loss to gw4 / gb4.
 cudaError_t dw4(const ProposalDev &pd, const __nv_bfloat16 *h3, const float4 *stat, const int32_t *target, int n,
                 float inv_n, float *gw4, float *gb4, int *err, cudaStream_t st);
-cudaError_t colsum_bf16(const __nv_bfloat16 *a, int n, int c, float *out, cudaStream_t st);
-cudaError_t colsum_f32(const float *a, int n, int c, float *out, cudaStream_t st);
-cudaError_t backward_rows(const __nv_bfloat16 *w123, const TrainBuffers &t, const float *dh3, float *da1, float *da2,
-                          float *da3, int n, cudaStream_t st);
+// The hidden layers' weight and bias gradients from dh3, added to gw1..gw3
+// (row-major, row = input) and gb1..gb3.
+cudaError_t backward_rows(const __nv_bfloat16 *w123, const TrainBuffers &t, const float *dh3, float *gw1, float *gw2,
+                          float *gw3, float *gb1, float *gb2, float *gb3, int n, cudaStream_t st);
 cudaError_t adam(float *w, const float *g, float *m, float *v, size_t n, float lr, int step, int c, cudaStream_t st);
 cudaError_t refresh(const float *params, int c, const uint8_t *valid, __nv_bfloat16 *w123img, __nv_bfloat16 *w4t,
                     __nv_bfloat16 *w4k, __nv_bfloat16 *w123, __nv_bfloat16 *w4, float *b4e, cudaStream_t st);

@@ -81,7 +81,7 @@ struct ProposalState {
     int32_t *rows = nullptr, *target = nullptr;
     float4 *tstat = nullptr;
     __nv_bfloat16 *x = nullptr, *h1 = nullptr, *h2 = nullptr, *h3 = nullptr;
-    float *dh3 = nullptr, *da1 = nullptr, *da2 = nullptr, *da3 = nullptr;
+    float *dh3 = nullptr;
     float *loss = nullptr;
     int *count = nullptr;
     bool has_loss = false;
@@ -106,7 +106,7 @@ struct ProposalState {
     }
     void release_train() {
         release(rows); release(target); release(tstat); release(x); release(h1); release(h2); release(h3);
-        release(dh3); release(da1); release(da2); release(da3);
+        release(dh3);
         train_cap = 0;
     }
     void release_all() {
@@ -153,9 +153,6 @@ int ensure_train(ProposalState &ps, int n) {
     if (e == cudaSuccess) e = alloc(&ps.h2, nn * mlp::kH);
     if (e == cudaSuccess) e = alloc(&ps.h3, nn * mlp::kH);
     if (e == cudaSuccess) e = alloc(&ps.dh3, nn * mlp::kH);
-    if (e == cudaSuccess) e = alloc(&ps.da1, nn * mlp::kH);
-    if (e == cudaSuccess) e = alloc(&ps.da2, nn * mlp::kH);
-    if (e == cudaSuccess) e = alloc(&ps.da3, nn * mlp::kH);
     if (e != cudaSuccess) {
         ps.release_train();
         return pcuda(e, "proposal training buffers");
@@ -172,11 +169,6 @@ int check_gbuf(const rg_gbuffer *g) {
     return RG_OK;
 }
 
-int splits_for(int k) {
-    const int chunks = (k + 63) / 64;
-    return chunks < 152 ? chunks : 152;
-}
-
 // Gradient of the mean loss over ps.rows/ps.target[0..n) into ps.grad.
 int gradients(ProposalState &ps, const GBufView &g, const float cam[3], int n, cudaStream_t st) {
     const mlp::ProposalDev pd = ps.dev();
@@ -190,21 +182,10 @@ int gradients(ProposalState &ps, const GBufView &g, const float cam[3], int n, c
             "proposal logits gradient");
     PR_CUDA(mlp::dw4(pd, ps.h3, ps.tstat, ps.target, n, 1.0f / (float)n, ps.grad + L.w4, ps.grad + L.b4, ps.err, st),
             "dW4");
-    const int sp = splits_for(n);
-    PR_CUDA(mlp::backward_rows(ps.w123, tb, ps.dh3, ps.da1, ps.da2, ps.da3, n, st), "hidden backward");
-    // dW3 = h2^T da3, dW2 = h1^T da2, dW1 = x^T da1, and the bias sums
-    PR_CUDA(launch_gemm_tc(ps.h2, 0, 1, mlp::kH, mlp::kH, ps.da3, 1, 1, mlp::kH, mlp::kH, n, ps.grad + L.w3, mlp::kH,
-                           1, 1.0f, sp, ps.err, st),
-            "dW3");
-    PR_CUDA(launch_gemm_tc(ps.h1, 0, 1, mlp::kH, mlp::kH, ps.da2, 1, 1, mlp::kH, mlp::kH, n, ps.grad + L.w2, mlp::kH,
-                           1, 1.0f, sp, ps.err, st),
-            "dW2");
-    PR_CUDA(launch_gemm_tc(ps.x, 0, 1, mlp::kIn, mlp::kIn, ps.da1, 1, 1, mlp::kH, mlp::kH, n, ps.grad + L.w1, mlp::kH,
-                           1, 1.0f, sp, ps.err, st),
-            "dW1");
-    PR_CUDA(mlp::colsum_f32(ps.da3, n, mlp::kH, ps.grad + L.b3, st), "db3");
-    PR_CUDA(mlp::colsum_f32(ps.da2, n, mlp::kH, ps.grad + L.b2, st), "db2");
-    PR_CUDA(mlp::colsum_f32(ps.da1, n, mlp::kH, ps.grad + L.b1, st), "db1");
+    // the hidden layers: weight and bias gradients from dh3
+    PR_CUDA(mlp::backward_rows(ps.w123, tb, ps.dh3, ps.grad + L.w1, ps.grad + L.w2, ps.grad + L.w3, ps.grad + L.b1,
+                               ps.grad + L.b2, ps.grad + L.b3, n, st),
+            "hidden backward");
     return RG_OK;
 }
 
