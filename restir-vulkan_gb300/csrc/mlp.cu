@@ -647,10 +647,17 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fused(const FusedParams p) {
 // the chunk's logits z = h3 . W4[:, chunk] on the tensor cores, the bf16
 // gradient dz = (softmax - onehot) / n as in kGrad (same formula, so the same
 // values), then dW[0..63] += h3^T dz and dW[64] += 1^T dz (db4) as one MMA
-// with M = 128 (rows 0..63: h3^T, row 64: ones for the valid rows, rows
-// 65..127: zero) and K = the tile's 128 rows, accumulated in tensor memory;
-// the CTA adds its 65 x 64 result to the gradient with atomics at the end.
-// Both transposed operands are written element-wise into the K-major layout.
+// with M = 128 and K = the tile's 128 rows, accumulated in tensor memory; the
+// CTA adds its 65 x 64 result to the gradient with atomics at the end.
+//
+// No operand is transposed element by element: the h tile (rows x [h3 | 1 |
+// 0], K-major over its 128 columns) and the dz tile (rows x clusters, K-major
+// over clusters) are read a second time through MN-major descriptors, as
+// [h3 | 1 | 0]^T (M = 128 columns, K = rows) and dz^T (N = clusters, K =
+// rows): in the canonical no-swizzle layouts a core matrix is 8 rows of 16
+// bytes either way, with SBO the step between core matrices along M/N and
+// LBO the step along K.  The tiles sit at the start of a 64 KB allocation, so
+// every address those descriptors can form stays inside it.
 struct Dw4Params {
     mlp::ProposalDev pd;
     const __nv_bfloat16 *h3;   // [n x 64]
@@ -662,13 +669,18 @@ struct Dw4Params {
     int *err;
 };
 
-constexpr int kDwOffBz = 0;                                 // W4^T chunk (64 x 64, K = hidden)
-constexpr int kDwOffH = kDwOffBz + kChunkBytes;             // h3 tile (128 x 64, K = hidden)
-constexpr int kDwOffHt = kDwOffH + kRows * mlp::kH * 2;     // [h3 | 1 | 0]^T (128 x 128, K = rows)
-constexpr int kDwOffDzt = kDwOffHt + 128 * kRows * 2;       // dz^T (64 x 128, K = rows)
-constexpr int kDwSmem = kDwOffDzt + kChunkN * kRows * 2;
+constexpr int kDwHCols = 128;                                // h tile columns: h3 (64) | 1 | 0 ... 0
+constexpr int kDwOffH = 0;                                   // h tile, 128 rows x 128 (K-major, 32 KB)
+constexpr int kDwOffDz = kDwOffH + kRows * kDwHCols * 2;     // dz tile, 128 rows x 64 (K-major, 16 KB)
+constexpr int kDwOffBz = kDwOffDz + kRows * kChunkN * 2;     // W4^T chunk, 64 x 64 (K-major, 8 KB)
+constexpr int kDwSmem = 64 * 1024;
 
-__global__ void __launch_bounds__(128) k_mlp_dw4(const Dw4Params p) {
+// kind::f16 instruction descriptor with both operands MN-major (bits 15, 16)
+__device__ __forceinline__ uint32_t idesc_mn_major(int m, int n) {
+    return umma::idesc_bf16_f32(m, n) | (1u << 15) | (1u << 16);
+}
+
+__global__ void __launch_bounds__(128, 3) k_mlp_dw4(const Dw4Params p) {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ uint64_t mbar_z, mbar_w;
     __shared__ uint32_t tmem_base;
@@ -676,11 +688,19 @@ __global__ void __launch_bounds__(128) k_mlp_dw4(const Dw4Params p) {
     const int chunk = blockIdx.x;
     const int t0 = blockIdx.y * p.tiles_per_slice;
     const int t1 = min((p.n + kRows - 1) / kRows, t0 + p.tiles_per_slice);
-    unsigned char *bz = smem + kDwOffBz, *ht = smem + kDwOffH, *htt = smem + kDwOffHt, *dzt = smem + kDwOffDzt;
+    unsigned char *ht = smem + kDwOffH, *dzt = smem + kDwOffDz, *bz = smem + kDwOffBz;
     copy_bytes(bz, reinterpret_cast<const unsigned char *>(p.pd.w4t) + (size_t)chunk * kChunkBytes, kChunkBytes);
     cp_async_commit();
-    for (int i = tid; i < 128 * kRows / 8; i += blockDim.x)  // zero [h3 | 1 | 0]^T (rows 65..127 stay zero)
-        reinterpret_cast<uint4 *>(htt)[i] = make_uint4(0, 0, 0, 0);
+    {  // this thread's row of the h tile, columns 64..127: 1 (the db4 row of the product), then zeros
+        __align__(16) __nv_bfloat16 one[8];
+        one[0] = __float2bfloat16_rn(1.0f);
+#pragma unroll
+        for (int i = 1; i < 8; ++i) one[i] = __float2bfloat16_rn(0.0f);
+        *reinterpret_cast<uint4 *>(ht + umma::kmajor_offset(tid, 64, kDwHCols)) = *reinterpret_cast<const uint4 *>(one);
+#pragma unroll
+        for (int j = 72; j < kDwHCols; j += 8)
+            *reinterpret_cast<uint4 *>(ht + umma::kmajor_offset(tid, j, kDwHCols)) = make_uint4(0, 0, 0, 0);
+    }
     if (warp == 0) umma::tmem_alloc(&tmem_base, 128);
     if (tid == 0) {
         umma::mbar_init(&mbar_z, 1);
@@ -696,45 +716,34 @@ __global__ void __launch_bounds__(128) k_mlp_dw4(const Dw4Params p) {
     uint64_t *last_mbar = nullptr;
     uint32_t last_parity = 0;
     const float4 *be = reinterpret_cast<const float4 *>(p.pd.b4e + chunk * kChunkN);
+    const uint32_t ht_a = umma::smem_addr(ht), dz_a = umma::smem_addr(dzt), bz_a = umma::smem_addr(bz);
     for (int t = t0; t < t1 && ok; ++t) {
         const int k = t - t0;
         if (k > 0) ok_warp = ok_warp && mma_wait(&mbar_w, (uint32_t)((k - 1) & 1));  // previous tile's operands free
         const int row = t * kRows + tid;
         const bool valid = row < p.n;
-        float h[64];
         if (valid) {
-            const uint4 *src = reinterpret_cast<const uint4 *>(p.h3 + (size_t)row * mlp::kH);
+            const unsigned char *src = reinterpret_cast<const unsigned char *>(p.h3 + (size_t)row * mlp::kH);
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const uint4 w = src[j];
-                *reinterpret_cast<uint4 *>(ht + umma::kmajor_offset(tid, 8 * j, mlp::kH)) = w;
-                const __nv_bfloat162 *b = reinterpret_cast<const __nv_bfloat162 *>(&w);
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const float2 f = __bfloat1622float2(b[i]);
-                    h[8 * j + 2 * i] = f.x;
-                    h[8 * j + 2 * i + 1] = f.y;
-                }
-            }
+            for (int j = 0; j < 8; ++j) cp_async16(ht + umma::kmajor_offset(tid, 8 * j, kDwHCols), src + 16 * j);
         } else {
 #pragma unroll
-            for (int j = 0; j < 64; ++j) h[j] = 0.0f;
-#pragma unroll
             for (int j = 0; j < 8; ++j)
-                *reinterpret_cast<uint4 *>(ht + umma::kmajor_offset(tid, 8 * j, mlp::kH)) = make_uint4(0, 0, 0, 0);
+                *reinterpret_cast<uint4 *>(ht + umma::kmajor_offset(tid, 8 * j, kDwHCols)) = make_uint4(0, 0, 0, 0);
         }
-#pragma unroll
-        for (int j = 0; j < 64; ++j)
-            *reinterpret_cast<__nv_bfloat16 *>(htt + umma::kmajor_offset(j, tid, kRows)) = __float2bfloat16_rn(h[j]);
-        *reinterpret_cast<__nv_bfloat16 *>(htt + umma::kmajor_offset(64, tid, kRows)) =
-            __float2bfloat16_rn(valid ? 1.0f : 0.0f);
+        cp_async_commit();
+        cp_async_wait_all();
         umma::fence_proxy_async();
         umma::fence_before_sync();
         ok = __syncthreads_and(ok_warp) != 0;
         umma::fence_after_sync();
         if (!ok) break;
-        if (tid == 0) {
-            umma::mma_chunk(tmem, ht, bz, mlp::kH, kRows, kChunkN, false);
+        if (tid == 0) {  // z = h3 . W4[:, chunk]: A = h tile (K-major, first 64 columns), B = W4^T chunk
+            const uint32_t idesc = umma::idesc_bf16_f32(kRows, kChunkN);
+#pragma unroll
+            for (int ks = 0; ks < mlp::kH / 16; ++ks)
+                umma::mma_bf16(tmem, umma::smem_desc(ht_a + (uint32_t)ks * 256u, 128u, (kDwHCols / 8) * 128u),
+                               umma::smem_desc(bz_a + (uint32_t)ks * 256u, 128u, (mlp::kH / 8) * 128u), idesc, ks > 0);
             umma::mma_commit(&mbar_z);
             last_mbar = &mbar_z;
             last_parity = (uint32_t)(k & 1);
@@ -758,14 +767,15 @@ __global__ void __launch_bounds__(128) k_mlp_dw4(const Dw4Params p) {
                     const float4 b = __ldg(be + piece * 8 + q);
                     v[4 * q] += b.x; v[4 * q + 1] += b.y; v[4 * q + 2] += b.z; v[4 * q + 3] += b.w;
                 }
+                float d[32];
 #pragma unroll
                 for (int i = 0; i < 32; ++i) {
                     const int col = chunk * kChunkN + piece * 32 + i;
                     const float pr = ex2(__fmaf_rn(v[i], kLog2e, nl2));
-                    const float d = target < 0 ? 0.0f : (pr - (col == target ? 1.0f : 0.0f)) * p.inv_n;
-                    *reinterpret_cast<__nv_bfloat16 *>(dzt + umma::kmajor_offset(piece * 32 + i, tid, kRows)) =
-                        __float2bfloat16_rn(d);
+                    d[i] = target < 0 ? 0.0f : (pr - (col == target ? 1.0f : 0.0f)) * p.inv_n;
                 }
+#pragma unroll
+                for (int q = 0; q < 32; q += 8) put8(dzt, tid, piece * 32 + q, kChunkN, d + q);
             }
         }
         umma::fence_proxy_async();
@@ -774,7 +784,15 @@ __global__ void __launch_bounds__(128) k_mlp_dw4(const Dw4Params p) {
         umma::fence_after_sync();
         if (!ok) break;
         if (tid == 0) {
-            umma::mma_chunk(tmem + 64, htt, dzt, kRows, 128, kChunkN, k > 0);
+            // dW += [h3 | 1 | 0]^T dz: both tiles through MN-major descriptors,
+            // K = the tile's rows in steps of 16 (two core matrices along K)
+            const uint32_t idesc = idesc_mn_major(128, kChunkN);
+            constexpr uint32_t lbo_h = 8 * kDwHCols * 2, lbo_dz = 8 * kChunkN * 2;  // K step: 8 rows of a tile
+#pragma unroll
+            for (int ks = 0; ks < kRows / 16; ++ks)
+                umma::mma_bf16(tmem + 64, umma::smem_desc(ht_a + (uint32_t)ks * 2u * lbo_h, lbo_h, 128u),
+                               umma::smem_desc(dz_a + (uint32_t)ks * 2u * lbo_dz, lbo_dz, 128u), idesc,
+                               k > 0 || ks > 0);
             umma::mma_commit(&mbar_w);
             last_mbar = &mbar_w;
             last_parity = (uint32_t)(k & 1);
