@@ -108,7 +108,7 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
     return y;
 }
 
-// The decision of box_filtered from a box's slab distances.
+// The filtered test's decision from a box's slab distances.
 __device__ __forceinline__ int filtered_decision(float rmin, float rmax) {
     constexpr float kEps = 1.9073486328125e-6f;     // 2^-19
     constexpr float kTiny = 8.0779356694631609e-28f; // 2^-90
