@@ -216,7 +216,10 @@ __device__ __forceinline__ void count_block_rays(const DevScene &s, int rays, co
 #define RG_SMEM_CARVEOUT -1
 #endif
 
-constexpr int kRisPpt = 4;  // pixels per thread of the single-view launch (the batched one is tuned)
+#ifndef RG_RIS_PPT
+#define RG_RIS_PPT 4
+#endif
+constexpr int kRisPpt = RG_RIS_PPT;  // pixels per thread of the single-view launch (the batched one is tuned)
 
 struct InitialParams {
     DevScene s;
