@@ -165,6 +165,28 @@ __device__ __forceinline__ void add_sample(ResV<R, MIS> &r, float4 pos_lum, floa
         update_at(r, j, weight, pos_lum, nrm, idx, p_hat, w, p_hat, rng);
     }
 }
+// add_sample with the reservoir-update uniforms drawn beforehand (u[j] is the
+// draw update_at would take for sample j): the same arithmetic.
+template <int R, bool MIS>
+__device__ __forceinline__ void add_sample_u(ResV<R, MIS> &r, float4 pos_lum, float4 nrm, int32_t idx, float p_hat,
+                                             float sample_p, const float (&u)[R]) {
+    const float weight = p_hat / sample_p;
+    r.m += 1u;
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        const float w = (r.sum_w[j] + weight) / ((float)r.m * p_hat);
+        r.sum_w[j] += weight;
+        const float replace = weight / r.sum_w[j];
+        if (u[j] < replace) {
+            r.pos_lum[j] = pos_lum;
+            r.nrm[j] = nrm;
+            r.idx[j] = idx;
+            r.p_hat[j] = p_hat;
+            r.w[j] = w;
+            if (MIS) r.sum_phat[j] += p_hat;
+        }
+    }
+}
 // reservoir.glsl:44-64.  With MIS the reference passes other's sumPHat where
 // updateReservoirAt takes w and other's w where it takes sumPHat (:55-60);
 // RG_FLAG_MIS_SWAP_FIX passes them in the declared order instead.
@@ -245,6 +267,53 @@ __device__ __forceinline__ ResV<R, MIS> ris(const DevScene &s, const Texel &t, f
     if (zero_normal) return r;
     const f3 wo = view_dir(cam, t.wpos);
     const int count = s.n_alias;
+    if (!lr.cand && s.n_point_lights != 0 && count_c > 0) {
+        // The plain point-light proposal with a one-candidate lookahead.  A
+        // candidate's draws are always r1, r2 and then one reservoir-update
+        // uniform per sample, so the next candidate's r1, r2 (and its
+        // alias-table column, both lights' positions loaded unconditionally)
+        // are taken right after this candidate's update uniforms, and the
+        // gather runs under this candidate's p-hat: same draws, same order,
+        // same arithmetic as the loop below.
+        float r1 = rand_float(rng), r2 = rand_float(rng);
+        int col = imin((int)((float)count * r1), count - 1);
+        float4 cc = __ldg(&s.alias[col].col), own = __ldg(&s.alias[col].own_pos), ali = __ldg(&s.alias[col].alias_pos);
+        const float4 nrm0 = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (uint32_t c = 0; c < count_c; ++c) {
+            float u[R];
+#pragma unroll
+            for (int j = 0; j < R; ++j) u[j] = rand_float(rng);
+            float r2n = 0.0f;
+            int coln = 0;
+            float4 ccn = cc, ownn = own, alin = ali;
+            if (c + 1 < count_c) {
+                const float r1n = rand_float(rng);
+                r2n = rand_float(rng);
+                coln = imin((int)((float)count * r1n), count - 1);
+                ccn = __ldg(&s.alias[coln].col);
+                ownn = __ldg(&s.alias[coln].own_pos);
+                alin = __ldg(&s.alias[coln].alias_pos);
+            }
+            const bool keep = cc.x > r2;  // restirOmni.glsl:73-83
+            const float4 pos_lum = keep ? own : ali;
+            const float prob = keep ? cc.z : cc.w;
+            const int32_t lidx = keep ? col : __float_as_int(cc.y);
+            const float ph = eval_phat_wo(t.wpos, xyz(pos_lum), wo, t.normal, xyz(nrm0), false, albedo_lum,
+                                          pos_lum.w, t.roughness, t.metallic);
+            add_sample_u(r, pos_lum, nrm0, lidx, ph, prob, u);
+            r2 = r2n;
+            col = coln;
+            cc = ccn;
+            own = ownn;
+            ali = alin;
+        }
+        if (flags & RG_FLAG_FINAL_RIS_WEIGHT) {
+#pragma unroll
+            for (int j = 0; j < R; ++j)
+                if (r.sum_w[j] > 0.0f) r.w[j] = r.sum_w[j] / ((float)r.m * r.p_hat[j]);
+        }
+        return r;
+    }
     for (uint32_t c = 0; c < count_c; ++c) {
         const float r1 = rand_float(rng), r2 = rand_float(rng);
         const int col = imin((int)((float)count * r1), count - 1);  // restirOmni.glsl:73-83
