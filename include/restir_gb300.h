@@ -279,7 +279,7 @@ int rg_render_frame_host(rg_context *ctx, int32_t width, int32_t height, const u
                          const uint16_t *normal, const uint16_t *material, const float *world_pos,
                          const float *depth, const rg_frame_params *params, float *rgba_out_host, void *stream);
 
-/* ---- tensor-core GEMM (used by the learned proposal's training) ----
+/* ---- tensor-core GEMM (a general utility of the library) ----
  * D = alpha * A . B^T, or D += alpha * A . B^T with accumulate != 0 (always
  * atomic when k_splits > 1).  A is m x k and B is n x k, read from device
  * memory with the given element strides of (row, k), as bf16 or, with
