@@ -77,7 +77,8 @@ def _arm(ctx, s, dg, res, image, crop, judge, frames, learned, steps_per_frame, 
 
 
 def run(width=1920, height=1080, frames=64, clusters=4096, n_tris=100_000, n_lights=65_536, crop_size=64,
-        lr=3e-3, steps_per_frame=1, batch=65_536, kmeans_iters=8, seed=4, log=print, learned_candidates=32):
+        lr=3e-3, steps_per_frame=1, batch=65_536, kmeans_iters=8, seed=4, log=print, learned_candidates=32,
+        zero_w4=False):
     import torch
 
     import oracle_binding as ob
@@ -106,6 +107,11 @@ def run(width=1920, height=1080, frames=64, clusters=4096, n_tris=100_000, n_lig
     _arm(ctx, s, dg, res, image, crop, judge, 2, False, 1)
     plain_ms, plain_rmse, _ = _arm(ctx, s, dg, res, image, crop, judge, frames, False, 1)
     ctx.create_proposal(cluster_of, clusters, mix=0.9, learning_rate=lr, batch=batch, seed=seed)
+    if zero_w4:  # the untrained proposal is then exactly the power-proportional one (plus the mixture)
+        params = ctx.proposal_params()
+        n123 = 16 * 64 + 64 + 2 * (64 * 64 + 64)
+        params[n123:n123 + 64 * clusters] = 0.0
+        ctx.set_proposal_params(params)
     lrn_ms, lrn_rmse, loss = _arm(ctx, s, dg, res, image, crop, judge, frames, True, steps_per_frame,
                                   learned_candidates)
     st = ctx.stats()
@@ -152,10 +158,12 @@ def main(argv=None):
     ap.add_argument("--steps-per-frame", type=int, default=1)
     ap.add_argument("--batch", type=int, default=65_536)
     ap.add_argument("--learned-candidates", type=int, default=32, help="RIS candidates of the learned arm")
+    ap.add_argument("--zero-w4", action="store_true", help="start the learned arm with W4 = 0")
     ap.add_argument("--out", default=None, help="also write the JSON here")
     a = ap.parse_args(argv)
     r = run(a.width, a.height, a.frames, a.clusters, a.tris, a.lights, a.crop, a.lr, a.steps_per_frame, a.batch,
-            log=lambda *x: print(*x, file=sys.stderr, flush=True), learned_candidates=a.learned_candidates)
+            log=lambda *x: print(*x, file=sys.stderr, flush=True), learned_candidates=a.learned_candidates,
+            zero_w4=a.zero_w4)
     txt = json.dumps(r)
     print(txt, flush=True)
     if a.out:
