@@ -8,6 +8,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
 #include <vector>
 
 #include "host_internal.h"
@@ -290,7 +291,7 @@ int rg_proposal_create(rg_context *ctx, const rg_proposal_config *cfg, const rg_
     ProposalState **slot = rg_internal_proposal(ctx);
     proposal_release(*slot);
     *slot = nullptr;
-    static uint64_t generations = 0;
+    static std::atomic<uint64_t> generations{0};  // contexts may live on different host threads
     ProposalState *ps = new ProposalState();
     ps->generation = ++generations;
     ps->c = C;
