@@ -357,6 +357,19 @@ int rg_batch_get_tuning(rg_batch *batch, rg_batch_tuning *tuning);
  * index and overwrite the views' reservoirs), keeps the fastest and returns it
  * with its mean run time. */
 int rg_batch_autotune(rg_batch *batch, int32_t repeats, rg_batch_tuning *best, float *best_ms, void *stream);
+/* Chooses the views' RIS candidate count (initial_light_sample_count) among
+ * counts[0..n_counts) by Monte Carlo efficiency, 1 / (time x variance): per
+ * count, the mean run time over `repeats` runs and the per-pixel variance of
+ * the shaded image's log(1 + luminance) (robust to firefly pixels), from two
+ * runs that start from the same previous-frame reservoirs (half the mean
+ * squared difference of their images).  Unlike the launch shapes, the count
+ * is part of the estimator: the
+ * chosen count stays set on every view (and in captured graphs of later
+ * runs).  Runs advance the frame index and overwrite the views' reservoirs
+ * and images.  ms_per_run and variance (n_counts each) may be null.  Counts
+ * are 1..32 with the learned proposal, else 1..4096. */
+int rg_batch_autotune_candidates(rg_batch *batch, const int32_t *counts, int32_t n_counts, int32_t repeats,
+                                 int32_t *best_count, float *ms_per_run, double *variance, void *stream);
 int rg_batch_destroy(rg_batch *batch);
 
 /* ---- learned light-cluster proposal ----

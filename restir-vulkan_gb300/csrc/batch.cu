@@ -150,6 +150,11 @@ int check_tuning(const rg_batch_tuning &t) {
     return RG_OK;
 }
 
+__global__ void k_set_view_candidates(mlp::ViewRows *v, int n, int32_t count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i].n_cand = count;
+}
+
 int enqueue_run(rg_batch *b, int parity, cudaStream_t st) {
     const int nl = 2 + b->spatial;
     B_CUDA(cudaMemsetAsync(b->counters, 0, (size_t)nl * sizeof(unsigned), st), "rg_batch_run");
@@ -424,6 +429,106 @@ int rg_batch_autotune(rg_batch *b, int32_t repeats, rg_batch_tuning *best_out, f
     if ((rc = rg_batch_set_tuning(b, &best))) return rc;
     if (best_out) *best_out = best;
     if (best_ms) *best_ms = best_t / (float)repeats;
+    return RG_OK;
+}
+
+int rg_batch_autotune_candidates(rg_batch *b, const int32_t *counts, int32_t n_counts, int32_t repeats,
+                                 int32_t *best_count, float *ms_per_run, double *variance, void *stream) {
+    if (!b || !counts || n_counts < 1 || n_counts > 16 || repeats < 1)
+        return bfail(RG_ERR_INVALID_ARGUMENT, "bad arguments");
+    for (int i = 0; i < n_counts; ++i)
+        if (counts[i] < 1 || counts[i] > (b->learned ? mlp::kCand : 4096))
+            return bfail(RG_ERR_INVALID_ARGUMENT, "candidate count %d out of range (1..%d)", counts[i],
+                         b->learned ? mlp::kCand : 4096);
+    B_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
+    cudaStream_t st = (cudaStream_t)stream;
+    // per-view first pixel in one luminance buffer over all views
+    std::vector<long long> first((size_t)b->n);
+    long long total = 0;
+    for (int v = 0; v < b->n; ++v) {
+        first[(size_t)v] = total;
+        total += (long long)b->views[(size_t)v].uniforms.screen_size[0] * b->views[(size_t)v].uniforms.screen_size[1];
+    }
+    float *lum = nullptr;
+    long long *first_d = nullptr;
+    double *acc = nullptr;
+    unsigned *counter = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = RG_OK;
+    auto cleanup = [&]() {
+        if (lum) cudaFree(lum);
+        if (first_d) cudaFree(first_d);
+        if (acc) cudaFree(acc);
+        if (counter) cudaFree(counter);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    };
+    cudaError_t e = cudaMalloc(&lum, (size_t)total * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&first_d, (size_t)b->n * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMemcpy(first_d, first.data(), (size_t)b->n * sizeof(long long), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&acc, 2 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&counter, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e != cudaSuccess) {
+        cleanup();
+        return bcuda(e, "candidate tuning buffers");
+    }
+    auto set_count = [&](int32_t c) -> cudaError_t {
+        cudaError_t r = launch_set_candidates(b->initial[0], b->n, (uint32_t)c, st);
+        if (r == cudaSuccess) r = launch_set_candidates(b->initial[1], b->n, (uint32_t)c, st);
+        if (r == cudaSuccess && b->learned) {
+            k_set_view_candidates<<<(b->n + 127) / 128, 128, 0, st>>>(b->mlp_views, b->n, c);
+            r = cudaGetLastError();
+        }
+        return r;
+    };
+    const ViewTiles vt{b->maps[2].view_start, b->maps[2].tiles_x, b->n, b->maps[2].total, counter};
+    double best_eff = -1.0;
+    int32_t best = counts[0];
+    for (int i = 0; i < n_counts && rc == RG_OK; ++i) {
+        if ((e = set_count(counts[i])) != cudaSuccess) { rc = bcuda(e, "candidate count"); break; }
+        if ((rc = enqueue_run(b, 0, st)) || (rc = enqueue_run(b, 1, st))) break;  // settle the reservoirs
+        e = cudaEventRecord(e0, st);
+        for (int k = 0; k < repeats && rc == RG_OK; ++k) rc = enqueue_run(b, k & 1, st);
+        if (rc) break;
+        if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+        // two runs from the same previous-frame reservoirs (parity 0 reads
+        // reservoirs[1], written before): independent estimates of one frame
+        if (e == cudaSuccess) e = cudaMemsetAsync(acc, 0, 2 * sizeof(double), st);
+        if (e != cudaSuccess) { rc = bcuda(e, "candidate tuning"); break; }
+        if ((rc = enqueue_run(b, 1, st))) break;
+        if ((rc = enqueue_run(b, 0, st))) break;
+        e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
+        if (e == cudaSuccess) e = launch_views_luminance(b->shade[0], vt, first_d, lum, 0, acc, b->maps[2].grid, st);
+        if (e != cudaSuccess) { rc = bcuda(e, "luminance"); break; }
+        if ((rc = enqueue_run(b, 0, st))) break;
+        e = cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
+        if (e == cudaSuccess) e = launch_views_luminance(b->shade[0], vt, first_d, lum, 1, acc, b->maps[2].grid, st);
+        double h[2] = {0.0, 0.0};
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        float ms = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e != cudaSuccess) { rc = bcuda(e, "candidate tuning"); break; }
+        ms /= (float)repeats;
+        const double var = h[1] > 0.0 ? h[0] / (2.0 * h[1]) : 0.0;  // E[(a - b)^2] / 2 per pixel
+        if (ms_per_run) ms_per_run[i] = ms;
+        if (variance) variance[i] = var;
+        const double eff = var > 0.0 ? 1.0 / ((double)ms * var) : 1e300 / (double)ms;
+        if (eff > best_eff) {
+            best_eff = eff;
+            best = counts[i];
+        }
+    }
+    if (rc == RG_OK) {
+        if ((e = set_count(best)) != cudaSuccess) rc = bcuda(e, "candidate count");
+        else if ((e = cudaStreamSynchronize(st)) != cudaSuccess) rc = bcuda(e, "candidate tuning");
+    }
+    cleanup();
+    if (rc) return rc;
+    for (auto &v : b->views) v.uniforms.initial_light_sample_count = (uint32_t)best;
+    if (best_count) *best_count = best;
     return RG_OK;
 }
 

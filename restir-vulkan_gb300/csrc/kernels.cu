@@ -883,6 +883,69 @@ __global__ void __launch_bounds__(128) k_shade_views(const ShadeParams *views, c
     for_each_view_tile(views, vt, [](const ShadeParams &p, int bx, int by) { shade_tile<1, false>(p, bx, by); });
 }
 
+// ---- candidate-count tuning of a batch (batch.cu): the views' RIS candidate
+// count, and the luminance of the views' shaded images (a snapshot, then the
+// sum of squared differences to it), over the shading launch's tile map.
+__global__ void k_set_candidates(InitialParams *ip, int n_views, uint32_t count) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < n_views) ip[v].u.initial_light_sample_count = count;
+}
+// The tone value of a pixel: log(1 + luminance), so that a few firefly
+// pixels (heavy-tailed near-field lights) do not dominate the variance.
+// mode 0: lum[first_px[v] + i] = tone value of pixel i of view v; mode 1: adds
+// sum (tone - lum)^2 over finite differences to acc[0] and their count to
+// acc[1]
+__global__ void __launch_bounds__(128) k_views_luminance(const ShadeParams *views, const ViewTiles vt,
+                                                         const long long *first_px, float *lum, int mode,
+                                                         double *acc) {
+    __shared__ int s_item;
+    const int tid = threadIdx.x + threadIdx.y * 32;
+    double sq = 0.0, cnt = 0.0;
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_item = (int)atomicAdd(vt.counter, 1u);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= vt.total) break;
+        int lo = 0, hi = vt.n_views - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(vt.view_start + mid) <= item) lo = mid;
+            else hi = mid - 1;
+        }
+        const int local = item - __ldg(vt.view_start + lo);
+        const int tx = __ldg(vt.tiles_x + lo);
+        const ShadeParams &p = views[lo];
+        const int x = (local % tx) * 32 + threadIdx.x, y = (local / tx) * 4 + threadIdx.y;
+        const int W = (int)p.u.buffer_size[0], H = (int)p.u.buffer_size[1];
+        if (x < W && y < H) {
+            const size_t i = (size_t)y * (size_t)W + (size_t)x;
+            const float4 c = p.out[i];
+            const float l = log1pf(fmaxf(luminance(c.x, c.y, c.z), 0.0f));
+            float *slot = lum + first_px[lo] + (long long)i;
+            if (mode == 0) {
+                *slot = l;
+            } else {
+                const double d = (double)l - (double)*slot;
+                if (isfinite(d)) {
+                    sq += d * d;
+                    cnt += 1.0;
+                }
+            }
+        }
+    }
+    if (mode == 1) {
+        for (int o = 16; o > 0; o >>= 1) {
+            sq += __shfl_xor_sync(0xffffffffu, sq, o);
+            cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        }
+        if ((tid & 31) == 0) {
+            atomicAdd(acc, sq);
+            atomicAdd(acc + 1, cnt);
+        }
+    }
+}
+
 // frame index of every view for the next run: start + (number of runs so far)
 __global__ void k_advance_frames(InitialParams *ip, SpatialParams *sp, int n_views, int n_spatial,
                                  const uint32_t *start_frame, uint32_t *runs, uint32_t *frame_out) {
@@ -1142,6 +1205,20 @@ cudaError_t launch_views_pass(int kind, int variant, bool unbiased, int num_neig
     return with_views_kernel(kind, variant, unbiased, num_neighbors, depth, [&](auto kernel, size_t smem) {
         return views_launch(kernel, params, vt, smem, grid, st);
     });
+}
+
+cudaError_t launch_set_candidates(void *initial_params, int n_views, uint32_t count, cudaStream_t st) {
+    k_set_candidates<<<(n_views + 127) / 128, 128, 0, st>>>(static_cast<InitialParams *>(initial_params), n_views,
+                                                             count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_views_luminance(const void *shade_params, const ViewTiles &vt, const long long *first_px, float *lum,
+                                   int mode, double *acc, int grid, cudaStream_t st) {
+    if (grid < 1) return cudaSuccess;
+    k_views_luminance<<<grid, dim3(32, 4), 0, st>>>(static_cast<const ShadeParams *>(shade_params), vt, first_px, lum,
+                                                    mode, acc);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_advance_frames(void *initial_params, void *spatial_params, int n_views, int n_spatial,

@@ -114,6 +114,13 @@ cudaError_t views_pass_grid(int kind, int variant, bool unbiased, int num_neighb
                             int ctas_per_sm, int *grid);
 cudaError_t launch_views_pass(int kind, int variant, bool unbiased, int num_neighbors, int depth, const void *params,
                               const ViewTiles &vt, int grid, cudaStream_t st);
+// Candidate-count tuning: every view's RIS candidate count; the luminance of
+// the views' shaded images (mode 0: into lum at first_px[v] + pixel; mode 1:
+// acc[0] += sum of squared differences to lum, acc[1] += pixels counted),
+// over the shading tile map (counter zeroed before the launch).
+cudaError_t launch_set_candidates(void *initial_params, int n_views, uint32_t count, cudaStream_t st);
+cudaError_t launch_views_luminance(const void *shade_params, const ViewTiles &vt, const long long *first_px, float *lum,
+                                   int mode, double *acc, int grid, cudaStream_t st);
 // Sets every view's frame index to start_frame[v] + *runs (also into
 // frame_out[v] when frame_out is not null), then adds one to *runs.
 cudaError_t launch_advance_frames(void *initial_params, void *spatial_params, int n_views, int n_spatial,

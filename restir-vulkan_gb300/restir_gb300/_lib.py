@@ -171,6 +171,9 @@ _SIGNATURES = {
     "rg_batch_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(BatchTuning)]),
     "rg_batch_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(BatchTuning), C.POINTER(C.c_float),
                                     C.c_void_p]),
+    "rg_batch_autotune_candidates": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_int32, C.c_int32,
+                                               C.POINTER(C.c_int32), C.POINTER(C.c_float), C.POINTER(C.c_double),
+                                               C.c_void_p]),
     "rg_batch_destroy": (C.c_int, [C.c_void_p]),
     "rg_cluster_lights": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_void_p,
                                     C.c_void_p]),

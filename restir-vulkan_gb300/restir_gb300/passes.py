@@ -301,6 +301,21 @@ class Batch:
         check(lib().rg_batch_autotune(self._h, repeats, C.byref(t), C.byref(ms), _stream_handle(stream)))
         return t, ms.value
 
+    def autotune_candidates(self, counts=(8, 16, 32), repeats: int = 1, stream=None):
+        """Chooses the views' RIS candidate count by Monte Carlo efficiency
+        (rg_batch_autotune_candidates): (chosen count, ms per run, per-pixel
+        variance of log(1 + luminance)) for every count tried."""
+        n = len(counts)
+        c_arr = (C.c_int32 * n)(*counts)
+        ms = (C.c_float * n)()
+        var = (C.c_double * n)()
+        best = C.c_int32()
+        check(lib().rg_batch_autotune_candidates(self._h, c_arr, n, repeats, C.byref(best), ms, var,
+                                                 _stream_handle(stream)))
+        for v in self._keep:
+            v["uniforms"].initial_light_sample_count = best.value
+        return best.value, list(ms), list(var)
+
     def close(self):
         if self._h:
             lib().rg_batch_destroy(self._h)

@@ -5,7 +5,8 @@ Bar: bit-exact.  Every view's reservoirs and shaded image after each run of a
 batch equal those of the single-view pass sequence of rg_render_frame
 (RIS + visibility + temporal, the spatial chain, shading) for that view and
 frame, for every launch-shape tuning, for the unbiased and the biased chains,
-and when the run is replayed from a captured CUDA graph."""
+and when the run is replayed from a captured CUDA graph; with the learned
+proposal; and after the candidate count is chosen by efficiency."""
 from __future__ import annotations
 
 import numpy as np
@@ -199,4 +200,36 @@ def test_batch_learned_guards(ctx, cuda, views5):
     ctx.create_proposal(cluster_of, 256, seed=6)  # a new proposal: the batch's tables are stale
     with pytest.raises(RestirError, match="proposal changed"):
         b.run(0)
+    b.close()
+
+
+@pytest.mark.parametrize("learned", [False, True])
+def test_candidate_tuning_by_efficiency(ctx, cuda, views5, learned):
+    """The tuner times each candidate count, measures the per-pixel variance
+    of one frame from two runs that share their history, keeps the most
+    efficient count, and leaves it set: afterwards every view equals its
+    single-view passes run with that count."""
+    from restir_gb300.passes import Batch, cluster_lights
+    base, views = views5
+    vws, fp = _make(ctx, cuda, base, views, unbiased=True, learned=learned)
+    if learned:
+        cluster_of, _ = cluster_lights(base.point_lights, 256, iterations=4, seed=3)
+        ctx.create_proposal(cluster_of, 256, seed=5)
+    b = Batch(ctx, vws, fp)
+    best, ms, var = b.autotune_candidates((4, 32), repeats=1)
+    assert best in (4, 32)
+    assert all(m > 0 for m in ms)
+    assert var[0] > var[1] > 0  # more candidates, less noise
+    eff = [1.0 / (m * v) for m, v in zip(ms, var)]
+    assert best == (4, 32)[int(np.argmax(eff))]
+    assert all(vw["uniforms"].initial_light_sample_count == best for vw in vws)
+    b.reset_frames()
+    for vw in vws:
+        for k in ("res0", "res1", "tmp"):
+            vw[k].zero_()
+    _compare(ctx, cuda, vws, fp, b, runs=2)
+    if learned:
+        from restir_gb300._lib import RestirError
+        with pytest.raises(RestirError, match="out of range"):
+            b.autotune_candidates((33,))
     b.close()
