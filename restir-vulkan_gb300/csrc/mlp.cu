@@ -658,6 +658,9 @@ __global__ void __launch_bounds__(128, 4) k_mlp_fused(const FusedParams p) {
 // bytes either way, with SBO the step between core matrices along M/N and
 // LBO the step along K.  The tiles sit at the start of a 64 KB allocation, so
 // every address those descriptors can form stays inside it.
+#ifndef RG_DW4_SLICE_CTAS
+#define RG_DW4_SLICE_CTAS 4
+#endif
 struct Dw4Params {
     mlp::ProposalDev pd;
     const __nv_bfloat16 *h3;   // [n x 64]
@@ -1159,8 +1162,8 @@ cudaError_t dw4(const ProposalDev &pd, const __nv_bfloat16 *h3, const float4 *st
     Dw4Params p{pd, h3, stat, target, n, 0, inv_n, gw4, gb4, err};
     const int tiles = (n + kRows - 1) / kRows;
     const int chunks = pd.c / kChunkN;
-    // enough CTAs for about four per SM; each keeps its tiles' sum in tensor memory
-    int slices = (4 * 152 + chunks - 1) / chunks;
+    // about RG_DW4_SLICE_CTAS CTAs per SM in all; each keeps its tiles' sum in tensor memory
+    int slices = (RG_DW4_SLICE_CTAS * 152 + chunks - 1) / chunks;
     if (slices > tiles) slices = tiles;
     p.tiles_per_slice = (tiles + slices - 1) / slices;
     slices = (tiles + p.tiles_per_slice - 1) / p.tiles_per_slice;
