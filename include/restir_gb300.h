@@ -279,6 +279,29 @@ int rg_render_frame_host(rg_context *ctx, int32_t width, int32_t height, const u
                          const uint16_t *normal, const uint16_t *material, const float *world_pos,
                          const float *depth, const rg_frame_params *params, float *rgba_out_host, void *stream);
 
+/* ---- triangle lights of a loaded scene ----
+ * Replaces collectTriangleLightsFromScene (src/misc.cpp:380-414), which
+ * walks the glTF scene's nodes after loading.  Parsing glTF files is not part
+ * of this library; the caller passes what the loaded scene holds: per node,
+ * its mesh's positions and triangle indices, the node's world matrix and its
+ * material's emissive factor. */
+typedef struct rg_mesh_instance {
+    const float *positions;    /* xyz per vertex (the mesh's vertex range) */
+    const uint32_t *indices;   /* index_count indices into positions, three per triangle */
+    uint32_t index_count;
+    float world_matrix[16];    /* column-major (nvmath::mat4f, the glTF node world matrix) */
+    float emissive_factor[3];
+} rg_mesh_instance;
+/* Every triangle of every instance whose emissive factor has a squared norm
+ * above 1e-6 becomes one rg_tri_light, in instance and index order: vertices
+ * transformed by the world matrix (w kept), normal = cross(p2 - p1, p3 - p1)
+ * divided by its length, area = half that length, emission = (emissive
+ * factor, its luminance).  Writes at most `capacity` lights to out (which may
+ * be null to count) and returns the number of lights, or a negative
+ * RG_ERR_* code. */
+int64_t rg_collect_triangle_lights(const rg_mesh_instance *instances, int32_t n_instances, rg_tri_light *out,
+                                   int64_t capacity);
+
 /* ---- tensor-core GEMM (a general utility of the library) ----
  * D = alpha * A . B^T, or D += alpha * A . B^T with accumulate != 0 (always
  * atomic when k_splits > 1).  A is m x k and B is n x k, read from device

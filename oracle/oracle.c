@@ -1367,3 +1367,62 @@ int or_cluster_tables(const or_point_light *pl, int32_t n, const int32_t *cluste
     free(cnt);
     return 0;
 }
+
+/* collectTriangleLightsFromScene (src/misc.cpp:380-414): every triangle of an
+ * instance whose material's emissiveFactor.sq_norm() > 1e-6 (a float compared
+ * with a double literal); vertices are node.worldMatrix * vec4(pos, 1)
+ * (nvmath.inl:491-499, sums left to right, matrix column-major), normal =
+ * cross(p2 - p1, p3 - p1) (nvmath.inl:254-261), area = normal.norm()
+ * (sqrtf of x*x + y*y + z*z), normal /= area, area *= 0.5f; emission =
+ * (emissiveFactor, luminance) with luminance of common.glsl:7-9. */
+int64_t or_collect_tri_lights(const or_mesh_instance *inst, int32_t n, or_tri_light *out, int64_t cap) {
+    int64_t count = 0;
+    for (int32_t k = 0; k < n; ++k) {
+        const float *ef = inst[k].emissive_factor;
+        float sq = ef[0] * ef[0];
+        sq = sq + ef[1] * ef[1];
+        sq = sq + ef[2] * ef[2];
+        if (!((double)sq > 1e-6)) continue;
+        const float *w = inst[k].world_matrix;
+        float lum = 0.2126f * ef[0];
+        lum = lum + 0.7152f * ef[1];
+        lum = lum + 0.0722f * ef[2];
+        for (uint32_t t = 0; t + 2 < inst[k].index_count; t += 3) {
+            float v[3][4];
+            for (int c = 0; c < 3; ++c) {
+                const float *pos = inst[k].positions + 3 * (size_t)inst[k].indices[t + c];
+                for (int row = 0; row < 4; ++row) {
+                    float acc = w[0 * 4 + row] * pos[0];
+                    acc = acc + w[1 * 4 + row] * pos[1];
+                    acc = acc + w[2 * 4 + row] * pos[2];
+                    acc = acc + w[3 * 4 + row] * 1.0f;
+                    v[c][row] = acc;
+                }
+            }
+            float e1[3], e2[3], nrm[3];
+            for (int c = 0; c < 3; ++c) {
+                e1[c] = v[1][c] - v[0][c];
+                e2[c] = v[2][c] - v[0][c];
+            }
+            nrm[0] = e1[1] * e2[2] - e1[2] * e2[1];
+            nrm[1] = e1[2] * e2[0] - e1[0] * e2[2];
+            nrm[2] = e1[0] * e2[1] - e1[1] * e2[0];
+            float len2 = nrm[0] * nrm[0];
+            len2 = len2 + nrm[1] * nrm[1];
+            len2 = len2 + nrm[2] * nrm[2];
+            float area = sqrtf(len2);
+            for (int c = 0; c < 3; ++c) nrm[c] = nrm[c] / area;
+            area = area * 0.5f;
+            if (out && count < cap) {
+                or_tri_light *o = &out[count];
+                o->p1 = (or_f4){v[0][0], v[0][1], v[0][2], v[0][3]};
+                o->p2 = (or_f4){v[1][0], v[1][1], v[1][2], v[1][3]};
+                o->p3 = (or_f4){v[2][0], v[2][1], v[2][2], v[2][3]};
+                o->emission_lum = (or_f4){ef[0], ef[1], ef[2], lum};
+                o->normal_area = (or_f4){nrm[0], nrm[1], nrm[2], area};
+            }
+            ++count;
+        }
+    }
+    return count;
+}

@@ -145,6 +145,13 @@ void or_raytrace_batch(const or_scene *scene, int32_t n, const float *rays, uint
 void or_test_visibility_batch(const or_scene *scene, int32_t n, const float *p1, const float *p2, uint8_t *out, or_stats *stats);
 void or_alias_sample_batch(const or_alias *table, int32_t count, int32_t n, const float *r, int32_t *idx, float *prob);
 void or_build_alias_table(const or_point_light *pl, int32_t n_pl, const or_tri_light *tl, int32_t n_tl, or_alias *out);
+/* Triangle lights of loaded meshes (collectTriangleLightsFromScene, src/misc.cpp:380-414); the instance
+ * record has the layout of the product's rg_mesh_instance.  Returns the light count, writing at most cap. */
+typedef struct {
+    const float *positions; const uint32_t *indices; uint32_t index_count;
+    float world_matrix[16]; float emissive_factor[3];
+} or_mesh_instance;
+int64_t or_collect_tri_lights(const or_mesh_instance *inst, int32_t n, or_tri_light *out, int64_t cap);
 
 /* ---- passes; crop = {x0, y0, w, h} or NULL for the full frame; out is full-frame sized ---- */
 typedef struct { int32_t key; float q; } or_candidate;     /* learned candidate (see or_mlp below) */

@@ -69,6 +69,8 @@ def oracle():
         for name in ("or_initial_temporal", "or_spatial_biased", "or_spatial_unbiased", "or_shade",
                      "or_brute_force_fp64"):
             getattr(_oracle, name).restype = C.c_int
+        _oracle.or_collect_tri_lights.restype = C.c_int64
+        _oracle.or_collect_tri_lights.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]
     return _oracle
 
 
@@ -80,6 +82,8 @@ def ref():
     global _ref
     if _ref is None:
         _ref = C.CDLL(str(REF_LIB))
+        _ref.ref_collect_tri_lights.restype = C.c_int64
+        _ref.ref_collect_tri_lights.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]
     return _ref
 
 

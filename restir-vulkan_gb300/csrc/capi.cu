@@ -200,6 +200,16 @@ int rg_get_stats(rg_context *ctx, rg_stats *out, int32_t reset) {
     return RG_OK;
 }
 
+int64_t rg_collect_triangle_lights(const rg_mesh_instance *instances, int32_t n_instances, rg_tri_light *out,
+                                   int64_t capacity) {
+    if (n_instances < 0 || capacity < 0 || (n_instances > 0 && !instances))
+        return fail(RG_ERR_INVALID_ARGUMENT, "rg_collect_triangle_lights: bad arguments");
+    for (int32_t k = 0; k < n_instances; ++k)
+        if (instances[k].index_count > 0 && (!instances[k].positions || !instances[k].indices))
+            return fail(RG_ERR_INVALID_ARGUMENT, "rg_collect_triangle_lights: instance %d has no mesh", k);
+    return host_collect_tri_lights(instances, n_instances, out, capacity);
+}
+
 int rg_build_bvh(const float *tri_xyz, int32_t n_tris, rg_aabb_tree_node *out_nodes, rg_triangle *out_tris) {
     if (!tri_xyz || !out_nodes || !out_tris) return fail(RG_ERR_INVALID_ARGUMENT, "null pointer");
     if (n_tris < 2) return fail(RG_ERR_INVALID_ARGUMENT, "the reference's tree needs at least 2 triangles");

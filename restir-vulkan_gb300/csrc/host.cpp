@@ -441,3 +441,59 @@ int host_cluster_tables(const rg_point_light *pl, int32_t n, const int32_t *clus
     }
     return RG_OK;
 }
+
+// ---------------------------------------------------------------- triangle lights
+// collectTriangleLightsFromScene (src/misc.cpp:380-414), with the float
+// operations of the nvmath calls it makes, in their order:
+//   M * vec4(p, 1): u_r = ((M[r][0] x + M[r][1] y) + M[r][2] z) + M[r][3] 1
+//                   (nvmath.inl:491-499; M column-major)
+//   cross(a, b) = (a.y b.z - a.z b.y, a.z b.x - a.x b.z, a.x b.y - a.y b.x)
+//                   (nvmath.inl:254-261)
+//   norm() = sqrtf((x x + y y) + z z), v /= s per component (nvmath_types.h)
+//   luminance = (0.2126f r + 0.7152f g) + 0.0722f b (common.glsl:7-9)
+// and the emissive test sq_norm() > 1e-6 made in double, as the reference's
+// float-to-double comparison does.
+int64_t host_collect_tri_lights(const rg_mesh_instance *inst, int32_t n, rg_tri_light *out, int64_t capacity) {
+    int64_t count = 0;
+    for (int32_t k = 0; k < n; ++k) {
+        const rg_mesh_instance &m = inst[k];
+        const float *e = m.emissive_factor;
+        const float esq = (e[0] * e[0] + e[1] * e[1]) + e[2] * e[2];
+        if (!((double)esq > 1e-6)) continue;
+        const float lum = (0.2126f * e[0] + 0.7152f * e[1]) + 0.0722f * e[2];
+        const float *M = m.world_matrix;
+        for (uint32_t i = 0; i + 2 < m.index_count; i += 3) {
+            float p[3][4];
+            for (int v = 0; v < 3; ++v) {
+                const float *q = m.positions + 3 * (size_t)m.indices[i + v];
+                for (int r = 0; r < 4; ++r) p[v][r] = ((M[r] * q[0] + M[4 + r] * q[1]) + M[8 + r] * q[2]) + M[12 + r] * 1.0f;
+            }
+            const float a0 = p[1][0] - p[0][0], a1 = p[1][1] - p[0][1], a2 = p[1][2] - p[0][2];
+            const float b0 = p[2][0] - p[0][0], b1 = p[2][1] - p[0][1], b2 = p[2][2] - p[0][2];
+            float nx = a1 * b2 - a2 * b1, ny = a2 * b0 - a0 * b2, nz = a0 * b1 - a1 * b0;
+            float area = sqrtf((nx * nx + ny * ny) + nz * nz);
+            nx /= area;
+            ny /= area;
+            nz /= area;
+            area *= 0.5f;
+            if (out && count < capacity) {
+                rg_tri_light &t = out[count];
+                for (int r = 0; r < 4; ++r) {
+                    t.p1[r] = p[0][r];
+                    t.p2[r] = p[1][r];
+                    t.p3[r] = p[2][r];
+                }
+                t.emission_luminance[0] = e[0];
+                t.emission_luminance[1] = e[1];
+                t.emission_luminance[2] = e[2];
+                t.emission_luminance[3] = lum;
+                t.normal_area[0] = nx;
+                t.normal_area[1] = ny;
+                t.normal_area[2] = nz;
+                t.normal_area[3] = area;
+            }
+            ++count;
+        }
+    }
+    return count;
+}

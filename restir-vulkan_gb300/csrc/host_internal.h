@@ -19,3 +19,6 @@ int host_kmeans(const float *pos4, int32_t n, int32_t k, int32_t iterations, uin
                 float *centers3);
 int host_cluster_tables(const rg_point_light *pl, int32_t n, const int32_t *cluster_of, int32_t k, int32_t *order,
                         int32_t *offset, rg_alias_table_column *col, float *within);
+// collectTriangleLightsFromScene (src/misc.cpp:380-414) on loaded meshes:
+// the light count; at most `capacity` lights written to out (may be null).
+int64_t host_collect_tri_lights(const rg_mesh_instance *inst, int32_t n, rg_tri_light *out, int64_t capacity);

@@ -91,6 +91,11 @@ class View(C.Structure):
                 ("rgba_out", C.c_void_p), ("uniforms", RestirUniforms)]
 
 
+class MeshInstance(C.Structure):
+    _fields_ = [("positions", C.c_void_p), ("indices", C.c_void_p), ("index_count", C.c_uint32),
+                ("world_matrix", C.c_float * 16), ("emissive_factor", C.c_float * 3)]
+
+
 class BatchTuning(C.Structure):
     _fields_ = [("ris_pixels_per_thread", C.c_int32), ("spatial_tile_width", C.c_int32), ("ctas_per_sm", C.c_int32)]
 
@@ -175,6 +180,7 @@ _SIGNATURES = {
                                                C.POINTER(C.c_int32), C.POINTER(C.c_float), C.POINTER(C.c_double),
                                                C.c_void_p]),
     "rg_batch_destroy": (C.c_int, [C.c_void_p]),
+    "rg_collect_triangle_lights": (C.c_int64, [C.POINTER(MeshInstance), C.c_int32, C.c_void_p, C.c_int64]),
     "rg_cluster_lights": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_void_p,
                                     C.c_void_p]),
     "rg_proposal_param_count": (C.c_int64, [C.c_int32]),

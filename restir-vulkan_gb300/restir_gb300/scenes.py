@@ -357,24 +357,21 @@ def config5(seed: int = 5, n_views: int = 64, n_tris: int = 100_000, n_lights: i
 
 
 def make_tri_lights(tri_xyz: np.ndarray, emission_rgb: np.ndarray) -> np.ndarray:
-    """triLight records as the reference collects them (src/misc.cpp:380-414):
-    normal = cross(p2-p1, p3-p1), area = |normal|, normal /= area, area *= 0.5."""
-    f = np.float32
-    t = tri_xyz.reshape(-1, 3, 3).astype(f)
-    n = np.cross(t[:, 1] - t[:, 0], t[:, 2] - t[:, 0]).astype(f)
-    area = np.sqrt((n * n).sum(1, dtype=f)).astype(f)
-    n = (n / area[:, None]).astype(f)
-    area = (area * f(0.5)).astype(f)
+    """triLight records of emissive triangles, collected by the library
+    (rg_collect_triangle_lights, the reference's collectTriangleLightsFromScene,
+    src/misc.cpp:380-414): one instance per triangle with an identity world
+    matrix and the triangle's emission as its emissive factor."""
+    t = np.ascontiguousarray(tri_xyz.reshape(-1, 3, 3), np.float32)
+    e = np.ascontiguousarray(emission_rgb, np.float32)
+    idx = np.arange(3, dtype=np.uint32)
+    eye = (C.c_float * 16)(*np.eye(4, dtype=np.float32).ravel())
+    inst = (_lib.MeshInstance * len(t))()
+    for i in range(len(t)):
+        inst[i] = _lib.MeshInstance(t[i].ctypes.data, idx.ctypes.data, 3, eye, (C.c_float * 3)(*e[i]))
     out = np.zeros(len(t), _lib.TRI_LIGHT_DTYPE)
-    for k, name in enumerate(("p1", "p2", "p3")):
-        out[name][:, :3] = t[:, k]
-        out[name][:, 3] = 1.0
-    e = emission_rgb.astype(f)
-    out["emission_lum"][:, :3] = e
-    out["emission_lum"][:, 3] = luminance_f32(e[:, 0], e[:, 1], e[:, 2])
-    out["normal_area"][:, :3] = n
-    out["normal_area"][:, 3] = area
-    return out
+    n = _lib.lib().rg_collect_triangle_lights(inst, len(t), out.ctypes.data, len(out))
+    _lib.check(n if n < 0 else 0)
+    return out[:n]
 
 
 def config1_triangle_lights(seed: int = 11, width: int = 128, height: int = 128, n_quads: int = 12) -> Scene:

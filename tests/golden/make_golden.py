@@ -47,6 +47,20 @@ def phat_args(rng, n):
     return a
 
 
+def tri_lights(seed=7):
+    """Triangle lights of the seeded meshes of tests/test_tri_lights.py as the
+    reference's nvmath arithmetic computes them (oracle/ref_lights_bridge.cpp)."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    sys.path.insert(0, str(ROOT / "restir-vulkan_gb300"))
+    import test_tri_lights as tt
+    arr, keep = tt.instances(seed)
+    ref = ob.ref()
+    n = ref.ref_collect_tri_lights(C.cast(arr, C.c_void_p), len(arr), None, 0)
+    out = np.zeros((n, 20), np.float32)
+    ref.ref_collect_tri_lights(C.cast(arr, C.c_void_p), len(arr), C.c_void_p(out.ctypes.data), n)
+    np.savez_compressed(OUT / "tri_lights.npz", seed=np.int64(seed), lights=out)
+
+
 def main():
     ob.build(ref=True)
     ref = ob.ref()
@@ -100,6 +114,7 @@ def main():
     np.savez_compressed(OUT / "bvh_visibility.npz", tri_xyz=xyz, nodes=nodes.view(np.uint8), tris=tris,
                         p1=p1, p2=p2, shadowed=shadowed)
     print("wrote", sorted(p.name for p in OUT.glob("*.npz")))
+    tri_lights()
 
 
 if __name__ == "__main__":
