@@ -584,34 +584,34 @@ __global__ void __launch_bounds__(128, RG_BIASED_MIN_BLOCKS) k_spatial_biased(co
 // steps 1 and 3.
 constexpr int kMaxNeighbors = 16;
 
-__host__ __device__ inline size_t unbiased_smem_bytes(int K, int depth, int R = 1, bool mis = false) {
+__host__ __device__ inline size_t unbiased_smem_bytes(int K, int depth, int R = 1, bool mis = false, int bt = 128) {
     const size_t slots = (size_t)K + 1, kp = (size_t)(K > 0 ? K : 1);
-    size_t b = 128 * slots * (size_t)R * sizeof(rgpool::Ray);
-    b += 128 * (size_t)R * sizeof(float4);
-    b += 128 * kp * sizeof(uint32_t);
-    b += 128 * kp * (mis ? (size_t)R : 1) * sizeof(uint32_t);
-    b += (128 * slots * (size_t)R + 15) & ~(size_t)15;
-    b += 128 * (size_t)depth * sizeof(int);
+    size_t b = (size_t)bt * slots * (size_t)R * sizeof(rgpool::Ray);
+    b += (size_t)bt * (size_t)R * sizeof(float4);
+    b += (size_t)bt * kp * sizeof(uint32_t);
+    b += (size_t)bt * kp * (mis ? (size_t)R : 1) * sizeof(uint32_t);
+    b += ((size_t)bt * slots * (size_t)R + 15) & ~(size_t)15;
+    b += (size_t)bt * (size_t)depth * sizeof(int);
     return b;
 }
 
 #ifndef RG_UNBIASED_MIN_BLOCKS
 #define RG_UNBIASED_MIN_BLOCKS 8
 #endif
-// One TW x (128/TW) pixel tile; the tile shape changes which pixels share a
-// ray pool, never a result.
-template <int TW, int R, bool MIS>
+// One TW x (BT/TW) pixel tile (BT threads); the tile shape and size change
+// which pixels share a ray pool, never a result.
+template <int TW, int R, bool MIS, int BT = 128>
 __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, int bx, int by) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int K = p.num_neighbors;
     const int slots = K + 1, kp = K > 0 ? K : 1;
     rgpool::Ray *pool = reinterpret_cast<rgpool::Ray *>(smem);
-    float4 *endp = reinterpret_cast<float4 *>(pool + 128 * slots * R);             // [R][128]
-    uint32_t *nidx = reinterpret_cast<uint32_t *>(endp + 128 * R);                  // [K][128]
-    uint32_t *nm = nidx + 128 * kp;                                                 // [K][128]
-    float *nsp = reinterpret_cast<float *>(nm);                                     // MIS: [R][K][128]
-    uint8_t *flag = reinterpret_cast<uint8_t *>(nm + 128 * kp * (MIS ? R : 1));     // [R][K+1][128]
-    int *stack = reinterpret_cast<int *>(flag + ((128 * slots * R + 15) & ~15));
+    float4 *endp = reinterpret_cast<float4 *>(pool + BT * slots * R);             // [R][BT]
+    uint32_t *nidx = reinterpret_cast<uint32_t *>(endp + BT * R);                  // [K][BT]
+    uint32_t *nm = nidx + BT * kp;                                                 // [K][BT]
+    float *nsp = reinterpret_cast<float *>(nm);                                     // MIS: [R][K][BT]
+    uint8_t *flag = reinterpret_cast<uint8_t *>(nm + BT * kp * (MIS ? R : 1));     // [R][K+1][BT]
+    int *stack = reinterpret_cast<int *>(flag + ((BT * slots * R + 15) & ~15));
     __shared__ int s_count, s_next;
     const int tid = threadIdx.x + threadIdx.y * 32;
     if (tid == 0) { s_count = 0; s_next = 0; }
@@ -619,7 +619,7 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
     const DevScene &s = p.s;
     const int W = (int)p.u.screen_size[0], H = (int)p.u.screen_size[1];
     const int x = bx * TW + tid % TW;
-    const int y = by * (128 / TW) + tid / TW;
+    const int y = by * (BT / TW) + tid / TW;
     const bool valid = x < W && y < H;
     const bool vis = (p.u.flags & RG_FLAG_VISIBILITY_REUSE) != 0;
     const size_t i = valid ? (size_t)y * (size_t)W + (size_t)x : 0;
@@ -655,12 +655,12 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
             const int ny = iclamp(y + (int)roundf(sn * radius), 0, (int)(p.u.screen_size[1] - 1u));
             const size_t ni = (size_t)ny * (size_t)W + (size_t)nx;
             const ResV<R, MIS> rr = load_resv<R, MIS>(p.in, ni);
-            nidx[k * 128 + tid] = (uint32_t)ni;
+            nidx[k * BT + tid] = (uint32_t)ni;
             if (MIS) {
 #pragma unroll
-                for (int q = 0; q < R; ++q) nsp[(q * kp + k) * 128 + tid] = rr.sum_phat[q];
+                for (int q = 0; q < R; ++q) nsp[(q * kp + k) * BT + tid] = rr.sum_phat[q];
             } else {
-                nm[k * 128 + tid] = rr.m;
+                nm[k * BT + tid] = rr.m;
             }
             r.m += rr.m;
 #pragma unroll
@@ -683,26 +683,26 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
     // pool consecutively, so the lanes that take them trace similar paths.
 #pragma unroll
     for (int q = 0; q < R; ++q) {
-        endp[q * 128 + tid] = make_float4(lpos[q].x, lpos[q].y, lpos[q].z, 0.0f);
+        endp[q * BT + tid] = make_float4(lpos[q].x, lpos[q].y, lpos[q].z, 0.0f);
         uint32_t wantm = 0;  // bit k: neighbour k's segment; bit K: the pixel's own
         for (int k = 0; k < K; ++k) {
             bool excluded = true;
             if (valid) {
-                const uint32_t ni = nidx[k * 128 + tid];
+                const uint32_t ni = nidx[k * BT + tid];
                 const f3 nw = load_wpos(p.g, ni);
                 const f3 nn = load_normal(p.g, ni);
                 excluded = dot(lpos[q] - nw, nn) < 0.0f;
                 if (!excluded && vis) wantm |= 1u << k;
             }
-            flag[(q * slots + k) * 128 + tid] = excluded ? 1 : 0;
+            flag[(q * slots + k) * BT + tid] = excluded ? 1 : 0;
         }
-        flag[(q * slots + K) * 128 + tid] = 0;
+        flag[(q * slots + K) * BT + tid] = 0;
         if (valid && vis) wantm |= 1u << K;
         int slot = rgpool::append_range(&s_count, __popc(wantm));
         for (uint32_t m = wantm; m != 0u; m &= m - 1u) {
             const int k = __ffs(m) - 1;
-            const f3 start = k < K ? load_wpos(p.g, nidx[k * 128 + tid]) : wpos;
-            rgpool::put_ray(pool, slot++, start, (q * slots + k) * 128 + tid);
+            const f3 start = k < K ? load_wpos(p.g, nidx[k * BT + tid]) : wpos;
+            rgpool::put_ray(pool, slot++, start, (q * slots + k) * BT + tid);
         }
     }
     __syncthreads();
@@ -710,7 +710,7 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
     rgpool::trace_pool(
         s, pool, s_count, &s_next, stack, s.depth, ts,
         [&](int owner) {
-            const float4 e = endp[(owner / (slots * 128)) * 128 + (owner & 127)];
+            const float4 e = endp[(owner / (slots * BT)) * BT + (owner % BT)];
             return mk(e.x, e.y, e.z);
         },
         [&](int owner, bool hit) { if (hit) flag[owner] = 1; });
@@ -719,12 +719,12 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
         ResV<R, MIS> r = load_resv<R, MIS>(p.out, i);
 #pragma unroll
         for (int q = 0; q < R; ++q) {
-            const uint8_t *fq = flag + q * slots * 128;
+            const uint8_t *fq = flag + q * slots * BT;
             if (MIS) {
                 float sp = orig_sp[q];
                 for (int k = 0; k < K; ++k)
-                    if (!fq[k * 128 + tid]) sp += nsp[(q * kp + k) * 128 + tid];
-                if (vis && fq[K * 128 + tid]) sp = 0.0f;
+                    if (!fq[k * BT + tid]) sp += nsp[(q * kp + k) * BT + tid];
+                if (vis && fq[K * BT + tid]) sp = 0.0f;
                 if (sp > 0.0f) {
                     r.w[q] = r.sum_w[q] * r.p_hat[q] / (sp * r.p_hat[q]);
                 } else {
@@ -735,8 +735,8 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
             } else {
                 uint32_t ns = orig_m;
                 for (int k = 0; k < K; ++k)
-                    if (!fq[k * 128 + tid]) ns += nm[k * 128 + tid];
-                if (vis && fq[K * 128 + tid]) ns = 0;
+                    if (!fq[k * BT + tid]) ns += nm[k * BT + tid];
+                if (vis && fq[K * BT + tid]) ns = 0;
                 if (ns > 0) {
                     r.w[q] = r.sum_w[q] / ((float)ns * r.p_hat[q]);
                 } else {
@@ -750,9 +750,12 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
     count_block_rays(s, tid == 0 ? s_count : 0, ts);
 }
 
-template <int TW, int R, bool MIS>
-__global__ void __launch_bounds__(128, RG_UNBIASED_MIN_BLOCKS) k_spatial_unbiased(const SpatialParams p) {
-    spatial_unbiased_tile<TW, R, MIS>(p, blockIdx.x, blockIdx.y);
+#ifndef RG_UNBIASED_BT
+#define RG_UNBIASED_BT 128
+#endif
+template <int TW, int R, bool MIS, int BT>
+__global__ void __launch_bounds__(BT, RG_UNBIASED_MIN_BLOCKS * 128 / BT) k_spatial_unbiased(const SpatialParams p) {
+    spatial_unbiased_tile<TW, R, MIS, BT>(p, blockIdx.x, blockIdx.y);
 }
 
 // ---------------------------------------------------------------- shading (lighting.frag:43-71,103)
@@ -1051,17 +1054,18 @@ cudaError_t launch_spatial_unbiased(const DevScene &s, const GBufView &g, const 
     return with_format(s, [&](auto tag) {
         constexpr int R = decltype(tag)::R;
         constexpr bool MIS = decltype(tag)::MIS;
-        const dim3 block(32, 4);
-        const size_t smem = unbiased_smem_bytes(num_neighbors, RG_STACK_LOCAL ? 0 : s.depth, R, MIS);
-        cudaError_t e = cudaFuncSetAttribute(k_spatial_unbiased<32, R, MIS>,
+        constexpr int BT = RG_UNBIASED_BT;  // block threads: the pixels sharing one ray pool
+        const dim3 block(32, BT / 32);
+        const size_t smem = unbiased_smem_bytes(num_neighbors, RG_STACK_LOCAL ? 0 : s.depth, R, MIS, BT);
+        cudaError_t e = cudaFuncSetAttribute(k_spatial_unbiased<32, R, MIS, BT>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         if (RG_SMEM_CARVEOUT >= 0) {
-            e = cudaFuncSetAttribute(k_spatial_unbiased<32, R, MIS>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                     RG_SMEM_CARVEOUT);
+            e = cudaFuncSetAttribute(k_spatial_unbiased<32, R, MIS, BT>,
+                                     cudaFuncAttributePreferredSharedMemoryCarveout, RG_SMEM_CARVEOUT);
             if (e != cudaSuccess) return e;
         }
-        k_spatial_unbiased<32, R, MIS>
+        k_spatial_unbiased<32, R, MIS, BT>
             <<<pixel_grid((int)u.screen_size[0], (int)u.screen_size[1], block), block, smem, st>>>(p);
         return cudaGetLastError();
     });
