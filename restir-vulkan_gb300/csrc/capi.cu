@@ -325,6 +325,7 @@ int rg_upload_scene(rg_context *ctx, const rg_scene_desc *sc) {
     s.nodes = ctx->nodes;
     s.n_nodes = sc->n_nodes;
     s.depth = depth < 1 ? 1 : depth;
+    s.box_nan = host_boxes_have_nan(sc->nodes, sc->n_nodes) ? 1 : 0;
     s.tris = ctx->tris;
     s.n_tris = sc->n_triangles;
     s.alias = ctx->alias;

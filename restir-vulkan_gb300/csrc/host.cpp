@@ -4,6 +4,7 @@
 //
 // Built with -ffp-contract=off so float arithmetic rounds after every
 // operation, as the reference's host build does on x86-64.
+#include <cmath>
 #include <float.h>
 #include <math.h>
 #include <stdint.h>
@@ -299,6 +300,19 @@ void host_pack_nodes(const rg_aabb_tree_node *src, int32_t n, float *dst16) {
         d[14] = 0.0f;
         d[15] = 0.0f;
     }
+}
+
+// True when a child box coordinate of some node is NaN (e.g. a tree built
+// over triangles with NaN vertices); the filtered slab test is then off.
+bool host_boxes_have_nan(const rg_aabb_tree_node *nodes, int32_t n) {
+    for (int32_t i = 0; i < n; ++i) {
+        const rg_aabb_tree_node &s = nodes[i];
+        for (int a = 0; a < 3; ++a)
+            if (std::isnan(s.left_aabb_min[a]) || std::isnan(s.left_aabb_max[a]) || std::isnan(s.right_aabb_min[a]) ||
+                std::isnan(s.right_aabb_max[a]))
+                return true;
+    }
+    return false;
 }
 
 // GTri: p1.xyz, e1 = p2-p1, e2 = p3-p1 (float subtraction, as the reference's

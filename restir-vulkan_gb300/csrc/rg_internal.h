@@ -37,6 +37,7 @@ struct DevScene {
     const GNode *nodes;
     int32_t n_nodes;
     int32_t depth;                // validated tree depth (root = 1): traversal stack size
+    int32_t box_nan;              // some node box coordinate is NaN: shadow rays use exact slab tests only
     const GTri *tris;
     int32_t n_tris;
     const AliasLight *alias;      // point-light scenes

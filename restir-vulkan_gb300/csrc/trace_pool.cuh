@@ -77,24 +77,33 @@ __device__ __forceinline__ bool box_hit(f3 o, f3 d, f3 bmin, f3 bmax, float &rmi
 }
 
 // Filtered slab test.  The reference computes t = RN((b-o)/d) per slab; here
-// t~ = RN((b-o) * RN(1/d)) with 1/d precomputed per ray, so
-//   |t~ - t| <= 1.5 * 2^-23 |t|            (normal range, no overflow).
-// rmin and rmax are max/min compositions, which are monotone, and
-// min(g(x), g(y)) = g(min(x, y)) for g(t) = t +- eps|t| (also monotone), so
-// rmin~ and rmax~ lie within eps|rmin| and eps|rmax| of the exact values.  The
-// three comparisons of the reference's test are therefore decided here
-// whenever each is farther than a 2^-19 relative margin (10x the bound) from
-// its threshold, and rmin~, rmax~ are finite and at least 2^-90 in magnitude;
-// otherwise the function returns -1 and the caller repeats the test with
-// exact division.  NaN slabs (b == o and d == 0) arise at the same positions
-// in both computations and propagate the same way through min/max.
-// Decisions: 1 hit, 0 miss, -1 undecided.
+// t~ = RN((b-o) * RN(1/d)) with 1/d precomputed per ray.  b-o is rounded the
+// same way in both, so
+//   |t~ - t| <= e|t| + a,   e = 1.5 * 2^-23, a = 2^-148,
+// and where either overflows to infinity the other is at least 2^127 in
+// magnitude with the same sign, so clamping both to +-2^127 restores the
+// bound.  rmin and rmax are max/min compositions, which
+// are monotone, and min(g(x), g(y)) = g(min(x, y)) for g(t) = t +- (e|t| + a)
+// (also monotone), so rmin~ and rmax~ keep the same bound against the
+// reference's rmin and rmax (clamped; clamping changes none of its three
+// comparisons, since rmin and rmax beyond +-2^127 already fail rmin < 1 or
+// rmax > 0).  With E = 2^-19 (about 10 e) and T = 2^-90 (far above a):
+//   rmin~ < 1 - E          =>  rmin < 1       rmin~ > 1 + E   =>  rmin >= 1
+//   rmax~ > T              =>  rmax > 0       rmax~ < -T      =>  rmax < 0
+//   D > S                  =>  rmax > rmin    D < -S          =>  rmax < rmin
+// where D = RN(rmax~ - rmin~) and S = E (|rmin~| + |rmax~|) + T (both
+// rounded: their errors are 2^-24 relative, far inside the factor 10).  The
+// reference hits iff rmin < 1 and rmax >= rmin and rmax > 0, so all three
+// left-hand tests true decide a hit and any right-hand test true decides a
+// miss; otherwise (values within the margins, infinities on both sides of a
+// difference, NaN) the test is undecided and the caller repeats it with
+// exact division.
 //
 // The fast path only runs for rays whose direction components are all
 // nonzero, finite and within [2^-100, 2^100] in magnitude (ray_inverse), so
-// no slab value is NaN or infinite and IEEE fminf/fmaxf select the same
-// values as the GLSL min/max definitions (a +-0 result fails the 2^-90 test
-// and is decided exactly).
+// 1/d is a normal float, and only on trees whose boxes hold no NaN
+// (DevScene::box_nan), so no slab value is NaN and IEEE fminf/fmaxf select
+// the same values as the GLSL min/max definitions.
 
 // max/min of three (IEEE maxNum/minNum, as fmaxf/fminf)
 __device__ __forceinline__ float max3f(float a, float b, float c) {
@@ -108,28 +117,25 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
     return y;
 }
 
-// The filtered test's decision from a box's slab distances.
-__device__ __forceinline__ int filtered_decision(float rmin, float rmax) {
+// The filtered test's decision from a box's slab distances: sets hit or miss
+// when decided (never both), neither when undecided.
+__device__ __forceinline__ void filtered_decision(float rmin, float rmax, bool &hit, bool &miss) {
     constexpr float kEps = 1.9073486328125e-6f;     // 2^-19
     constexpr float kTiny = 8.0779356694631609e-28f; // 2^-90
-    constexpr float kBig = 1.0e38f;
-    const float ar = fabsf(rmin), ax = fabsf(rmax);
-    if (!(ar >= kTiny && ar <= kBig && ax >= kTiny && ax <= kBig)) return -1;
-    if (rmax < 0.0f) return 0;
-    const float m1 = kEps * ar;
-    if (rmin > 1.0f + m1) return 0;
-    const float m2 = kEps * (ar + ax);
-    if (rmin - rmax > m2) return 0;
-    if (rmin < 1.0f - m1 && rmax - rmin > m2) return 1;
-    return -1;
+    const float dd = rmax - rmin;
+    const float ss = __fmaf_rn(kEps, fabsf(rmin) + fabsf(rmax), kTiny);
+    hit = rmin < 1.0f - kEps && rmax > kTiny && dd > ss;
+    miss = rmin > 1.0f + kEps || rmax < -kTiny || dd < -ss;
 }
 
 // The filtered test of both children of a node at once: lane .x of every
 // packed pair is the left box, lane .y the right box; each lane rounds
 // exactly like the scalar t~ = RN((b - o) * RN(1/d)) (b - o is b + (-o)),
-// and min/max of three is the nested min/max.
-__device__ __forceinline__ void boxes_filtered(f3 o, f3 inv, const float4 &na, const float4 &nb, const float4 &nc,
-                                               int &fl, int &fr, float &tl, float &tr) {
+// and min/max of three is the nested min/max.  Returns false when both
+// children are decided (hl, hr hold the decisions), true when either needs
+// the exact test.
+__device__ __forceinline__ bool boxes_filtered(f3 o, f3 inv, const float4 &na, const float4 &nb, const float4 &nc,
+                                               bool &hl, bool &hr, float &tl, float &tr) {
     const float2 nox = make_float2(-o.x, -o.x), noy = make_float2(-o.y, -o.y), noz = make_float2(-o.z, -o.z);
     const float2 ix = make_float2(inv.x, inv.x), iy = make_float2(inv.y, inv.y), iz = make_float2(inv.z, inv.z);
     const float2 t0x = __fmul2_rn(__fadd2_rn(make_float2(na.x, na.y), nox), ix);
@@ -144,8 +150,21 @@ __device__ __forceinline__ void boxes_filtered(f3 o, f3 inv, const float4 &na, c
     const float rmaxr = min3f(fmaxf(t0x.y, t1x.y), fmaxf(t0y.y, t1y.y), fmaxf(t0z.y, t1z.y));
     tl = rminl;
     tr = rminr;
-    fl = filtered_decision(rminl, rmaxl);
-    fr = filtered_decision(rminr, rmaxr);
+    bool ml, mr;
+    filtered_decision(rminl, rmaxl, hl, ml);
+    filtered_decision(rminr, rmaxr, hr, mr);
+    return !((hl || ml) && (hr || mr));
+}
+
+// The exact slab tests of both children of a node; returns bit 0 left hit,
+// bit 1 right hit.  Kept out of line: it runs only for nodes with an
+// undecided filtered test and for rays without the fast path, and its
+// divisions inlined into the walk would cost every node visit.
+__device__ __noinline__ int boxes_exact(f3 o, f3 d, float4 na, float4 nb, float4 nc) {
+    float t;
+    const bool l = box_hit(o, d, mk(na.x, nb.x, nc.x), mk(na.z, nb.z, nc.z), t);
+    const bool r = box_hit(o, d, mk(na.y, nb.y, nc.y), mk(na.w, nb.w, nc.w), t);
+    return (l ? 1 : 0) | (r ? 2 : 0);
 }
 
 // Per-ray reciprocal of the direction; false when a component is zero,
@@ -232,7 +251,7 @@ __device__ void trace_pool(const DevScene &s, const Ray *pool, int n, int *next,
                     const float4 a = pool[k].a;
                     owner = __float_as_int(a.w);
                     rgm::shadow_segment(mk(a.x, a.y, a.z), endpoint(owner), o, d);
-                    fast = ray_inverse(d, inv);
+                    fast = ray_inverse(d, inv) && !s.box_nan;
                     node = 0;
                     sp = 0;
                     visits = 0;
@@ -279,13 +298,16 @@ __device__ void trace_pool(const DevScene &s, const Ray *pool, int n, int *next,
             const GNode *np = s.nodes + node;
             const float4 na = __ldg(&np->a), nb = __ldg(&np->b), nc = __ldg(&np->c);
             const int4 ch = __ldg(&np->d);
-            float tl, tr;
-            // both filtered tests at once, then the rare exact retests
-            int fl = -1, fr = -1;
-            if (fast) boxes_filtered(o, inv, na, nb, nc, fl, fr, tl, tr);
-            if (fl < 0) fl = box_hit(o, d, mk(na.x, nb.x, nc.x), mk(na.z, nb.z, nc.z), tl) ? 1 : 0;
-            if (fr < 0) fr = box_hit(o, d, mk(na.y, nb.y, nc.y), mk(na.w, nb.w, nc.w), tr) ? 1 : 0;
-            const bool hl = fl != 0, hr = fr != 0;
+            // both filtered tests at once, then the rare exact retests; the
+            // entry distances tl, tr only order the walk (approximate ones
+            // suffice, and rays without the filtered test go left first)
+            float tl = 0.0f, tr = 0.0f;
+            bool hl = false, hr = false;
+            if (!fast || boxes_filtered(o, inv, na, nb, nc, hl, hr, tl, tr)) {
+                const int e = boxes_exact(o, d, na, nb, nc);
+                hl = (e & 1) != 0;
+                hr = (e & 2) != 0;
+            }
             if (hl && ch.x < 0) leaf0 = ~ch.x;
             if (hr && ch.y < 0) {
                 if (leaf0 < 0) leaf0 = ~ch.y;
