@@ -16,6 +16,13 @@
 #include "mlp.cuh"
 #include "rg_internal.h"
 
+// RG_NODE_PREORDER: the device copy of the tree is renumbered in depth-first
+// preorder (host_pack_nodes_preorder); the walk's results do not depend on
+// the numbering.
+#ifndef RG_NODE_PREORDER
+#define RG_NODE_PREORDER 1
+#endif
+
 namespace {
 
 thread_local char g_err[512] = "";
@@ -278,7 +285,11 @@ int rg_upload_scene(rg_context *ctx, const rg_scene_desc *sc) {
     ctx->release_scene();
     cudaError_t e = cudaSuccess;
     std::vector<float> n16(16 * (size_t)sc->n_nodes), t12(12 * (size_t)sc->n_triangles);
+#if RG_NODE_PREORDER
+    host_pack_nodes_preorder(sc->nodes, sc->n_nodes, n16.data());
+#else
     host_pack_nodes(sc->nodes, sc->n_nodes, n16.data());
+#endif
     host_pack_tris(sc->triangles, sc->n_triangles, t12.data());
     e = dev_alloc(&ctx->nodes, (size_t)sc->n_nodes);
     if (e == cudaSuccess && sc->n_nodes) e = cudaMemcpy(ctx->nodes, n16.data(), n16.size() * 4, cudaMemcpyHostToDevice);

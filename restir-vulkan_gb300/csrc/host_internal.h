@@ -10,6 +10,7 @@ int host_validate_tree(const rg_aabb_tree_node *nodes, int32_t n_nodes, int32_t 
 int host_build_alias_table(const rg_point_light *pl, int32_t n_pl, const rg_tri_light *tl, int32_t n_tl,
                            rg_alias_table_column *out);
 void host_pack_nodes(const rg_aabb_tree_node *src, int32_t n, float *dst16);
+void host_pack_nodes_preorder(const rg_aabb_tree_node *src, int32_t n, float *dst16);
 bool host_boxes_have_nan(const rg_aabb_tree_node *nodes, int32_t n);
 void host_pack_tris(const rg_triangle *src, int32_t n, float *dst12);
 void srgb_lut_host(float *out256);
