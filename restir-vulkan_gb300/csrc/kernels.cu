@@ -586,10 +586,10 @@ constexpr int kMaxNeighbors = 16;
 
 __host__ __device__ inline size_t unbiased_smem_bytes(int K, int depth, int R = 1, bool mis = false, int bt = 128) {
     const size_t slots = (size_t)K + 1, kp = (size_t)(K > 0 ? K : 1);
-    size_t b = (size_t)bt * slots * (size_t)R * sizeof(rgpool::Ray);
-    b += (size_t)bt * (size_t)R * sizeof(float4);
+    size_t b = (size_t)bt * (size_t)R * sizeof(float4);
     b += (size_t)bt * kp * sizeof(uint32_t);
     b += (size_t)bt * kp * (mis ? (size_t)R : 1) * sizeof(uint32_t);
+    b += (size_t)bt * slots * (size_t)R * sizeof(int);
     b += ((size_t)bt * slots * (size_t)R + 15) & ~(size_t)15;
     b += (size_t)bt * (size_t)depth * sizeof(int);
     return b;
@@ -605,12 +605,15 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
     extern __shared__ __align__(16) unsigned char smem[];
     const int K = p.num_neighbors;
     const int slots = K + 1, kp = K > 0 ? K : 1;
-    rgpool::Ray *pool = reinterpret_cast<rgpool::Ray *>(smem);
-    float4 *endp = reinterpret_cast<float4 *>(pool + BT * slots * R);             // [R][BT]
+    // The ray pool holds owner tags only (a segment's start is re-read from
+    // the G-buffer when a lane takes it), which leaves more of the SM's
+    // L1/shared storage to the L1 cache that serves the tree.
+    float4 *endp = reinterpret_cast<float4 *>(smem);                                // [R][BT]
     uint32_t *nidx = reinterpret_cast<uint32_t *>(endp + BT * R);                  // [K][BT]
     uint32_t *nm = nidx + BT * kp;                                                 // [K][BT]
     float *nsp = reinterpret_cast<float *>(nm);                                     // MIS: [R][K][BT]
-    uint8_t *flag = reinterpret_cast<uint8_t *>(nm + BT * kp * (MIS ? R : 1));     // [R][K+1][BT]
+    int *pool = reinterpret_cast<int *>(nm + BT * kp * (MIS ? R : 1));             // owners, [R][K+1][BT] slots
+    uint8_t *flag = reinterpret_cast<uint8_t *>(pool + BT * slots * R);            // [R][K+1][BT]
     int *stack = reinterpret_cast<int *>(flag + ((BT * slots * R + 15) & ~15));
     __shared__ int s_count, s_next;
     const int tid = threadIdx.x + threadIdx.y * 32;
@@ -701,14 +704,23 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
         int slot = rgpool::append_range(&s_count, __popc(wantm));
         for (uint32_t m = wantm; m != 0u; m &= m - 1u) {
             const int k = __ffs(m) - 1;
-            const f3 start = k < K ? load_wpos(p.g, nidx[k * BT + tid]) : wpos;
-            rgpool::put_ray(pool, slot++, start, (q * slots + k) * BT + tid);
+            pool[slot++] = (q * slots + k) * BT + tid;
         }
     }
     __syncthreads();
     rgpool::TraceStats ts;
-    rgpool::trace_pool(
-        s, pool, s_count, &s_next, stack, s.depth, ts,
+    rgpool::trace_pool_f(
+        s,
+        [&](int slot, f3 &p1) {  // start: the neighbour's (k < K) or the pixel's own position
+            const int owner = pool[slot];
+            const int r = owner % (slots * BT);
+            const int k = r / BT, t = r % BT;
+            const size_t pi = k < K ? (size_t)nidx[k * BT + t]
+                                    : (size_t)(by * (BT / TW) + t / TW) * (size_t)W + (size_t)(bx * TW + t % TW);
+            p1 = load_wpos(p.g, pi);
+            return owner;
+        },
+        s_count, &s_next, stack, s.depth, ts,
         [&](int owner) {
             const float4 e = endp[(owner / (slots * BT)) * BT + (owner % BT)];
             return mk(e.x, e.y, e.z);

@@ -212,15 +212,16 @@ struct TraceStats {
     unsigned tri_tests = 0;  // triangle tests
 };
 
-// Traces pool[0..n) with all threads of the block; reports shadowed (1) /
-// unoccluded (0) through `emit(owner, shadowed)`.  `stack` points at
+// Traces pool slots 0..n-1 with all threads of the block; `fetch(k, p1)`
+// returns slot k's owner tag and sets its segment start p1; reports shadowed
+// (1) / unoccluded (0) through `emit(owner, shadowed)`.  `stack` points at
 // blockDim.x * blockDim.y * depth ints of shared memory.  Sets ts.err on a
 // walk longer than one visit per node or a stack overflow (malformed tree;
 // not reachable for trees validated at upload).  Every thread of the block
 // must call it, and the block size must be a multiple of 32.
-template <typename Endpoint, typename Emit>
-__device__ void trace_pool(const DevScene &s, const Ray *pool, int n, int *next, int *stack, int depth,
-                           TraceStats &ts, Endpoint endpoint, Emit emit) {
+template <typename Fetch, typename Endpoint, typename Emit>
+__device__ void trace_pool_f(const DevScene &s, Fetch fetch, int n, int *next, int *stack, int depth,
+                             TraceStats &ts, Endpoint endpoint, Emit emit) {
     constexpr unsigned kFull = 0xffffffffu;
 #if RG_STACK_LOCAL
     int local_stack[RG_MAX_TREE_DEPTH + 1];
@@ -250,9 +251,9 @@ __device__ void trace_pool(const DevScene &s, const Ray *pool, int n, int *next,
                     retired = true;
                 } else {
                     cur = k;
-                    const float4 a = pool[k].a;
-                    owner = __float_as_int(a.w);
-                    rgm::shadow_segment(mk(a.x, a.y, a.z), endpoint(owner), o, d);
+                    f3 p1;
+                    owner = fetch(k, p1);
+                    rgm::shadow_segment(p1, endpoint(owner), o, d);
                     fast = ray_inverse(d, inv) && !s.box_nan;
                     node = 0;
                     sp = 0;
@@ -344,6 +345,20 @@ __device__ void trace_pool(const DevScene &s, const Ray *pool, int n, int *next,
             }
         }
     }
+}
+
+// trace_pool_f over a pool of Ray entries (start point and owner stored).
+template <typename Endpoint, typename Emit>
+__device__ __forceinline__ void trace_pool(const DevScene &s, const Ray *pool, int n, int *next, int *stack,
+                                           int depth, TraceStats &ts, Endpoint endpoint, Emit emit) {
+    trace_pool_f(
+        s,
+        [&](int k, f3 &p1) {
+            const float4 a = pool[k].a;
+            p1 = mk(a.x, a.y, a.z);
+            return __float_as_int(a.w);
+        },
+        n, next, stack, depth, ts, endpoint, emit);
 }
 
 }  // namespace rgpool
