@@ -626,10 +626,9 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
     const bool valid = x < W && y < H;
     const bool vis = (p.u.flags & RG_FLAG_VISIBILITY_REUSE) != 0;
     const size_t i = valid ? (size_t)y * (size_t)W + (size_t)x : 0;
-    f3 wpos = mk(0.f, 0.f, 0.f);
     f3 lpos[R];
 #pragma unroll
-    for (int q = 0; q < R; ++q) lpos[q] = wpos;
+    for (int q = 0; q < R; ++q) lpos[q] = mk(0.f, 0.f, 0.f);
     uint32_t orig_m = 0;
     float orig_sp[MIS ? R : 1];
 #pragma unroll
@@ -637,7 +636,6 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
     if (valid) {
         Texel t;
         load_texel(p.g, i, t);
-        wpos = t.wpos;
         const float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
         const f3 cam = mk(p.u.camera_pos[0], p.u.camera_pos[1], p.u.camera_pos[2]);
         const f3 wo = view_dir(cam, t.wpos);
