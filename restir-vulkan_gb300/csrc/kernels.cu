@@ -227,7 +227,7 @@ __device__ __forceinline__ void count_block_rays(const DevScene &s, int rays, co
 }
 
 // ---------------------------------------------------------------- RIS + visibility + temporal (restirOmni.glsl:86-212)
-// A block of 32x4 threads covers a 32x16 pixel tile, 4 pixels per thread:
+// A block of 32x4 threads covers a 32 x (4*PPT) pixel tile, PPT pixels per thread:
 //   1. RIS for each pixel; the reservoir goes to `out`, the PCG state stays in
 //      registers, the visibility-reuse segment goes to the block's ray pool;
 //   2. the block traces its pool (trace_pool);
@@ -238,10 +238,13 @@ __device__ __forceinline__ void count_block_rays(const DevScene &s, int rays, co
 #define RG_SMEM_CARVEOUT -1
 #endif
 
+// Pixels per thread of the single-view launch (the batched one is tuned):
+// 3 (32 x 12 tiles) measured fastest at 1080p among 2 to 6 (3.33 ms against
+// 3.34, 3.48, 3.44 and 4.21 ms for 2, 4, 5 and 6).
 #ifndef RG_RIS_PPT
-#define RG_RIS_PPT 4
+#define RG_RIS_PPT 3
 #endif
-constexpr int kRisPpt = RG_RIS_PPT;  // pixels per thread of the single-view launch (the batched one is tuned)
+constexpr int kRisPpt = RG_RIS_PPT;
 
 struct InitialParams {
     DevScene s;

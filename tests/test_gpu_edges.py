@@ -1,6 +1,6 @@
 """Frame sizes that do not fill the launch tiles, and degenerate sizes.
 
-Bar: bit-exact against the oracle.  Every pass tiles the frame (RIS 32 x 16,
+Bar: bit-exact against the oracle.  Every pass tiles the frame (RIS 32 x 12,
 unbiased spatial 32 x 4, biased spatial and shading 32 x 4 pixels); frames of
 1 x 1, 1 x 7, 33 x 5 and 97 x 61 pixels leave partial tiles on both axes and
 rows narrower than a warp, and spatial neighbours clamp at every border.
