@@ -219,6 +219,15 @@ int rg_build_bvh_device(rg_context *ctx, const float *tri_xyz, int32_t n_tris, r
                         rg_triangle *triangles, int32_t *ref_undefined, void *stream);
 /* Depth of the tree (root = 1). */
 int rg_tree_depth(const rg_aabb_tree_node *nodes, int32_t n_nodes);
+/* The same tree with its nodes renumbered in depth-first preorder (root 0,
+ * each node's left subtree right after it, then its right subtree); child
+ * links remapped, leaves (~triangle index) unchanged, boxes copied bit for
+ * bit.  rg_upload_scene keeps its device copy of the tree in this order, so
+ * a left-first walk mostly steps to the next node in memory; traversal
+ * results do not depend on the numbering.  No counterpart in the reference,
+ * whose builder numbers nodes breadth first (aabbTreeBuilder.cpp:52-214).
+ * Returns n_nodes or an error (malformed tree). */
+int rg_tree_preorder(const rg_aabb_tree_node *nodes, int32_t n_nodes, rg_aabb_tree_node *out);
 /* createAliasTable: point lights if n_point > 0, else triangle lights. */
 int rg_build_alias_table(const rg_point_light *point_lights, int32_t n_point, const rg_tri_light *tri_lights,
                          int32_t n_tri, rg_alias_table_column *out);

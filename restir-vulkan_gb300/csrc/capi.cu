@@ -233,6 +233,16 @@ int rg_tree_depth(const rg_aabb_tree_node *nodes, int32_t n_nodes) {
     return d;
 }
 
+int rg_tree_preorder(const rg_aabb_tree_node *nodes, int32_t n_nodes, rg_aabb_tree_node *out) {
+    if ((!nodes || !out) && n_nodes > 0) return fail(RG_ERR_INVALID_ARGUMENT, "null pointer");
+    if (n_nodes < 0) return fail(RG_ERR_INVALID_ARGUMENT, "negative node count");
+    if (nodes == out && n_nodes > 0) return fail(RG_ERR_INVALID_ARGUMENT, "nodes and out must differ");
+    const int d = host_validate_tree(nodes, n_nodes, n_nodes + 1);
+    if (d < 0) return fail(d, "malformed tree");
+    host_tree_preorder(nodes, n_nodes, out);
+    return n_nodes;
+}
+
 int rg_build_alias_table(const rg_point_light *pl, int32_t n_pl, const rg_tri_light *tl, int32_t n_tl,
                          rg_alias_table_column *out) {
     if (!out) return fail(RG_ERR_INVALID_ARGUMENT, "null output");

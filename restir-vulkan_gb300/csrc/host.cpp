@@ -302,12 +302,11 @@ void host_pack_nodes(const rg_aabb_tree_node *src, int32_t n, float *dst16) {
     }
 }
 
-// As host_pack_nodes, with the nodes renumbered in depth-first preorder
-// (root 0, a node's left subtree right after it, then its right subtree) and
-// the child links remapped; leaves keep their triangle indices.  A walk that
-// takes the left child first then mostly steps to the next node in memory.
-// The tree must be valid (host_validate_tree).
-void host_pack_nodes_preorder(const rg_aabb_tree_node *src, int32_t n, float *dst16) {
+// The tree renumbered in depth-first preorder (root 0, a node's left
+// subtree right after it, then its right subtree), child links remapped;
+// leaves keep their triangle indices.  The tree must be valid
+// (host_validate_tree).
+void host_tree_preorder(const rg_aabb_tree_node *src, int32_t n, rg_aabb_tree_node *dst) {
     if (n <= 0) return;
     std::vector<int32_t> order, renum((size_t)n, -1), st;
     order.reserve((size_t)n);
@@ -320,13 +319,20 @@ void host_pack_nodes_preorder(const rg_aabb_tree_node *src, int32_t n, float *ds
         if (src[x].right_child >= 0) st.push_back(src[x].right_child);
         if (src[x].left_child >= 0) st.push_back(src[x].left_child);
     }
-    std::vector<rg_aabb_tree_node> tmp((size_t)n);
     for (int32_t i = 0; i < n; ++i) {
         rg_aabb_tree_node nd = src[order[(size_t)i]];
         if (nd.left_child >= 0) nd.left_child = renum[(size_t)nd.left_child];
         if (nd.right_child >= 0) nd.right_child = renum[(size_t)nd.right_child];
-        tmp[(size_t)i] = nd;
+        dst[i] = nd;
     }
+}
+
+// As host_pack_nodes, over the preorder-renumbered tree: a walk that takes
+// the left child first then mostly steps to the next node in memory.
+void host_pack_nodes_preorder(const rg_aabb_tree_node *src, int32_t n, float *dst16) {
+    if (n <= 0) return;
+    std::vector<rg_aabb_tree_node> tmp((size_t)n);
+    host_tree_preorder(src, n, tmp.data());
     host_pack_nodes(tmp.data(), n, dst16);
 }
 

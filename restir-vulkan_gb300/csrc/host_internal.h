@@ -11,6 +11,7 @@ int host_build_alias_table(const rg_point_light *pl, int32_t n_pl, const rg_tri_
                            rg_alias_table_column *out);
 void host_pack_nodes(const rg_aabb_tree_node *src, int32_t n, float *dst16);
 void host_pack_nodes_preorder(const rg_aabb_tree_node *src, int32_t n, float *dst16);
+void host_tree_preorder(const rg_aabb_tree_node *src, int32_t n, rg_aabb_tree_node *dst);
 bool host_boxes_have_nan(const rg_aabb_tree_node *nodes, int32_t n);
 void host_pack_tris(const rg_triangle *src, int32_t n, float *dst12);
 void srgb_lut_host(float *out256);

@@ -140,6 +140,7 @@ _SIGNATURES = {
     "rg_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats), C.c_int32]),
     "rg_build_bvh": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "rg_tree_depth": (C.c_int, [C.c_void_p, C.c_int32]),
+    "rg_tree_preorder": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "rg_build_alias_table": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]),
     "rg_trace_gbuffer_host": (C.c_int, [C.POINTER(SceneDesc), C.POINTER(Camera), C.c_int32, C.c_int32, C.c_void_p,
                                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

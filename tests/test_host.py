@@ -90,6 +90,46 @@ def test_tree_validation_rejects_malformed(restir_lib):
     assert restir_lib.rg_tree_depth(bad.ctypes.data, len(bad)) < 0
 
 
+def test_tree_preorder_renumbering(restir_lib, oracle_lib):
+    """rg_tree_preorder (the order of the device copy rg_upload_scene keeps):
+    the same tree, renumbered so each internal left child follows its
+    parent; the CPU G-buffer and the oracle's visibility over it are
+    unchanged."""
+    import dataclasses
+
+    import oracle_binding as ob
+    from restir_gb300 import scenes
+    s = scenes.config1(width=64, height=48)
+    n = len(s.nodes)
+    out = np.zeros_like(s.nodes)
+    assert restir_lib.rg_tree_preorder(s.nodes.ctypes.data, n, out.ctypes.data) == n
+    assert restir_lib.rg_tree_depth(out.ctypes.data, n) == restir_lib.rg_tree_depth(s.nodes.ctypes.data, n)
+    internal_left = np.nonzero(out["left"] >= 0)[0]
+    assert np.array_equal(out["left"][internal_left], internal_left + 1)
+    # the same node records up to the numbering: boxes bit for bit, same leaves
+    key = lambda a: np.sort(np.concatenate([a["lmin"], a["lmax"], a["rmin"], a["rmax"]], 1).view(np.uint32), axis=0)
+    assert np.array_equal(key(out), key(s.nodes))
+    assert np.array_equal(np.sort(out["left"][out["left"] < 0]), np.sort(s.nodes["left"][s.nodes["left"] < 0]))
+    so = dataclasses.replace(s, nodes=out)
+    g0, g1 = scenes.trace_gbuffer_host(s, 0), scenes.trace_gbuffer_host(so, 0)
+    for k in g0:
+        assert np.array_equal(g0[k], g1[k]), k
+    rng = np.random.default_rng(3)
+    m = 20_000
+    p1 = rng.uniform(-0.05, 1.05, (m, 3)).astype(np.float32)
+    p2 = rng.uniform(-0.05, 1.05, (m, 3)).astype(np.float32)
+    vis = []
+    for sc in (s, so):
+        st, keep = ob.scene_struct(sc)
+        r = np.zeros(m, np.uint8)
+        ob.oracle().or_test_visibility_batch(C.byref(st), m, ob.P(p1), ob.P(p2), ob.P(r), None)
+        vis.append(r)
+    assert np.array_equal(vis[0], vis[1]) and 0.02 < vis[0].mean() < 0.98
+    bad = s.nodes.copy()
+    bad[3]["left"] = 0  # cycle back to the root
+    assert restir_lib.rg_tree_preorder(bad.ctypes.data, n, out.ctypes.data) < 0
+
+
 def test_alias_table_product_equals_oracle(restir_lib, oracle_lib):
     from restir_gb300 import _lib
     rng = np.random.default_rng(4)
