@@ -332,10 +332,15 @@ int rg_gemm_bf16(rg_context *ctx, const void *a, int32_t a_fp32, int64_t a_row_s
  * intermediate reservoirs live in a 16 MiB buffer built into the library,
  * present on every GPU that loads it until the process exits.  Frames are
  * limited to 262144 pixels (512x512); larger ones return
- * RG_ERR_INVALID_ARGUMENT.  The first call on a device looks up that buffer's
- * device address, so make the first call before any stream capture.  All
- * calls share the buffer: calls whose GPU work overlaps (other streams or
- * host threads) race and must be serialised.  Allocates nothing. */
+ * RG_ERR_INVALID_ARGUMENT.  The first call on a device after a context is
+ * created there looks up that buffer's device address (rg_create drops the
+ * cached one: a reset of the device's primary context unloads the module that
+ * holds the buffer, and no context may be used across such a reset), so make
+ * that call before any stream capture.  All calls share the buffer: calls
+ * whose GPU work overlaps (other streams or host threads) race and must be
+ * serialised.  Arguments are checked as rg_spatial_unbiased checks them, and
+ * only the default reservoir format is accepted (RG_ERR_UNSUPPORTED
+ * otherwise).  Allocates nothing. */
 int rg_spatial_unbiased_chain_noalloc(rg_context *ctx, const rg_gbuffer *gbuf, const rg_reservoir *in,
                                       rg_reservoir *out, const rg_restir_uniforms *uniforms, int32_t num_neighbors,
                                       int32_t num_passes, void *stream);

@@ -16,7 +16,9 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libref.so"
-REFERENCE_ROOT = Path(os.environ.get("RESTIR_REFERENCE", "/root/reference"))
+# The reference project's sources: $RESTIR_REFERENCE, else a checkout named
+# "reference" beside this repository.
+REFERENCE_ROOT = Path(os.environ.get("RESTIR_REFERENCE") or (HERE.parent.parent / "reference")).resolve()
 
 
 def build(ref: bool | None = None) -> None:

@@ -158,6 +158,7 @@ int rg_create(int32_t device, rg_context **out) {
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
     if (device < 0 || device >= n) return fail(RG_ERR_INVALID_ARGUMENT, "device %d out of range (%d devices)", device, n);
     RG_CUDA(cudaSetDevice(device), "cudaSetDevice");
+    noalloc_forget_device(device);
     rg_context *ctx = new rg_context();
     ctx->device = device;
     float lut[256];
@@ -631,6 +632,17 @@ int rg_internal_prepare(rg_context *ctx, const DevScene **scene, int *device) {
     if (rc) return rc;
     *scene = &ctx->scene;
     *device = ctx->device;
+    return RG_OK;
+}
+
+int rg_internal_check_spatial_args(const rg_gbuffer *g, const void *in, const void *out,
+                                   const rg_restir_uniforms *u) {
+    if (!u) return fail(RG_ERR_INVALID_ARGUMENT, "null uniforms");
+    int rc = check_size(u->screen_size[0], u->screen_size[1]);
+    if (rc) return rc;
+    if ((rc = check_gbuffer(g, u->screen_size[0], u->screen_size[1], "G-buffer"))) return rc;
+    if ((rc = check_res(in, "in")) || (rc = check_res(out, "out"))) return rc;
+    if (in == out) return fail(RG_ERR_INVALID_ARGUMENT, "in and out must differ");
     return RG_OK;
 }
 

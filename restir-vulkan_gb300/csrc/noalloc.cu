@@ -16,7 +16,11 @@
 //    process exits, whether or not the entry point is used;
 //  - frames are limited to kNoAllocMaxPixels pixels (512 x 512);
 //  - all calls share the one array, so calls whose work overlaps on the GPU
-//    (other streams, other host threads) race; serialise them.
+//    (other streams, other host threads) race; serialise them;
+//  - the array's device address is looked up by the first call on a device
+//    after a context is created there (rg_create forgets the cached address,
+//    because a reset of the device's primary context unloads the module that
+//    holds the array), so that call must come before any stream capture.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -56,6 +60,12 @@ int scratch_for_device(int device, rg_reservoir **out) {
 
 }  // namespace
 
+void noalloc_forget_device(int device) {
+    if (device < 0 || device >= kMaxDevices) return;
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    g_scratch_addr[device] = nullptr;
+}
+
 extern "C" int rg_spatial_unbiased_chain_noalloc(rg_context *ctx, const rg_gbuffer *gbuf, const rg_reservoir *in,
                                                  rg_reservoir *out, const rg_restir_uniforms *u,
                                                  int32_t num_neighbors, int32_t num_passes, void *stream) {
@@ -63,25 +73,17 @@ extern "C" int rg_spatial_unbiased_chain_noalloc(rg_context *ctx, const rg_gbuff
     int device = 0;
     int rc = rg_internal_prepare(ctx, &scene, &device);  // also makes the context's device current
     if (rc) return rc;
-    if (!u || !gbuf || !in || !out)
-        return rg_internal_fail(RG_ERR_INVALID_ARGUMENT, "rg_spatial_unbiased_chain_noalloc: null argument");
+    // the checks of rg_spatial_unbiased: every plane present and aligned for
+    // the kernel's loads, distinct 16-byte aligned reservoir buffers
+    if ((rc = rg_internal_check_spatial_args(gbuf, in, out, u))) return rc;
     if (scene->res_samples != 1 || scene->res_mis)
         return rg_internal_fail(RG_ERR_UNSUPPORTED,
                                 "rg_spatial_unbiased_chain_noalloc: its scratch holds the default reservoir format");
     const size_t w = u->screen_size[0], h = u->screen_size[1];
-    if (w == 0 || h == 0 || (uint32_t)gbuf->width != w || (uint32_t)gbuf->height != h)
-        return rg_internal_fail(RG_ERR_INVALID_ARGUMENT,
-                                "rg_spatial_unbiased_chain_noalloc: G-buffer size does not match the uniforms");
     if (w * h > kNoAllocMaxPixels)
         return rg_internal_fail(RG_ERR_INVALID_ARGUMENT,
                                 "rg_spatial_unbiased_chain_noalloc: frame larger than 262144 pixels (512x512), "
                                 "the size of its built-in scratch buffer");
-    if (!gbuf->albedo || !gbuf->normal || !gbuf->material || !gbuf->world_pos || !gbuf->depth ||
-        ((uintptr_t)gbuf->normal & 7u) || ((uintptr_t)gbuf->world_pos & 15u) || ((uintptr_t)in & 15u) ||
-        ((uintptr_t)out & 15u))
-        return rg_internal_fail(RG_ERR_INVALID_ARGUMENT,
-                                "rg_spatial_unbiased_chain_noalloc: null or misaligned buffer");
-    if (in == out) return rg_internal_fail(RG_ERR_INVALID_ARGUMENT, "rg_spatial_unbiased_chain_noalloc: in == out");
     if (num_neighbors < 0 || num_neighbors > 16 || num_passes < 1 || num_passes > 64)
         return rg_internal_fail(RG_ERR_INVALID_ARGUMENT,
                                 "rg_spatial_unbiased_chain_noalloc: num_neighbors must be 0..16, num_passes 1..64");

@@ -132,6 +132,16 @@ int rg_internal_fail(int code, const char *msg);
 int rg_internal_prepare(rg_context *ctx, const DevScene **scene, int *device);
 // A valid context (no scene needed); makes its device current.
 int rg_internal_device(rg_context *ctx, int *device);
+// The argument checks of rg_spatial_unbiased (frame size, every G-buffer
+// plane present and aligned for the kernels' loads, reservoir buffers
+// present, 16-byte aligned and distinct), for entry points that launch the
+// same kernel.
+int rg_internal_check_spatial_args(const rg_gbuffer *g, const void *in, const void *out,
+                                   const rg_restir_uniforms *u);
+// noalloc.cu: forget the cached device address of the allocation-free
+// chain's scratch array on `device` (a new context may follow a reset of the
+// device's primary context, which unloads the module holding the array).
+void noalloc_forget_device(int device);
 
 // gpu_bvh.cu: the reference tree built on the device (node count, or < 0).
 int gpu_build_bvh(const float *xyz, int n, rg_aabb_tree_node *nodes, rg_triangle *tris, int *undefined,

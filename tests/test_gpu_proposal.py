@@ -26,28 +26,36 @@ from helpers import mismatch, mlp_params, new_res
 
 pytestmark = pytest.mark.gpu
 
-CLUSTERS = 256
+# Two networks: a small one (256 clusters: 4 logit chunks of 64) and config
+# 4's own (4096 clusters: 64 chunks through the double-buffered tensor-memory
+# pipeline, the 32-wide piece search over 4096 columns) on config 2's scene
+# with its 65,536 lights and 100k triangles at 320x180.
+SETUPS = {
+    "small": dict(width=128, height=96, n_tris=20_000, n_lights=4096, clusters=256),
+    "config4": dict(width=320, height=180, n_tris=100_000, n_lights=65_536, clusters=4096),
+}
 
 
-@pytest.fixture(scope="module")
-def scene4(restir_lib):
+@pytest.fixture(scope="module", params=list(SETUPS))
+def scene4(request, restir_lib):
     from restir_gb300 import scenes
     from restir_gb300.passes import cluster_lights
-    s = scenes.config2(width=128, height=96, n_tris=20_000, n_lights=4096, frames=2)
+    c = SETUPS[request.param]
+    s = scenes.config2(width=c["width"], height=c["height"], n_tris=c["n_tris"], n_lights=c["n_lights"], frames=2)
     gs = [scenes.trace_gbuffer_host(s, f) for f in range(s.frames)]
-    cluster_of, _ = cluster_lights(s.point_lights, CLUSTERS, iterations=6, seed=4)
-    return s, gs, cluster_of
+    cluster_of, _ = cluster_lights(s.point_lights, c["clusters"], iterations=6, seed=4)
+    return s, gs, cluster_of, c["clusters"]
 
 
 def _setup(ctx, scene4, seed=1, scale_w4=0.3, lr=1e-3):
     from restir_gb300.passes import DeviceGBuffer
-    s, gs, cluster_of = scene4
+    s, gs, cluster_of, clusters = scene4
     ctx.upload_scene(s)
-    ctx.create_proposal(cluster_of, CLUSTERS, mix=0.9, batch=4096, seed=seed, learning_rate=lr)
+    ctx.create_proposal(cluster_of, clusters, mix=0.9, batch=4096, seed=seed, learning_rate=lr)
     count = len(ctx.proposal_params())
-    params = mlp_params(count, CLUSTERS, seed, scale_w4)
+    params = mlp_params(count, clusters, seed, scale_w4)
     ctx.set_proposal_params(params)
-    m = ob.OracleMlp(ctx.proposal_params(), cluster_of, CLUSTERS, mix=0.9)
+    m = ob.OracleMlp(ctx.proposal_params(), cluster_of, clusters, mix=0.9)
     return s, gs, cluster_of, [DeviceGBuffer.from_host(g) for g in gs], m
 
 
@@ -121,7 +129,7 @@ def test_learned_ris_bit_exact(ctx, scene4, cuda):
         got = reservoirs_to_numpy(out)
         exp = new_res(n)
         ob.initial_temporal_learned(s, gs[f], gs[f - 1] if f else None, prev_orc, exp, u, cand, cluster_of,
-                                    CLUSTERS, mix=0.9)
+                                    m.clusters, mix=0.9)
         assert mismatch(got, exp) == 0
         assert np.mean(got["w"] > 0) > 0.2
         prev_gpu, prev_orc = out, exp
@@ -152,7 +160,7 @@ def test_gradients_match_oracle(ctx, scene4, cuda):
     loss_o, g_orc = m.loss_grad(gs[0], cam, rows, targets, emulate=True)
     assert abs(loss - loss_o) <= 1e-4 * abs(loss_o), (loss, loss_o)
     blocks = {"W1": (0, 1024), "b1": (1024, 1088), "W2": (1088, 5184), "b2": (5184, 5248), "W3": (5248, 9344),
-              "b3": (9344, 9408), "W4": (9408, 9408 + 64 * CLUSTERS), "b4": (9408 + 64 * CLUSTERS, len(g_orc))}
+              "b3": (9344, 9408), "W4": (9408, 9408 + 64 * m.clusters), "b4": (9408 + 64 * m.clusters, len(g_orc))}
     for name, (a, b) in blocks.items():
         err = np.linalg.norm(g_gpu[a:b] - g_orc[a:b]) / max(np.linalg.norm(g_orc[a:b]), 1e-30)
         assert err <= 2e-2, (name, err)
