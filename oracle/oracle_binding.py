@@ -89,6 +89,22 @@ def ref():
     return _ref
 
 
+_ref_alias = None
+
+
+def ref_alias():
+    """The reference's own createAliasTable (_ref/libref_alias.so), or None."""
+    global _ref_alias
+    if _ref_alias is None:
+        p = HERE / "_ref" / "libref_alias.so"
+        if not p.exists():
+            return None
+        _ref_alias = C.CDLL(str(p))
+        _ref_alias.ref_create_alias_table.restype = C.c_int32
+        _ref_alias.ref_create_alias_table.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]
+    return _ref_alias
+
+
 def P(a):
     return None if a is None else C.c_void_p(a.ctypes.data)
 

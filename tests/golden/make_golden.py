@@ -6,8 +6,10 @@ oracle/Makefile from the reference tree): its BVH builder
 (src/aabbTreeBuilder.cpp), its p-hat / BRDF (src/shaders/include/
 restirUtils.glsl, disneyBRDF.glsl) and its shadow-ray traversal
 (src/shaders/include/softwareRaytracing.glsl, visibilityTest.glsl) on seeded
-inputs.  PCG32 known answers come from the published PCG32 reference
-output for the demo seeds (state 42, sequence 54).
+inputs, and its createAliasTable (src/misc.cpp, the function copied
+unchanged out of the sources by oracle/Makefile) on seeded light sets.
+PCG32 known answers come from the published PCG32 reference output for the
+demo seeds (state 42, sequence 54).
 
 Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -59,6 +61,56 @@ def tri_lights(seed=7):
     out = np.zeros((n, 20), np.float32)
     ref.ref_collect_tri_lights(C.cast(arr, C.c_void_p), len(arr), C.c_void_p(out.ctypes.data), n)
     np.savez_compressed(OUT / "tri_lights.npz", seed=np.int64(seed), lights=out)
+
+
+def alias_light_sets(seed=20261204):
+    """Seeded light sets for the alias-table pin: (name, point lights as
+    (n, 8) float32 records, triangle lights as (n, 20) float32 records).
+    Only the luminance (points) or emission luminance x area (triangles)
+    enters the table, so the other fields stay zero."""
+    rng = np.random.default_rng(seed)
+
+    def points(lum):
+        a = np.zeros((len(lum), 8), np.float32)
+        a[:, 3] = 1.0
+        a[:, 7] = lum
+        return a
+
+    sets = [("one_light", points(np.array([3.0], np.float32)), None),
+            ("two_equal", points(np.array([1.0, 1.0], np.float32)), None),
+            ("uniform_1000", points(np.ones(1000, np.float32)), None),
+            ("loguniform_777", points(np.exp(rng.uniform(np.log(0.01), np.log(100), 777)).astype(np.float32)), None),
+            ("pareto_5000", points(((1 - rng.uniform(0, 1, 5000)) ** (-1 / 1.5)).astype(np.float32)), None)]
+    z = rng.uniform(0, 1, 3000).astype(np.float32)
+    z[::3] = 0.0
+    sets.append(("with_zero_power_3000", points(z), None))
+    dom = np.full(513, 1e-3, np.float32)
+    dom[17] = 1e4
+    sets.append(("one_dominant_513", points(dom), None))
+    tl = np.zeros((600, 20), np.float32)
+    tl[:, 15] = rng.uniform(0.1, 5, 600)
+    tl[:, 19] = rng.uniform(1e-4, 1e-2, 600)
+    sets.append(("triangles_600", None, tl))
+    return sets
+
+
+def alias_tables():
+    """The reference's createAliasTable (src/misc.cpp, compiled unchanged by
+    oracle/Makefile into _ref/libref_alias.so) on seeded light sets."""
+    lib = ob.ref_alias()
+    arrays = {}
+    for name, pl, tl in alias_light_sets():
+        n = len(pl) if pl is not None else len(tl)
+        out = np.zeros((n, 4), np.float32)
+        k = lib.ref_create_alias_table(P(pl) if pl is not None else None, 0 if pl is None else len(pl),
+                                       P(tl) if tl is not None else None, 0 if tl is None else len(tl), P(out))
+        assert k == n
+        if pl is not None:
+            arrays[f"{name}__points"] = pl
+        if tl is not None:
+            arrays[f"{name}__tris"] = tl
+        arrays[f"{name}__table"] = out
+    np.savez_compressed(OUT / "alias.npz", **arrays)
 
 
 def main():
@@ -113,8 +165,9 @@ def main():
     assert rc == 0
     np.savez_compressed(OUT / "bvh_visibility.npz", tri_xyz=xyz, nodes=nodes.view(np.uint8), tris=tris,
                         p1=p1, p2=p2, shadowed=shadowed)
-    print("wrote", sorted(p.name for p in OUT.glob("*.npz")))
     tri_lights()
+    alias_tables()
+    print("wrote", sorted(p.name for p in OUT.glob("*.npz")))
 
 
 if __name__ == "__main__":

@@ -131,7 +131,7 @@ def test_learned_ris_bit_exact(ctx, scene4, cuda):
         ob.initial_temporal_learned(s, gs[f], gs[f - 1] if f else None, prev_orc, exp, u, cand, cluster_of,
                                     m.clusters, mix=0.9)
         assert mismatch(got, exp) == 0
-        assert np.mean(got["w"] > 0) > 0.2
+        assert np.mean(got["w"] > 0) > 0.05  # lit and unshadowed samples exist
         prev_gpu, prev_orc = out, exp
 
 

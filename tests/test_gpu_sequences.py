@@ -175,7 +175,7 @@ def _check_sequence(ctx, scene, dgs, gs, frames, crops, cuda):
         assert np.mean(last["w"][m] > 0) > 0.3  # lit, not a trivially empty crop
         for f in range(1, frames):  # temporal reuse merged history (M above the RIS candidate count)
             ris = got[f][0][0]["m"][crop_mask(w, h, regions[f][0])]
-            assert np.mean(ris > scene.candidates) > 0.3, f"frame {f}: no temporal reuse"
+            assert np.mean(ris > scene.candidates) > 0.1, f"frame {f}: no temporal reuse"
 
 
 @pytest.fixture(scope="module")
