@@ -1048,6 +1048,213 @@ int or_brute_force_fp64(const or_scene *sc, const or_gbuffer *g, const float *ca
     return 0;
 }
 
+/* ------------------------------------------------------------------ primary-ray G-buffer
+ * The reference rasterises its G-buffer (src/passes/gBufferPass.cpp:75-108,
+ * src/shaders/gBuffer.vert, src/shaders/gBuffer.frag:27-79); headless, the
+ * same planes come from one closest-hit ray per pixel centre:
+ *   - the camera of src/camera.h:25-50: view rows (right, -up, forward), clip
+ *     x = f/aspect * view x, clip y = f * view y, clip w = view z, so the
+ *     pixel centre (px + 0.5, py + 0.5) at NDC (nx, ny) looks along
+ *     right * (nx * aspect * tan(fov/2)) - up * (ny * tan(fov/2)) + forward
+ *     (NDC y grows downwards in Vulkan, the view's y axis is -up);
+ *   - the visible surface is the triangle with the smallest ray parameter t > 0
+ *     of the Moller-Trumbore test of softwareRaytracing.glsl:15-37 (float, same
+ *     operation order; 0 <= b1, 0 <= b2, b1 + b2 <= 1, NaN = miss, no upper
+ *     bound on t), ties to the smaller triangle index -- the depth test's
+ *     nearest fragment;
+ *   - outputs as gBuffer.frag writes them for a flat, untextured triangle:
+ *     albedo RGBA8 sRGB with alpha 255 for emissive surfaces (:73-79), normal
+ *     = the face normal normalize(cross(p2 - p1, p3 - p1)) turned towards the
+ *     viewer (gBuffer.frag:40-43 writes the interpolated vertex normal as it
+ *     is; the generated scenes carry no vertex normals, so the face normal of
+ *     the side the camera sees stands for it) as RGBA16F (w = 0), material
+ *     RG16 unorm (roughness, metallic), world position o + t*d as RGBA32F
+ *     (w = 1), depth = clip z / clip w of P*V times that position (the
+ *     rasteriser's depth);
+ *   - a ray that hits nothing leaves zero planes and depth 1 (the clear
+ *     values).
+ * The walk over the reference's tree is conservative: every box is grown by
+ * 1e-5 (absolute) plus 1e-5 of its coordinates and tested in double, and a
+ * box is skipped only when it starts beyond the best t found so far plus a
+ * margin of the same size, so no triangle the float test hits in front of the
+ * current best is missed; nearer children are walked first.
+ * Triangles without a material take albedo (180, 180, 180), roughness 1. */
+uint16_t or_float_to_half(float f) {
+    /* IEEE 754 binary16, round to nearest even: the value scaled by the
+     * spacing of halves at its exponent is rounded by nearbyint (exact in
+     * double: a float has 24 significant bits). */
+    uint32_t x;
+    memcpy(&x, &f, 4);
+    const uint16_t sign = (uint16_t)((x >> 16) & 0x8000u);
+    const float a = fabsf(f);
+    if (a != a) return (uint16_t)(sign | 0x7e00u);
+    if (a >= 65520.0f) return (uint16_t)(sign | 0x7c00u);        /* rounds to infinity */
+    if (a < 6.103515625e-05f) {                                  /* below 2^-14: spacing 2^-24 */
+        const double m = nearbyint((double)a * 16777216.0);      /* m = 1024 is the smallest normal */
+        return (uint16_t)(sign | (uint16_t)m);
+    }
+    int e;
+    frexp((double)a, &e);                                        /* a in [2^(e-1), 2^e) */
+    int E = e - 1;
+    double m = nearbyint((double)a / ldexp(1.0, E - 10));        /* in [1024, 2048] */
+    if (m >= 2048.0) { m = 1024.0; E += 1; }
+    return (uint16_t)(sign | (uint16_t)(((E + 15) << 10) | ((int)m - 1024)));
+}
+
+/* ray parameter of the float Moller-Trumbore test, or -1 on a miss */
+static float gb_tri_t(const or_tri *tr, v3 o, v3 d) {
+    const v3 p1 = f4xyz(tr->p1);
+    const v3 e1 = vsub(f4xyz(tr->p2), p1), e2 = vsub(f4xyz(tr->p3), p1);
+    const v3 p = vcross(d, e2);
+    const float f = 1.0f / vdot(e1, p);
+    const v3 s = vsub(o, p1);
+    const float bx = f * vdot(s, p);
+    if (!(bx >= 0.0f && bx <= 1.0f)) return -1.0f;
+    const v3 q = vcross(s, e1);
+    const float by = f * vdot(d, q);
+    if (!(by >= 0.0f && by + bx <= 1.0f)) return -1.0f;
+    const float t = f * vdot(e2, q);
+    return t > 0.0f ? t : -1.0f;
+}
+
+/* entry parameter of the grown box along o + t d in double, or +inf when the
+ * line misses it or it lies behind the origin */
+static double gb_box_entry(const double o[3], const double d[3], or_f4 bmin, or_f4 bmax) {
+    const float lo3[3] = {bmin.x, bmin.y, bmin.z}, hi3[3] = {bmax.x, bmax.y, bmax.z};
+    double lo = -INFINITY, hi = INFINITY;
+    for (int a = 0; a < 3; ++a) {
+        const double m = 1e-5 + 1e-5 * fmax(fabs((double)lo3[a]), fabs((double)hi3[a]));
+        const double b0 = (double)lo3[a] - m, b1 = (double)hi3[a] + m;
+        if (!(b0 <= b1)) return INFINITY;   /* NaN box */
+        if (d[a] == 0.0) {
+            if (o[a] < b0 || o[a] > b1) return INFINITY;
+            continue;
+        }
+        double t0 = (b0 - o[a]) / d[a], t1 = (b1 - o[a]) / d[a];
+        if (t0 > t1) { const double tt = t0; t0 = t1; t1 = tt; }
+        if (t0 > lo) lo = t0;
+        if (t1 < hi) hi = t1;
+    }
+    if (!(lo <= hi) || hi < 0.0) return INFINITY;
+    return lo;
+}
+
+typedef struct { float t; int tri; } gb_hit;
+
+static int gb_closest(const or_scene *sc, v3 o, v3 d, gb_hit *best) {
+    best->t = INFINITY;
+    best->tri = -1;
+    if (sc->n_nodes <= 0) {
+        for (int i = 0; i < sc->n_tris; ++i) {
+            const float t = gb_tri_t(&sc->tris[i], o, d);
+            if (t > 0.0f && (t < best->t || (t == best->t && i < best->tri))) { best->t = t; best->tri = i; }
+        }
+        return 0;
+    }
+    const double od[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+    int stack[256], top = 0, node = 0;
+    double stack_t[256];
+    int64_t visits = 0;
+    for (;;) {
+        if (++visits > (int64_t)sc->n_nodes) return -5;
+        const or_node *nd = &sc->nodes[node];
+        const int child[2] = {nd->left, nd->right};
+        const or_f4 mn[2] = {nd->lmin, nd->rmin}, mx[2] = {nd->lmax, nd->rmax};
+        double te[2];
+        for (int k = 0; k < 2; ++k) {
+            te[k] = gb_box_entry(od, dd, mn[k], mx[k]);
+            const double limit = best->tri < 0 ? INFINITY : (double)best->t + 1e-5 * (1.0 + (double)best->t);
+            if (!(te[k] <= limit)) te[k] = INFINITY;
+            if (te[k] != INFINITY && child[k] < 0) {   /* a leaf: its triangle now */
+                const int i = ~child[k];
+                const float t = gb_tri_t(&sc->tris[i], o, d);
+                if (t > 0.0f && (t < best->t || (t == best->t && i < best->tri))) { best->t = t; best->tri = i; }
+                te[k] = INFINITY;
+            }
+        }
+        /* inner children: the nearer one is walked first (pushed last) */
+        const int near = te[1] < te[0] ? 1 : 0;
+        for (int j = 0; j < 2; ++j) {
+            const int k = j == 0 ? 1 - near : near;
+            if (te[k] == INFINITY) continue;
+            if (top >= 256) return -5;
+            stack[top] = child[k];
+            stack_t[top++] = te[k];
+        }
+        node = -1;
+        while (top > 0) {
+            --top;
+            const double limit = best->tri < 0 ? INFINITY : (double)best->t + 1e-5 * (1.0 + (double)best->t);
+            if (stack_t[top] <= limit) { node = stack[top]; break; }
+        }
+        if (node < 0) return 0;
+    }
+}
+
+int or_trace_gbuffer(const or_scene *sc, const or_material *mats, int32_t n_mats, const or_camera *c, int32_t W,
+                     int32_t H, const int32_t *crop, uint8_t *albedo, uint16_t *normal, uint16_t *material,
+                     float *world_pos, float *depth) {
+    int x0, y0, cw, ch;
+    if (!crop_ok(crop, W, H, &x0, &y0, &cw, &ch)) return -2;
+    int err = 0;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t pi = 0; pi < (int64_t)cw * ch; ++pi) {
+        const int px = x0 + (int)(pi % cw), py = y0 + (int)(pi / cw);
+        const float ndc_x = (((float)px + 0.5f) / (float)W) * 2.0f - 1.0f;
+        const float ndc_y = (((float)py + 0.5f) / (float)H) * 2.0f - 1.0f;
+        const float vx = ndc_x * c->aspect * c->tan_half_fov_y;
+        const float vy = ndc_y * c->tan_half_fov_y;
+        const v3 right = V(c->right[0], c->right[1], c->right[2]);
+        const v3 up = V(c->up[0], c->up[1], c->up[2]);
+        const v3 fwd = V(c->forward[0], c->forward[1], c->forward[2]);
+        const v3 o = V(c->position[0], c->position[1], c->position[2]);
+        const v3 d = vadd(vsub(vmuls(vx, right), vmuls(vy, up)), fwd);
+        gb_hit hit;
+        const int rc = gb_closest(sc, o, d, &hit);
+        const size_t i = (size_t)py * (size_t)W + (size_t)px;
+        if (rc != 0) {
+#pragma omp atomic write
+            err = rc;
+        }
+        if (rc != 0 || hit.tri < 0) {
+            memset(albedo + 4 * i, 0, 4);
+            memset(normal + 4 * i, 0, 8);
+            memset(material + 2 * i, 0, 4);
+            memset(world_pos + 4 * i, 0, 16);
+            depth[i] = 1.0f;
+            continue;
+        }
+        const or_tri *tr = &sc->tris[hit.tri];
+        const v3 p1 = f4xyz(tr->p1);
+        v3 n = vnormalize(vcross(vsub(f4xyz(tr->p2), p1), vsub(f4xyz(tr->p3), p1)));
+        if (vdot(n, d) > 0.0f) n = V(-n.x, -n.y, -n.z);
+        const v3 p = vadd(o, vmuls(hit.t, d));
+        if (mats && hit.tri < n_mats) {
+            memcpy(albedo + 4 * i, mats[hit.tri].albedo_srgb, 4);
+            material[2 * i] = mats[hit.tri].roughness;
+            material[2 * i + 1] = mats[hit.tri].metallic;
+        } else {
+            albedo[4 * i] = albedo[4 * i + 1] = albedo[4 * i + 2] = 180;
+            albedo[4 * i + 3] = 0;
+            material[2 * i] = 65535;
+            material[2 * i + 1] = 0;
+        }
+        normal[4 * i] = or_float_to_half(n.x);
+        normal[4 * i + 1] = or_float_to_half(n.y);
+        normal[4 * i + 2] = or_float_to_half(n.z);
+        normal[4 * i + 3] = 0;
+        world_pos[4 * i] = p.x;
+        world_pos[4 * i + 1] = p.y;
+        world_pos[4 * i + 2] = p.z;
+        world_pos[4 * i + 3] = 1.0f;
+        const float *m = c->projection_view;
+        const float cz = ((m[2] * p.x + m[6] * p.y) + m[10] * p.z) + m[14] * 1.0f;
+        const float cwv = ((m[3] * p.x + m[7] * p.y) + m[11] * p.z) + m[15] * 1.0f;
+        depth[i] = cz / cwv;
+    }
+    return err;
+}
+
 int or_max_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();

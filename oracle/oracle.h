@@ -209,6 +209,21 @@ void or_reservoir_layout(int32_t *reservoir_size, int32_t *unbiased_mis, int32_t
 void or_reservoir_script(const float *cand, int32_t n, const or_reservoir *other, const float *other_phat,
                          uint64_t seed, uint64_t seq, int32_t swap_fix, or_reservoir *out);
 
+/* ---- primary-ray G-buffer (replaces the raster pass gBufferPass.cpp / gBuffer.frag) ---- */
+typedef struct { uint8_t albedo_srgb[4]; uint16_t roughness, metallic; } or_material;   /* 8 B per triangle */
+typedef struct {             /* pinhole camera (camera.h:25-50), the library's rg_camera layout */
+    float position[3], right[3], up[3], forward[3];
+    float tan_half_fov_y, aspect;
+    float projection_view[16];   /* column-major P*V */
+} or_camera;
+/* One closest-hit ray through every pixel centre of the crop (NULL: the whole
+ * frame); planes are full-frame, row-major, written only inside the crop.
+ * Returns 0, or -2 for a bad crop, -5 for a malformed tree. */
+int or_trace_gbuffer(const or_scene *scene, const or_material *mats, int32_t n_mats, const or_camera *cam,
+                     int32_t width, int32_t height, const int32_t *crop, uint8_t *albedo, uint16_t *normal,
+                     uint16_t *material, float *world_pos, float *depth);
+uint16_t or_float_to_half(float f);
+
 int or_max_threads(void);
 void or_set_threads(int32_t n);
 

@@ -69,8 +69,10 @@ def oracle():
         _oracle.or_pcg_stream.argtypes = [C.c_uint64, C.c_uint64, C.c_int32, C.c_void_p]
         _oracle.or_rand_floats.argtypes = [C.c_uint64, C.c_uint64, C.c_int32, C.c_void_p]
         for name in ("or_initial_temporal", "or_spatial_biased", "or_spatial_unbiased", "or_shade",
-                     "or_brute_force_fp64"):
+                     "or_brute_force_fp64", "or_trace_gbuffer"):
             getattr(_oracle, name).restype = C.c_int
+        _oracle.or_float_to_half.restype = C.c_uint16
+        _oracle.or_float_to_half.argtypes = [C.c_float]
         _oracle.or_collect_tri_lights.restype = C.c_int64
         _oracle.or_collect_tri_lights.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]
     return _oracle
@@ -178,6 +180,50 @@ def brute_force(scene, g, camera_pos3, crop=None):
     cam = np.asarray(camera_pos3, np.float32)
     check(oracle().or_brute_force_fp64(C.byref(s), C.byref(gg), P(cam), P(out), crop_arg(crop)), "brute_force")
     return out
+
+
+# ---------------------------------------------------------------- primary-ray G-buffer
+class Camera(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("right", C.c_float * 3), ("up", C.c_float * 3),
+                ("forward", C.c_float * 3), ("tan_half_fov_y", C.c_float), ("aspect", C.c_float),
+                ("projection_view", C.c_float * 16)]
+
+
+def camera_struct(cam) -> Camera:
+    """The oracle's camera record of a CameraModel (src/camera.h:25-50 basis,
+    float32 values as the model computes them)."""
+    import math
+    pos, right, up, fwd = cam.basis()
+    c = Camera()
+    c.position[:] = [float(v) for v in pos]
+    c.right[:] = [float(v) for v in right]
+    c.up[:] = [float(v) for v in up]
+    c.forward[:] = [float(v) for v in fwd]
+    c.tan_half_fov_y = float(np.float32(math.tan(0.5 * cam.fov_y)))
+    c.aspect = float(np.float32(cam.aspect))
+    c.projection_view[:] = [float(v) for v in cam.projection_view_colmajor()]
+    return c
+
+
+def has_gbuffer_tracer() -> bool:
+    return hasattr(oracle(), "or_trace_gbuffer")
+
+
+def trace_gbuffer(scene, frame_index: int = 0, crop=None, camera=None) -> dict:
+    """The oracle's primary-ray G-buffer of one frame (dict of numpy planes in
+    the library's formats); with `crop` only that region is traced, the rest
+    stays zero."""
+    w, h = scene.width, scene.height
+    g = {"albedo": np.zeros((h, w, 4), np.uint8), "normal": np.zeros((h, w, 4), np.uint16),
+         "material": np.zeros((h, w, 2), np.uint16), "world_pos": np.zeros((h, w, 4), np.float32),
+         "depth": np.zeros((h, w), np.float32)}
+    s, keep = scene_struct(scene)
+    cam = camera_struct(camera if camera is not None else scene.cameras[frame_index])
+    mats = np.ascontiguousarray(scene.materials)
+    check(oracle().or_trace_gbuffer(C.byref(s), P(mats), C.c_int32(len(mats)), C.byref(cam), C.c_int32(w),
+                                    C.c_int32(h), crop_arg(crop), P(g["albedo"]), P(g["normal"]), P(g["material"]),
+                                    P(g["world_pos"]), P(g["depth"])), "trace_gbuffer")
+    return g
 
 
 # ---------------------------------------------------------------- learned proposal

@@ -66,15 +66,23 @@ def test_visibility_batch_bit_exact(ctx, cfg1, cuda):
     assert st.rays_traced == n and st.traversal_errors == 0
 
 
-def test_gbuffer_gpu_equals_cpu(ctx, cfg1, cuda):
+@pytest.mark.parametrize("name,frames", [("config1", [0]), ("config2", [0, 7]), ("config3", [0, 15])])
+def test_gbuffer_gpu_equals_oracle(ctx, cuda, name, frames):
+    """k_trace_gbuffer against the oracle's independent primary-ray G-buffer
+    (or_trace_gbuffer: gBuffer.frag's planes for one closest-hit ray per
+    pixel centre, camera.h's convention), every plane byte for byte, at the
+    configurations' own sizes."""
+    from restir_gb300 import scenes
     from restir_gb300.passes import DeviceGBuffer
-    s, g = cfg1
+    s = scenes.CONFIGS[name]()
     ctx.upload_scene(s)
     d = DeviceGBuffer(s.width, s.height)
-    ctx.trace_gbuffer(s.cameras[0], d)
-    got = d.to_host()
-    for k in g:
-        assert np.array_equal(got[k].reshape(g[k].shape), g[k]), k
+    for f in frames:
+        ctx.trace_gbuffer(s.cameras[f], d)
+        got = d.to_host()
+        exp = ob.trace_gbuffer(s, f)
+        for k in exp:
+            assert np.array_equal(got[k].reshape(exp[k].shape).view(np.uint8), exp[k].view(np.uint8)), (name, f, k)
 
 
 def test_config1_frame_bit_exact(ctx, cfg1, cuda):
