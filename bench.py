@@ -734,9 +734,20 @@ def batched_section(dev: int, steps: int = 5, n_views: int = 64, clusters: int =
 def reference_arm(args, rank: int, world: int) -> dict | None:
     if rank != 0:
         return None
-    s = make_scene(args.config, args.width, args.height, args.frames)
+    # Everything of this arm runs on the CPU oracle, the library is never
+    # loaded: the scene's tree and alias table come from the oracle's
+    # restatements of the reference's builders (byte-identical to them,
+    # tests/test_bvh_oracle.py, tests/test_alias_pin.py) and the G-buffers
+    # from the oracle's primary-ray tracer.
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle_binding as ob
     from restir_gb300 import scenes
-    gb = [scenes.trace_gbuffer_host(s, 0), scenes.trace_gbuffer_host(s, 1)]
+    scenes.set_preprocessing(bvh=ob.build_bvh, alias=ob.build_alias_table)
+    try:
+        s = make_scene(args.config, args.width, args.height, args.frames)
+    finally:
+        scenes.set_preprocessing()
+    gb = [ob.trace_gbuffer(s, 0), ob.trace_gbuffer(s, 1)]
     vals = []
     for k in range(args.warmup + args.steps):
         r = cpu_sample(s, gb, args.cpu_crop)
@@ -754,7 +765,8 @@ def reference_arm(args, rank: int, world: int) -> dict | None:
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": ("the reference's passes are Vulkan GLSL (no graphics stack on this box); its CPU "
                      "implementation of the path is the oracle's restatement, pinned against the reference's "
-                     "own BVH builder, BRDF/p-hat and traversal compiled from source")}
+                     "own BVH builder, alias table, BRDF/p-hat and traversal compiled from source; scene "
+                     "preprocessing and G-buffers also come from the oracle (the library is not loaded)")}
 
 
 def main(argv=None):

@@ -1048,6 +1048,184 @@ int or_brute_force_fp64(const or_scene *sc, const or_gbuffer *g, const float *ca
     return 0;
 }
 
+/* ------------------------------------------------------------------ tree builder
+ * AabbTree::build (src/aabbTreeBuilder.cpp:52-214) restated in C, operation
+ * for operation, so the node and triangle buffers come out byte-identical:
+ *   - triangles pass through the node's world matrix (identity here), which
+ *     turns a -0 coordinate into +0 and keeps every other value;
+ *   - a leaf's box is the component-wise nvmath min/max of its vertices
+ *     (nv_min(a, b) = a < b ? a : b, nv_max(a, b) = a > b ? a : b), its
+ *     centroid 0.5f * (min + max);
+ *   - ranges are split breadth first (a FIFO queue; nodes are numbered in pop
+ *     order, the root is node 0): 1 triangle = a leaf link ~index, 2 = a node
+ *     with both leaves; otherwise 12 buckets over the widest centroid axis
+ *     (x > y ? x : y, then z if larger), bucket = (size_t)clamp((c - cmin) /
+ *     (span / 12), 0.5, 11.5), the split minimising
+ *     0.125 + (nL * SA(L) + nR * SA(R)) / SA(range) over the 11 split points
+ *     (SA = sx*sy + sx*sz + sy*sz; the right-side bounds accumulated from
+ *     the top bucket down), an in-place swap partition, and the median split
+ *     with recomputed bounds when one side is empty. */
+typedef struct { float c[3], mn[3], mx[3]; int32_t geom; size_t bucket; } bl_leaf;
+typedef struct { float mn[3], mx[3]; size_t count; } bl_bucket;
+typedef struct { int32_t *parent; size_t beg, end; } bl_step;
+
+static inline float nvmn(float a, float b) { return a < b ? a : b; }
+static inline float nvmx(float a, float b) { return a > b ? a : b; }
+static float bl_sah(const float mn[3], const float mx[3]) {
+    const float sx = mx[0] - mn[0], sy = mx[1] - mn[1], sz = mx[2] - mn[2];
+    return (sx * sy + sx * sz) + sy * sz;
+}
+static void bl_bucket_init(bl_bucket *b) {
+    for (int a = 0; a < 3; ++a) { b->mn[a] = 3.402823466e38f; b->mx[a] = -3.402823466e38f; }
+    b->count = 0;
+}
+static bl_bucket bl_merge(bl_bucket l, const bl_bucket *r) {
+    l.count += r->count;
+    for (int a = 0; a < 3; ++a) { l.mn[a] = nvmn(l.mn[a], r->mn[a]); l.mx[a] = nvmx(l.mx[a], r->mx[a]); }
+    return l;
+}
+static float bl_heur(const bl_bucket *b) { return (float)b->count * bl_sah(b->mn, b->mx); }
+static void bl_set(or_f4 *dst, const float v[3]) { dst->x = v[0]; dst->y = v[1]; dst->z = v[2]; dst->w = 1.0f; }
+
+int32_t or_build_bvh(const float *xyz, int32_t n, or_node *nodes, or_tri *tris) {
+    enum { NB = 12 };
+    if (n < 2) return -1;
+    bl_leaf *leaves = (bl_leaf *)malloc(sizeof(bl_leaf) * (size_t)n);
+    bl_step *q = (bl_step *)malloc(sizeof(bl_step) * (size_t)(2 * n));
+    if (!leaves || !q) { free(leaves); free(q); return -2; }
+    for (int32_t i = 0; i < n; ++i) {
+        float p[3][3];
+        for (int k = 0; k < 3; ++k)
+            for (int a = 0; a < 3; ++a) p[k][a] = xyz[(size_t)i * 9 + 3 * k + a] + 0.0f;  /* -0 -> +0 */
+        or_tri *t = &tris[i];
+        t->p1.x = p[0][0]; t->p1.y = p[0][1]; t->p1.z = p[0][2]; t->p1.w = 1.0f;
+        t->p2.x = p[1][0]; t->p2.y = p[1][1]; t->p2.z = p[1][2]; t->p2.w = 1.0f;
+        t->p3.x = p[2][0]; t->p3.y = p[2][1]; t->p3.z = p[2][2]; t->p3.w = 1.0f;
+        bl_leaf *L = &leaves[i];
+        for (int a = 0; a < 3; ++a) {
+            L->mn[a] = L->mx[a] = p[0][a];
+            L->mn[a] = nvmn(L->mn[a], p[1][a]);
+            L->mx[a] = nvmx(L->mx[a], p[1][a]);
+            L->mn[a] = nvmn(L->mn[a], p[2][a]);
+            L->mx[a] = nvmx(L->mx[a], p[2][a]);
+            L->c[a] = 0.5f * (L->mn[a] + L->mx[a]);
+        }
+        L->geom = i;
+        L->bucket = 0;
+    }
+    memset(nodes, 0, sizeof(or_node) * (size_t)(n - 1));
+    int32_t alloc = 0, dummy_root = -1, rc = n - 1;
+    size_t qh = 0, qt = 0;
+    q[qt].parent = &dummy_root; q[qt].beg = 0; q[qt].end = (size_t)n; ++qt;
+    while (qh < qt) {
+        const bl_step st = q[qh++];
+        const size_t cnt = st.end - st.beg;
+        if (cnt == 1) {
+            *st.parent = ~leaves[st.beg].geom;
+            continue;
+        }
+        if (cnt == 2) {
+            const bl_leaf *l = &leaves[st.beg], *r = &leaves[st.beg + 1];
+            const int32_t ni = alloc++;
+            *st.parent = ni;
+            or_node *nd = &nodes[ni];
+            nd->left = ~l->geom;
+            nd->right = ~r->geom;
+            bl_set(&nd->lmin, l->mn); bl_set(&nd->lmax, l->mx);
+            bl_set(&nd->rmin, r->mn); bl_set(&nd->rmax, r->mx);
+            continue;
+        }
+        float cmin[3], cmax[3], bmin[3], bmax[3];
+        for (int a = 0; a < 3; ++a) {
+            cmin[a] = cmax[a] = leaves[st.beg].c[a];
+            bmin[a] = leaves[st.beg].mn[a];
+            bmax[a] = leaves[st.beg].mx[a];
+        }
+        for (size_t i = st.beg + 1; i < st.end; ++i)
+            for (int a = 0; a < 3; ++a) {
+                cmin[a] = nvmn(cmin[a], leaves[i].c[a]);
+                cmax[a] = nvmx(cmax[a], leaves[i].c[a]);
+                bmin[a] = nvmn(bmin[a], leaves[i].mn[a]);
+                bmax[a] = nvmx(bmax[a], leaves[i].mx[a]);
+            }
+        const float outer = bl_sah(bmin, bmax);
+        const float span[3] = {cmax[0] - cmin[0], cmax[1] - cmin[1], cmax[2] - cmin[2]};
+        int dim = span[0] > span[1] ? 0 : 1;
+        if (span[2] > span[dim]) dim = 2;
+        if (!(span[dim] > 0.0f)) { rc = -3; break; }   /* (c - cmin) / 0: undefined in the reference */
+        bl_bucket bk[NB];
+        for (int b = 0; b < NB; ++b) bl_bucket_init(&bk[b]);
+        const float range = span[dim] / (float)NB;
+        for (size_t i = st.beg; i < st.end; ++i) {
+            float u = (leaves[i].c[dim] - cmin[dim]) / range;
+            u = u < 0.5f ? 0.5f : u;
+            u = u > (float)NB - 0.5f ? (float)NB - 0.5f : u;
+            leaves[i].bucket = (size_t)u;
+            bl_bucket *b = &bk[leaves[i].bucket];
+            for (int a = 0; a < 3; ++a) { b->mn[a] = nvmn(b->mn[a], leaves[i].mn[a]); b->mx[a] = nvmx(b->mx[a], leaves[i].mx[a]); }
+            ++b->count;
+        }
+        bl_bucket cache[NB - 1];
+        {
+            bl_bucket cur = bk[NB - 1];
+            for (size_t i = NB - 1; i > 0;) {
+                cache[--i] = cur;
+                cur = bl_merge(cur, &bk[i]);
+            }
+        }
+        size_t opt = 0;
+        int found = 0;
+        float lmn[3] = {0, 0, 0}, lmx[3] = {0, 0, 0}, rmn[3] = {0, 0, 0}, rmx[3] = {0, 0, 0};
+        {
+            float best = 3.402823466e38f;
+            bl_bucket left;
+            bl_bucket_init(&left);
+            for (size_t sp = 0; sp < NB - 1; ++sp) {
+                left = bl_merge(left, &bk[sp]);
+                const bl_bucket *right = &cache[sp];
+                const float h = 0.125f + (bl_heur(&left) + bl_heur(right)) / outer;
+                if (h < best) {
+                    best = h;
+                    opt = sp;
+                    found = 1;
+                    memcpy(lmn, left.mn, sizeof(lmn)); memcpy(lmx, left.mx, sizeof(lmx));
+                    memcpy(rmn, right->mn, sizeof(rmn)); memcpy(rmx, right->mx, sizeof(rmx));
+                }
+            }
+        }
+        size_t pivot = st.beg;
+        for (size_t i = st.beg; i < st.end; ++i)
+            if (leaves[i].bucket <= opt) {
+                const bl_leaf tmp = leaves[i];
+                leaves[i] = leaves[pivot];
+                leaves[pivot] = tmp;
+                ++pivot;
+            }
+        if (pivot == st.beg || pivot == st.end) {
+            pivot = (st.beg + st.end) / 2;
+            for (int a = 0; a < 3; ++a) { lmn[a] = leaves[st.beg].mn[a]; lmx[a] = leaves[st.beg].mx[a]; }
+            for (size_t i = st.beg + 1; i < pivot; ++i)
+                for (int a = 0; a < 3; ++a) { lmn[a] = nvmn(lmn[a], leaves[i].mn[a]); lmx[a] = nvmx(lmx[a], leaves[i].mx[a]); }
+            for (int a = 0; a < 3; ++a) { rmn[a] = leaves[pivot].mn[a]; rmx[a] = leaves[pivot].mx[a]; }
+            for (size_t i = pivot; i < st.end; ++i)
+                for (int a = 0; a < 3; ++a) { rmn[a] = nvmn(rmn[a], leaves[i].mn[a]); rmx[a] = nvmx(rmx[a], leaves[i].mx[a]); }
+        } else if (!found) {
+            rc = -3;   /* no finite heuristic: the reference's bounds stay uninitialised */
+            break;
+        }
+        const int32_t ni = alloc++;
+        *st.parent = ni;
+        or_node *nd = &nodes[ni];
+        bl_set(&nd->lmin, lmn); bl_set(&nd->lmax, lmx);
+        bl_set(&nd->rmin, rmn); bl_set(&nd->rmax, rmx);
+        q[qt].parent = &nd->left; q[qt].beg = st.beg; q[qt].end = pivot; ++qt;
+        q[qt].parent = &nd->right; q[qt].beg = pivot; q[qt].end = st.end; ++qt;
+    }
+    free(leaves);
+    free(q);
+    return rc;
+}
+
 /* ------------------------------------------------------------------ primary-ray G-buffer
  * The reference rasterises its G-buffer (src/passes/gBufferPass.cpp:75-108,
  * src/shaders/gBuffer.vert, src/shaders/gBuffer.frag:27-79); headless, the

@@ -209,6 +209,13 @@ void or_reservoir_layout(int32_t *reservoir_size, int32_t *unbiased_mis, int32_t
 void or_reservoir_script(const float *cand, int32_t n, const or_reservoir *other, const float *other_phat,
                          uint64_t seed, uint64_t seq, int32_t swap_fix, or_reservoir *out);
 
+/* ---- the reference's tree builder (AabbTree::build, aabbTreeBuilder.cpp:52-214) ----
+ * tri_xyz: n triangles x 9 floats.  Writes n-1 nodes and n triangles (w = 1)
+ * and returns n-1; -1 for n < 2; -3 when the input takes a path the reference
+ * leaves undefined (a range whose centroids all coincide, or one with no
+ * finite split heuristic). */
+int32_t or_build_bvh(const float *tri_xyz, int32_t n, or_node *out_nodes, or_tri *out_tris);
+
 /* ---- primary-ray G-buffer (replaces the raster pass gBufferPass.cpp / gBuffer.frag) ---- */
 typedef struct { uint8_t albedo_srgb[4]; uint16_t roughness, metallic; } or_material;   /* 8 B per triangle */
 typedef struct {             /* pinhole camera (camera.h:25-50), the library's rg_camera layout */

@@ -182,6 +182,48 @@ def brute_force(scene, g, camera_pos3, crop=None):
     return out
 
 
+# ---------------------------------------------------------------- host preprocessing
+NODE_DTYPE = np.dtype([("lmin", "<f4", 4), ("lmax", "<f4", 4), ("rmin", "<f4", 4), ("rmax", "<f4", 4),
+                       ("left", "<i4"), ("right", "<i4"), ("pad", "<i4", 2)])                 # 80 B
+TRI_DTYPE = np.dtype([("p1", "<f4", 4), ("p2", "<f4", 4), ("p3", "<f4", 4)])              # 48 B
+ALIAS_DTYPE = np.dtype([("prob", "<f4"), ("alias", "<i4"), ("ori_prob", "<f4"), ("alias_ori_prob", "<f4")])
+
+
+def tree_depth(nodes) -> int:
+    """Levels of the tree (root = 1), breadth first over the child links."""
+    left = np.asarray(nodes["left"]).astype(np.int64)
+    right = np.asarray(nodes["right"]).astype(np.int64)
+    level, depth = np.array([0], np.int64), 0
+    while len(level):
+        depth += 1
+        kids = np.concatenate([left[level], right[level]])
+        level = kids[kids >= 0]
+    return depth
+
+
+def build_bvh(tri_xyz):
+    """The oracle's restatement of the reference's AabbTree::build: (nodes,
+    triangles, depth) in the reference's layouts."""
+    xyz = np.ascontiguousarray(tri_xyz, np.float32).reshape(-1, 9)
+    n = len(xyz)
+    nodes = np.zeros(max(n - 1, 1), NODE_DTYPE)
+    tris = np.zeros(n, TRI_DTYPE)
+    o = oracle()
+    o.or_build_bvh.restype = C.c_int32
+    rc = o.or_build_bvh(P(xyz), C.c_int32(n), P(nodes), P(tris))
+    if rc != n - 1:
+        raise RuntimeError(f"oracle tree build failed: {rc}")
+    return nodes, tris, tree_depth(nodes)
+
+
+def build_alias_table(point_lights):
+    """The oracle's restatement of createAliasTable over point lights."""
+    pl = np.ascontiguousarray(point_lights)
+    out = np.zeros(len(pl), ALIAS_DTYPE)
+    oracle().or_build_alias_table(P(pl), C.c_int32(len(pl)), None, C.c_int32(0), P(out))
+    return out
+
+
 # ---------------------------------------------------------------- primary-ray G-buffer
 class Camera(C.Structure):
     _fields_ = [("position", C.c_float * 3), ("right", C.c_float * 3), ("up", C.c_float * 3),

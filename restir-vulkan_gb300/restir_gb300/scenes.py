@@ -217,8 +217,28 @@ def make_materials(albedo_lin: np.ndarray, roughness: np.ndarray, metallic: np.n
 
 
 # ------------------------------------------------------------------ host preprocessing through the C ABI
+# The tree and alias-table builds the scenes use: the library's (rg_build_bvh,
+# rg_build_alias_table) unless set_preprocessing replaced them, e.g. with
+# another implementation of the same reference functions for a run that must
+# not load the library.
+_PREPROCESS = {}
+
+
+def set_preprocessing(bvh=None, alias=None):
+    """bvh(tri_xyz) -> (nodes, triangles, depth) and alias(point_lights) ->
+    alias table, in the reference's layouts; None restores the library's."""
+    _PREPROCESS.clear()
+    if bvh is not None:
+        _PREPROCESS["bvh"] = bvh
+    if alias is not None:
+        _PREPROCESS["alias"] = alias
+
+
 def build_bvh(tri_xyz: np.ndarray):
     tri_xyz = np.ascontiguousarray(tri_xyz, np.float32)
+    if "bvh" in _PREPROCESS:
+        nodes, tris, depth = _PREPROCESS["bvh"](tri_xyz)
+        return nodes.view(_lib.NODE_DTYPE), tris.view(_lib.TRI_DTYPE), depth
     n = len(tri_xyz)
     nodes = np.zeros(max(n - 1, 1), _lib.NODE_DTYPE)
     tris = np.zeros(n, _lib.TRI_DTYPE)
@@ -232,6 +252,8 @@ def build_alias(point_lights: np.ndarray, uniform: bool = False) -> np.ndarray:
     src = point_lights.copy()
     if uniform:  # equal weights give the uniform source pdf through the same table
         src["color_lum"][:, 3] = 1.0
+    if "alias" in _PREPROCESS:
+        return _PREPROCESS["alias"](src).view(_lib.ALIAS_DTYPE)
     out = np.zeros(len(src), _lib.ALIAS_DTYPE)
     _lib.check(_lib.lib().rg_build_alias_table(src.ctypes.data, len(src), None, 0, out.ctypes.data))
     return out
