@@ -11,9 +11,34 @@ def new_res(n):
     return np.zeros(n, _lib.RESERVOIR_DTYPE)
 
 
+# Float words of a reservoir (pos_lum, normal, p-hat, sum of weights, W); word 8
+# is the light index and word 12 M.
+_FLOAT_WORDS = np.array([0, 1, 2, 3, 4, 5, 6, 7, 9, 10, 11])
+QNAN = np.uint32(0x7FC00000)
+
+
+def canonical_nan(bits: np.ndarray) -> np.ndarray:
+    """32-bit float patterns with every NaN replaced by one quiet NaN: where
+    the reference's arithmetic yields NaN (0/0 in the unbiased pass's W for a
+    reservoir without a sample), the GPU writes 0x7fffffff and the CPU
+    0x7fc00000; parity compares NaN with NaN."""
+    b = bits.copy()
+    nan = ((b & np.uint32(0x7F800000)) == np.uint32(0x7F800000)) & ((b & np.uint32(0x007FFFFF)) != 0)
+    b[nan] = QNAN
+    return b
+
+
 def res_bits(a: np.ndarray) -> np.ndarray:
-    """Reservoirs as raw 32-bit words without the padding lanes."""
-    return a.view(np.uint32).reshape(-1, 16)[:, :13]
+    """Reservoirs as raw 32-bit words without the padding lanes (float words
+    with canonical NaN)."""
+    w = a.view(np.uint32).reshape(-1, 16)[:, :13].copy()
+    w[:, _FLOAT_WORDS] = canonical_nan(w[:, _FLOAT_WORDS])
+    return w
+
+
+def image_bits(img: np.ndarray) -> np.ndarray:
+    """Image floats as 32-bit patterns with canonical NaN."""
+    return canonical_nan(np.ascontiguousarray(img, np.float32).view(np.uint32))
 
 
 def mismatch(a: np.ndarray, b: np.ndarray, mask=None) -> int:

@@ -10,7 +10,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from helpers import mismatch, new_res, oracle_frame
+from helpers import mismatch, new_res, oracle_frame, image_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -37,7 +37,7 @@ def test_biased_frame_odd_sizes_bit_exact(ctx, cuda, w, h):
     assert mismatch(reservoirs_to_numpy(r2), stages[-1]) == 0
     out = cuda.zeros((h, w, 4), dtype=cuda.float32, device="cuda")
     ctx.shade(dg, r2, s.lighting_uniforms(0), out)
-    assert np.array_equal(out.cpu().numpy().view(np.uint32), img.view(np.uint32))
+    assert np.array_equal(image_bits(out.cpu().numpy()), image_bits(img))
 
 
 @pytest.mark.parametrize("w,h", SIZES)
@@ -58,7 +58,7 @@ def test_unbiased_temporal_odd_sizes_bit_exact(ctx, cuda, w, h):
         ctx.render_frame(dgs[f], dgs[f - 1] if f else None, f % 2, s.frame_params(f), out)
         got = device_view(ctx.frame_reservoirs_ptr(f % 2), n * 64).cpu().numpy().view(stages[-1].dtype)
         assert mismatch(got, stages[-1]) == 0, f"frame {f}"
-        assert np.array_equal(out.cpu().numpy().view(np.uint32), img.view(np.uint32)), f"frame {f}"
+        assert np.array_equal(image_bits(out.cpu().numpy()), image_bits(img)), f"frame {f}"
         prev_res = stages[-1]
     assert ctx.stats().traversal_errors == 0
 

@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 import oracle_binding as ob
-from helpers import crop_mask, mismatch, new_res, oracle_frame
+from helpers import crop_mask, mismatch, new_res, oracle_frame, image_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -107,11 +107,11 @@ def test_config1_frame_bit_exact(ctx, cfg1, cuda):
     out = cuda.zeros((s.height, s.width, 4), dtype=cuda.float32, device="cuda")
     ctx.shade(dg, r2, s.lighting_uniforms(0), out)
     gi = out.cpu().numpy()
-    assert np.array_equal(gi.view(np.uint32), img.view(np.uint32))
+    assert np.array_equal(image_bits(gi), image_bits(img))
     # shading from a reservoir buffer the oracle produced
     out2 = cuda.zeros_like(out)
     ctx.shade(dg, reservoirs_from_numpy(stages[-1]), s.lighting_uniforms(0), out2)
-    assert np.array_equal(out2.cpu().numpy().view(np.uint32), img.view(np.uint32))
+    assert np.array_equal(image_bits(out2.cpu().numpy()), image_bits(img))
 
 
 def test_frame_sequence_unbiased_temporal_bit_exact(ctx, cfg2_small, cuda):
@@ -130,7 +130,7 @@ def test_frame_sequence_unbiased_temporal_bit_exact(ctx, cfg2_small, cuda):
         from restir_gb300.passes import device_view
         got = device_view(ctx.frame_reservoirs_ptr(f % 2), n * 64).cpu().numpy().view(stages[-1].dtype)
         assert mismatch(got, stages[-1]) == 0, f"frame {f}"
-        assert np.array_equal(out.cpu().numpy().view(np.uint32), img.view(np.uint32)), f"frame {f}"
+        assert np.array_equal(image_bits(out.cpu().numpy()), image_bits(img)), f"frame {f}"
         prev_res = stages[-1]
 
 
@@ -210,7 +210,7 @@ def test_render_frame_host_matches_device(ctx, cfg2_small, cuda):
         ctx.render_frame_host(gs[f], s.frame_params(f), h)
         imgs_host.append(h)
     for a, b in zip(imgs_dev, imgs_host):
-        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+        assert np.array_equal(image_bits(a), image_bits(b))
 
 
 def test_triangle_light_scene_bit_exact(ctx, cuda):
@@ -237,7 +237,7 @@ def test_triangle_light_scene_bit_exact(ctx, cuda):
     assert (got["light_index"] < 0).mean() > 0.5
     out = cuda.zeros((s.height, s.width, 4), dtype=cuda.float32, device="cuda")
     ctx.shade(dg, r2, s.lighting_uniforms(0), out)
-    assert np.array_equal(out.cpu().numpy().view(np.uint32), img.view(np.uint32))
+    assert np.array_equal(image_bits(out.cpu().numpy()), image_bits(img))
 
 
 def test_final_ris_weight_flag_bit_exact(ctx, cfg1, cuda):

@@ -25,7 +25,7 @@ import numpy as np
 import pytest
 
 import oracle_binding as ob
-from helpers import crop_mask, mismatch, new_res
+from helpers import crop_mask, mismatch, new_res, image_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -169,13 +169,14 @@ def _check_sequence(ctx, scene, dgs, gs, frames, crops, cuda):
                 assert bad == 0, f"crop {crop} frame {f} stage {k} region {region}: {bad} reservoirs differ"
             fin = crop_mask(w, h, regions[f][-1]).reshape(h, w)
             gi, ei = got[f][1][fin], exp[f][1][fin]
-            assert np.array_equal(gi.view(np.uint32), ei.view(np.uint32)), f"crop {crop} frame {f}: image differs"
+            assert np.array_equal(image_bits(gi), image_bits(ei)), f"crop {crop} frame {f}: image differs"
         last = got[frames - 1][0][-1]
         m = crop_mask(w, h, crop)
         assert np.mean(last["w"][m] > 0) > 0.3  # lit, not a trivially empty crop
-        for f in range(1, frames):  # temporal reuse merged history (M above the RIS candidate count)
-            ris = got[f][0][0]["m"][crop_mask(w, h, regions[f][0])]
-            assert np.mean(ris > scene.candidates) > 0.1, f"frame {f}: no temporal reuse"
+    # temporal reuse merged history somewhere in every later frame (M above the
+    # RIS candidate count); near the frame's edges new content may have none
+    for f in range(1, frames):
+        assert np.mean(got[f][0][0]["m"] > scene.candidates) > 0.1, f"frame {f}: no temporal reuse"
 
 
 @pytest.fixture(scope="module")
