@@ -137,17 +137,45 @@ typedef struct rg_lighting_uniforms {
     float gamma;
 } rg_lighting_uniforms;
 
+/* G-buffer attachment formats.  The reference takes the first format the
+ * device supports from a list per attachment (GBuffer::Formats::initialize,
+ * src/passes/gBufferPass.cpp:75-101); the values here are the VkFormat
+ * numbers of those candidates, so a host passes what it selected.  0 (the
+ * default) is the headless layout: RGBA16F normals, RGBA32F positions, D32F
+ * depth.  Texels are tightly packed in each plane (a 3-component 16-bit
+ * normal takes 6 bytes).  Decoding: SNORM16 c -> max(c / 32767, -1) (Vulkan's
+ * normalized fixed-point rule, IEEE division), half and float exactly, the
+ * D24 depth of D24_UNORM_S8_UINT from the low 24 bits of each 32-bit word
+ * (d / 16777215, the stencil byte above it ignored); D32_SFLOAT_S8_UINT's
+ * depth plane is plain float (its stencil lives in a plane of its own, which
+ * no pass reads). */
+#define RG_FORMAT_DEFAULT 0
+#define RG_FORMAT_R16G16B16_SNORM 85
+#define RG_FORMAT_R16G16B16_SFLOAT 90
+#define RG_FORMAT_R16G16B16A16_SNORM 92
+#define RG_FORMAT_R16G16B16A16_SFLOAT 97
+#define RG_FORMAT_R32G32B32_SFLOAT 106
+#define RG_FORMAT_R32G32B32A32_SFLOAT 109
+#define RG_FORMAT_D32_SFLOAT 126
+#define RG_FORMAT_D24_UNORM_S8_UINT 129
+#define RG_FORMAT_D32_SFLOAT_S8_UINT 130
+
 /* G-buffer planes (device pointers), width*height texels each, row-major. */
 typedef struct rg_gbuffer {
     int32_t width, height;
     const void *albedo;     /* R8G8B8A8_SRGB: sRGB-encoded rgb, alpha 255 = emissive */
-    const void *normal;     /* R16G16B16A16_SFLOAT */
+    const void *normal;     /* normal_format (default R16G16B16A16_SFLOAT) */
     const void *material;   /* R16G16_UNORM: roughness, metallic */
-    const void *world_pos;  /* R32G32B32A32_SFLOAT */
-    const void *depth;      /* D32_SFLOAT: projected z/w */
+    const void *world_pos;  /* world_pos_format (default R32G32B32A32_SFLOAT) */
+    const void *depth;      /* depth_format (default D32_SFLOAT): projected z/w */
+    int32_t normal_format;     /* 0, R16G16B16_SNORM, R16G16B16_SFLOAT, R16G16B16A16_SNORM,
+                                  R16G16B16A16_SFLOAT or R32G32B32_SFLOAT (gBufferPass.cpp:81-89) */
+    int32_t world_pos_format;  /* 0, R32G32B32_SFLOAT or R32G32B32A32_SFLOAT (:98-101) */
+    int32_t depth_format;      /* 0, D32_SFLOAT, D32_SFLOAT_S8_UINT or D24_UNORM_S8_UINT (:90-93) */
+    int32_t _reserved;         /* 0 */
 } rg_gbuffer;
 
-/* Writable G-buffer planes, for rg_trace_gbuffer. */
+/* Writable G-buffer planes, for rg_trace_gbuffer (default formats). */
 typedef struct rg_gbuffer_out {
     int32_t width, height;
     void *albedo, *normal, *material, *world_pos, *depth;

@@ -172,19 +172,73 @@ typedef struct {
     float depth;
 } texel_t;
 
+/* G-buffer attachment formats: the VkFormat numbers of the reference's
+ * candidates (src/passes/gBufferPass.cpp:81-101); 0 is the default layout. */
+#define OR_R16G16B16_SNORM 85
+#define OR_R16G16B16_SFLOAT 90
+#define OR_R16G16B16A16_SNORM 92
+#define OR_R16G16B16A16_SFLOAT 97
+#define OR_R32G32B32_SFLOAT 106
+#define OR_R32G32B32A32_SFLOAT 109
+#define OR_D32_SFLOAT 126
+#define OR_D24_UNORM_S8_UINT 129
+#define OR_D32_SFLOAT_S8_UINT 130
+
+/* Vulkan's conversion from normalized fixed point: max(c / (2^15 - 1), -1) */
+static inline float snorm16(uint16_t c) {
+    const float v = (float)(int16_t)c / 32767.0f;
+    return v < -1.0f ? -1.0f : v;
+}
+static v3 g_normal(const or_gbuffer *g, size_t i) {
+    switch (g->normal_format) {
+        case OR_R16G16B16A16_SNORM: {
+            const uint16_t *n = g->normal + 4 * i;
+            return V(snorm16(n[0]), snorm16(n[1]), snorm16(n[2]));
+        }
+        case OR_R16G16B16_SNORM: {
+            const uint16_t *n = g->normal + 3 * i;
+            return V(snorm16(n[0]), snorm16(n[1]), snorm16(n[2]));
+        }
+        case OR_R16G16B16_SFLOAT: {
+            const uint16_t *n = g->normal + 3 * i;
+            return V(or_half_to_float(n[0]), or_half_to_float(n[1]), or_half_to_float(n[2]));
+        }
+        case OR_R32G32B32_SFLOAT: {
+            const float *n = (const float *)(const void *)g->normal + 3 * i;
+            return V(n[0], n[1], n[2]);
+        }
+        default: {   /* R16G16B16A16_SFLOAT */
+            const uint16_t *n = g->normal + 4 * i;
+            return V(or_half_to_float(n[0]), or_half_to_float(n[1]), or_half_to_float(n[2]));
+        }
+    }
+}
+static inline v3 g_wpos(const or_gbuffer *g, size_t i) {
+    const float *p = g->world_pos + (g->world_pos_format == OR_R32G32B32_SFLOAT ? 3 : 4) * i;
+    return V(p[0], p[1], p[2]);
+}
+/* D32F (also the depth plane of D32_SFLOAT_S8_UINT), or D24_UNORM_S8_UINT:
+ * the low 24 bits of each 32-bit word over 2^24 - 1 */
+static inline float g_depth(const or_gbuffer *g, size_t i) {
+    if (g->depth_format == OR_D24_UNORM_S8_UINT) {
+        uint32_t w;
+        memcpy(&w, g->depth + i, 4);
+        return (float)(w & 0xffffffu) / 16777215.0f;
+    }
+    return g->depth[i];
+}
+
 static inline void fetch_texel(const or_gbuffer *g, int x, int y, texel_t *t) {
     size_t i = (size_t)y * (size_t)g->width + (size_t)x;
     const uint8_t *a = g->albedo + 4 * i;
     t->albedo = V(g_srgb[a[0]], g_srgb[a[1]], g_srgb[a[2]]);
     t->albedo_a = (float)a[3] / 255.0f;
-    const uint16_t *n = g->normal + 4 * i;
-    t->normal = V(or_half_to_float(n[0]), or_half_to_float(n[1]), or_half_to_float(n[2]));
+    t->normal = g_normal(g, i);
     const uint16_t *m = g->material + 2 * i;
     t->roughness = (float)m[0] / 65535.0f;
     t->metallic = (float)m[1] / 65535.0f;
-    const float *p = g->world_pos + 4 * i;
-    t->wpos = V(p[0], p[1], p[2]);
-    t->depth = g->depth[i];
+    t->wpos = g_wpos(g, i);
+    t->depth = g_depth(g, i);
 }
 
 /* ------------------------------------------------------------------ BRDF (disneyBRDF.glsl:5-90) */
@@ -743,9 +797,8 @@ int or_spatial_biased(const or_scene *sc, const or_gbuffer *g, const or_reservoi
             int ox = (int)floorf(c * radius), oy = (int)floorf(s * radius);
             int nx = iclamp(x + ox, 0, W - 1), ny = iclamp(y + oy, 0, H - 1);
             size_t ni = (size_t)ny * (size_t)W + (size_t)nx;
-            float nd = g->depth[ni];
-            const uint16_t *nn = g->normal + 4 * ni;
-            v3 nnor = V(or_half_to_float(nn[0]), or_half_to_float(nn[1]), or_half_to_float(nn[2]));
+            float nd = g_depth(g, ni);
+            v3 nnor = g_normal(g, ni);
             if (fabsf(nd - t.depth) > u->pos_threshold * fabsf(t.depth) || vdot(nnor, t.normal) < cos_thr) continue;
             const or_reservoir *rr = &in[ni];
             float ph[OR_RS];

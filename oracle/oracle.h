@@ -113,10 +113,13 @@ typedef struct {
 typedef struct {             /* headless G-buffer planes, row-major, width*height texels */
     int32_t width, height;
     const uint8_t *albedo;   /* RGBA8, sRGB-encoded rgb, a = emissive flag */
-    const uint16_t *normal;  /* RGBA16F bit patterns */
+    const uint16_t *normal;  /* normal_format; 0: RGBA16F bit patterns */
     const uint16_t *material;/* RG16 unorm (roughness, metallic) */
-    const float *world_pos;  /* RGBA32F */
-    const float *depth;      /* D32F */
+    const float *world_pos;  /* world_pos_format; 0: RGBA32F */
+    const float *depth;      /* depth_format; 0: D32F */
+    /* VkFormat numbers of the reference's attachment candidates
+     * (gBufferPass.cpp:81-101), 0 = the default above */
+    int32_t normal_format, world_pos_format, depth_format, reserved;
 } or_gbuffer;
 
 typedef struct {

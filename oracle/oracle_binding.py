@@ -46,7 +46,9 @@ class Scene(C.Structure):
 
 class GBuffer(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("albedo", C.c_void_p), ("normal", C.c_void_p),
-                ("material", C.c_void_p), ("world_pos", C.c_void_p), ("depth", C.c_void_p)]
+                ("material", C.c_void_p), ("world_pos", C.c_void_p), ("depth", C.c_void_p),
+                ("normal_format", C.c_int32), ("world_pos_format", C.c_int32), ("depth_format", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -124,9 +126,12 @@ def scene_struct(scene) -> tuple[Scene, list]:
 
 
 def gbuffer_struct(g: dict) -> GBuffer:
-    h, w = g["depth"].shape
+    """Planes of a G-buffer dict; an optional "formats" entry holds the
+    (normal, world position, depth) VkFormat numbers (0 = default)."""
+    h, w = g["depth"].shape[:2]
+    nf, pf, df = g.get("formats", (0, 0, 0))
     return GBuffer(w, h, g["albedo"].ctypes.data, g["normal"].ctypes.data, g["material"].ctypes.data,
-                   g["world_pos"].ctypes.data, g["depth"].ctypes.data)
+                   g["world_pos"].ctypes.data, g["depth"].ctypes.data, nf, pf, df, 0)
 
 
 def crop_arg(crop):

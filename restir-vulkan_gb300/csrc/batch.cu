@@ -214,6 +214,8 @@ int rg_batch_create(rg_context *ctx, const rg_view *views, int32_t n_views, cons
             if (((uintptr_t)g->normal & 7u) || ((uintptr_t)g->world_pos & 15u) || ((uintptr_t)g->albedo & 3u) ||
                 ((uintptr_t)g->material & 3u) || ((uintptr_t)g->depth & 3u))
                 return bfail(RG_ERR_INVALID_ARGUMENT, "view %d: misaligned G-buffer plane", v);
+            if (!default_formats(make_view(g)) || g->_reserved != 0)
+                return bfail(RG_ERR_UNSUPPORTED, "view %d: batched views take the default G-buffer formats", v);
         }
         if (!w.reservoirs[0] || !w.reservoirs[1] || !w.tmp || !w.rgba_out || ((uintptr_t)w.reservoirs[0] & 15u) ||
             ((uintptr_t)w.reservoirs[1] & 15u) || ((uintptr_t)w.tmp & 15u) || ((uintptr_t)w.rgba_out & 15u))

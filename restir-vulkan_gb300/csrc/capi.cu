@@ -64,6 +64,7 @@ struct GBufSlot {
     void release() { dev_free(albedo); dev_free(normal); dev_free(material); dev_free(wpos); dev_free(depth); w = h = 0; }
     rg_gbuffer view() const {
         rg_gbuffer g;
+        memset(&g, 0, sizeof(g));  // default formats
         g.width = w; g.height = h;
         g.albedo = albedo; g.normal = normal; g.material = material; g.world_pos = wpos; g.depth = depth;
         return g;
@@ -127,8 +128,26 @@ int check_gbuffer(const rg_gbuffer *g, uint32_t w, uint32_t h, const char *name)
         return fail(RG_ERR_INVALID_ARGUMENT, "%s: G-buffer is %dx%d, uniforms say %ux%u", name, g->width, g->height, w, h);
     if (!g->albedo || !g->normal || !g->material || !g->world_pos || !g->depth)
         return fail(RG_ERR_INVALID_ARGUMENT, "%s: null G-buffer plane", name);
-    if (((uintptr_t)g->normal & 7u) || ((uintptr_t)g->world_pos & 15u) || ((uintptr_t)g->albedo & 3u) ||
-        ((uintptr_t)g->material & 3u) || ((uintptr_t)g->depth & 3u))
+    // formats: the reference's candidates (gBufferPass.cpp:81-101) or 0
+    const int nf = g->normal_format, pf = g->world_pos_format, df = g->depth_format;
+    uintptr_t n_align;
+    switch (nf) {
+        case 0: case RG_FORMAT_R16G16B16A16_SFLOAT: case RG_FORMAT_R16G16B16A16_SNORM: n_align = 8; break;
+        case RG_FORMAT_R16G16B16_SNORM: case RG_FORMAT_R16G16B16_SFLOAT: n_align = 2; break;
+        case RG_FORMAT_R32G32B32_SFLOAT: n_align = 4; break;
+        default: return fail(RG_ERR_UNSUPPORTED, "%s: normal format %d is not one of the reference's", name, nf);
+    }
+    uintptr_t p_align;
+    switch (pf) {
+        case 0: case RG_FORMAT_R32G32B32A32_SFLOAT: p_align = 16; break;
+        case RG_FORMAT_R32G32B32_SFLOAT: p_align = 4; break;
+        default: return fail(RG_ERR_UNSUPPORTED, "%s: world-position format %d is not one of the reference's", name, pf);
+    }
+    if (df != 0 && df != RG_FORMAT_D32_SFLOAT && df != RG_FORMAT_D32_SFLOAT_S8_UINT && df != RG_FORMAT_D24_UNORM_S8_UINT)
+        return fail(RG_ERR_UNSUPPORTED, "%s: depth format %d is not one of the reference's", name, df);
+    if (g->_reserved != 0) return fail(RG_ERR_INVALID_ARGUMENT, "%s: reserved field must be 0", name);
+    if (((uintptr_t)g->normal & (n_align - 1)) || ((uintptr_t)g->world_pos & (p_align - 1)) ||
+        ((uintptr_t)g->albedo & 3u) || ((uintptr_t)g->material & 3u) || ((uintptr_t)g->depth & 3u))
         return fail(RG_ERR_INVALID_ARGUMENT, "%s: misaligned G-buffer plane", name);
     return RG_OK;
 }

@@ -42,10 +42,37 @@ __device__ __forceinline__ f3 load_albedo(const GBufView &g, size_t i, float *al
     if (alpha) *alpha = (float)(a >> 24) / 255.0f;
     return mk(__ldg(&g_srgb_lut[a & 0xffu]), __ldg(&g_srgb_lut[(a >> 8) & 0xffu]), __ldg(&g_srgb_lut[(a >> 16) & 0xffu]));
 }
+// SNORM16 -> float: max(c / 32767, -1), Vulkan's conversion from normalized
+// fixed point (IEEE division).
+__device__ __forceinline__ float snorm16(uint16_t c) { return fmaxf((float)(int16_t)c / 32767.0f, -1.0f); }
+
+// The reference's normal attachment candidates (gBufferPass.cpp:81-89);
+// nfmt is warp-uniform, so the switch costs a uniform branch.
 __device__ __forceinline__ f3 load_normal(const GBufView &g, size_t i) {
-    const uint2 n = __ldg(g.normal + i);
-    return mk(half_bits_to_float((uint16_t)(n.x & 0xffffu)), half_bits_to_float((uint16_t)(n.x >> 16)),
-              half_bits_to_float((uint16_t)(n.y & 0xffffu)));
+    if (g.nfmt == 0) {
+        const uint2 n = __ldg(g.normal + i);
+        return mk(half_bits_to_float((uint16_t)(n.x & 0xffffu)), half_bits_to_float((uint16_t)(n.x >> 16)),
+                  half_bits_to_float((uint16_t)(n.y & 0xffffu)));
+    }
+    if (g.nfmt == RG_FORMAT_R16G16B16A16_SNORM) {
+        const uint2 n = __ldg(g.normal + i);
+        return mk(snorm16((uint16_t)(n.x & 0xffffu)), snorm16((uint16_t)(n.x >> 16)), snorm16((uint16_t)(n.y & 0xffffu)));
+    }
+    if (g.nfmt == RG_FORMAT_R32G32B32_SFLOAT) {
+        const float *p = reinterpret_cast<const float *>(g.normal) + 3 * i;
+        return mk(__ldg(p), __ldg(p + 1), __ldg(p + 2));
+    }
+    const unsigned short *p = reinterpret_cast<const unsigned short *>(g.normal) + 3 * i;
+    const uint16_t a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+    if (g.nfmt == RG_FORMAT_R16G16B16_SNORM) return mk(snorm16(a), snorm16(b), snorm16(c));
+    return mk(half_bits_to_float(a), half_bits_to_float(b), half_bits_to_float(c));  // R16G16B16_SFLOAT
+}
+// depth: D32F (also the depth plane of D32_SFLOAT_S8_UINT) or the low 24 bits
+// of D24_UNORM_S8_UINT's 32-bit words over 2^24 - 1.
+__device__ __forceinline__ float load_depth(const GBufView &g, size_t i) {
+    if (g.dfmt == 0) return __ldg(g.depth + i);
+    const uint32_t w = __ldg(reinterpret_cast<const uint32_t *>(g.depth) + i);
+    return (float)(w & 0xffffffu) / 16777215.0f;
 }
 __device__ __forceinline__ void load_material(const GBufView &g, size_t i, float &rough, float &metal) {
     const uint32_t m = __ldg(g.material + i);
@@ -53,8 +80,12 @@ __device__ __forceinline__ void load_material(const GBufView &g, size_t i, float
     metal = (float)(m >> 16) / 65535.0f;
 }
 __device__ __forceinline__ f3 load_wpos(const GBufView &g, size_t i) {
-    const float4 p = __ldg(g.wpos + i);
-    return mk(p.x, p.y, p.z);
+    if (g.pfmt == 0) {
+        const float4 p = __ldg(g.wpos + i);
+        return mk(p.x, p.y, p.z);
+    }
+    const float *p = reinterpret_cast<const float *>(g.wpos) + 3 * i;  // R32G32B32_SFLOAT
+    return mk(__ldg(p), __ldg(p + 1), __ldg(p + 2));
 }
 __device__ __forceinline__ void load_texel(const GBufView &g, size_t i, Texel &t) {
     t.albedo = load_albedo(g, i, &t.albedo_a);
@@ -536,7 +567,7 @@ __device__ __forceinline__ void spatial_biased_tile(const SpatialParams &p, int 
     const size_t i = (size_t)y * (size_t)W + (size_t)x;
     Texel t;
     load_texel(p.g, i, t);
-    const float depth = __ldg(p.g.depth + i);
+    const float depth = load_depth(p.g, i);
     const float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
     const f3 cam = mk(p.u.camera_pos[0], p.u.camera_pos[1], p.u.camera_pos[2]);
     const f3 wo = view_dir(cam, t.wpos);
@@ -551,7 +582,7 @@ __device__ __forceinline__ void spatial_biased_tile(const SpatialParams &p, int 
         const int nx = iclamp(x + (int)floorf(cs * radius), 0, W - 1);
         const int ny = iclamp(y + (int)floorf(sn * radius), 0, H - 1);
         const size_t ni = (size_t)ny * (size_t)W + (size_t)nx;
-        const float nd = __ldg(p.g.depth + ni);
+        const float nd = load_depth(p.g, ni);
         const f3 nn = load_normal(p.g, ni);
         if (fabsf(nd - depth) > p.u.spatial_pos_threshold * fabsf(depth) || dot(nn, t.normal) < p.cos_thr) continue;
         const ResV<R, MIS> rr = load_resv<R, MIS>(p.in, ni);
@@ -1003,6 +1034,11 @@ GBufView make_view(const rg_gbuffer *g) {
     v.material = static_cast<const uint32_t *>(g->material);
     v.wpos = static_cast<const float4 *>(g->world_pos);
     v.depth = static_cast<const float *>(g->depth);
+    // the default's explicit VkFormat numbers load like the default
+    v.nfmt = g->normal_format == RG_FORMAT_R16G16B16A16_SFLOAT ? 0 : g->normal_format;
+    v.pfmt = g->world_pos_format == RG_FORMAT_R32G32B32A32_SFLOAT ? 0 : g->world_pos_format;
+    v.dfmt = (g->depth_format == RG_FORMAT_D32_SFLOAT || g->depth_format == RG_FORMAT_D32_SFLOAT_S8_UINT)
+                 ? 0 : g->depth_format;
     return v;
 }
 

@@ -167,6 +167,8 @@ int check_gbuf(const rg_gbuffer *g) {
         return pfail(RG_ERR_INVALID_ARGUMENT, "bad G-buffer");
     if (((uintptr_t)g->normal & 7u) || ((uintptr_t)g->world_pos & 15u))
         return pfail(RG_ERR_INVALID_ARGUMENT, "misaligned G-buffer plane");
+    if (!default_formats(make_view(g)))
+        return pfail(RG_ERR_UNSUPPORTED, "the learned proposal takes the default G-buffer formats");
     return RG_OK;
 }
 

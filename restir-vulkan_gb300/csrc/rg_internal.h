@@ -55,14 +55,20 @@ struct DevScene {
     int32_t res_mis;              // and UNBIASED_MIS (0 or 1)
 };
 
+// G-buffer planes with their formats (rg_gbuffer's VkFormat numbers, 0 =
+// default).  The typed pointers are the default layouts; the loaders in
+// kernels.cu reinterpret them for the other formats.
 struct GBufView {
     int32_t w, h;
     const uint32_t *albedo;  // RGBA8
-    const uint2 *normal;     // RGBA16F
+    const uint2 *normal;     // RGBA16F (nfmt 0)
     const uint32_t *material;// RG16
-    const float4 *wpos;
-    const float *depth;
+    const float4 *wpos;      // RGBA32F (pfmt 0)
+    const float *depth;      // D32F (dfmt 0)
+    int32_t nfmt, pfmt, dfmt;
 };
+// True when every plane of g is in the default layout.
+inline bool default_formats(const GBufView &g) { return g.nfmt == 0 && g.pfmt == 0 && g.dfmt == 0; }
 
 GBufView make_view(const rg_gbuffer *g);
 

@@ -54,13 +54,29 @@ class LightingUniforms(C.Structure):
                 ("debug_mode", C.c_int32), ("gamma", C.c_float)]
 
 
+# G-buffer formats (VkFormat numbers of the reference's candidates; 0 = default)
+FORMAT_DEFAULT = 0
+FORMAT_R16G16B16_SNORM = 85
+FORMAT_R16G16B16_SFLOAT = 90
+FORMAT_R16G16B16A16_SNORM = 92
+FORMAT_R16G16B16A16_SFLOAT = 97
+FORMAT_R32G32B32_SFLOAT = 106
+FORMAT_R32G32B32A32_SFLOAT = 109
+FORMAT_D32_SFLOAT = 126
+FORMAT_D24_UNORM_S8_UINT = 129
+FORMAT_D32_SFLOAT_S8_UINT = 130
+
+
 class GBuffer(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("albedo", C.c_void_p), ("normal", C.c_void_p),
+                ("material", C.c_void_p), ("world_pos", C.c_void_p), ("depth", C.c_void_p),
+                ("normal_format", C.c_int32), ("world_pos_format", C.c_int32), ("depth_format", C.c_int32),
+                ("_reserved", C.c_int32)]
+
+
+class GBufferOut(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("albedo", C.c_void_p), ("normal", C.c_void_p),
                 ("material", C.c_void_p), ("world_pos", C.c_void_p), ("depth", C.c_void_p)]
-
-
-class GBufferOut(GBuffer):
-    pass
 
 
 class Camera(C.Structure):
