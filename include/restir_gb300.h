@@ -224,6 +224,8 @@ typedef struct rg_stats {
     uint64_t node_visits;            /* tree nodes visited by those segments */
     uint64_t triangle_tests;         /* triangle tests made by those segments */
     uint64_t mma_timeouts;           /* tensor-core launches whose bounded completion wait ran out */
+    uint64_t wide_nodes;             /* nodes of the uploaded tree's 4-wide copy (0: not built, every ray walks
+                                        the binary tree) */
 } rg_stats;
 
 /* ---- context ---- */

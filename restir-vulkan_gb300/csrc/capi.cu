@@ -22,6 +22,11 @@
 #ifndef RG_NODE_PREORDER
 #define RG_NODE_PREORDER 1
 #endif
+// RG_WIDE_TREE: keep a 4-wide copy of the tree (host_pack_wide) for shadow
+// rays on the filtered fast path.
+#ifndef RG_WIDE_TREE
+#define RG_WIDE_TREE 1
+#endif
 
 namespace {
 
@@ -78,6 +83,7 @@ struct rg_context {
     DevScene scene{};
     bool has_scene = false;
     GNode *nodes = nullptr;
+    WNode *wide = nullptr;
     GTri *tris = nullptr;
     AliasLight *alias = nullptr;
     float4 *pl_color = nullptr;
@@ -100,7 +106,7 @@ struct rg_context {
     void release_scene() {
         proposal_release(proposal);
         proposal = nullptr;
-        dev_free(nodes); dev_free(tris); dev_free(alias); dev_free(pl_color); dev_free(tri_lights);
+        dev_free(nodes); dev_free(wide); dev_free(tris); dev_free(alias); dev_free(pl_color); dev_free(tri_lights);
         dev_free(tri_alias); dev_free(materials);
         has_scene = false;
     }
@@ -222,6 +228,7 @@ int rg_get_stats(rg_context *ctx, rg_stats *out, int32_t reset) {
     int to = 0;
     RG_CUDA(cudaMemcpy(&to, ctx->mma_timeouts, sizeof(int), cudaMemcpyDeviceToHost), "rg_get_stats");
     out->mma_timeouts = (uint64_t)to;
+    out->wide_nodes = ctx->has_scene ? (uint64_t)ctx->scene.n_wide : 0u;
     if (reset) RG_CUDA(cudaMemset(ctx->mma_timeouts, 0, sizeof(int)), "rg_get_stats");
     if (reset) RG_CUDA(cudaMemset(ctx->counters, 0, sizeof(c)), "rg_get_stats");
     return RG_OK;
@@ -321,8 +328,20 @@ int rg_upload_scene(rg_context *ctx, const rg_scene_desc *sc) {
     host_pack_nodes(sc->nodes, sc->n_nodes, n16.data());
 #endif
     host_pack_tris(sc->triangles, sc->n_triangles, t12.data());
+    // the 4-wide copy for fast-path shadow rays (RG_WIDE_TREE=0 builds leave it out)
+    const bool box_nan = host_boxes_have_nan(sc->nodes, sc->n_nodes);
+    std::vector<float> w32;
+    int wide_depth = 0;
+    int32_t n_wide = -1;
+    if (RG_WIDE_TREE && sc->n_nodes > 0 && !box_nan) n_wide = host_pack_wide(sc->nodes, sc->n_nodes, w32, &wide_depth);
+    const int wide_stack = 3 * wide_depth + 1;
+    if (n_wide > 0 && wide_stack > RG_MAX_TREE_DEPTH + 1) n_wide = -1;
     e = dev_alloc(&ctx->nodes, (size_t)sc->n_nodes);
     if (e == cudaSuccess && sc->n_nodes) e = cudaMemcpy(ctx->nodes, n16.data(), n16.size() * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n_wide > 0) {
+        e = dev_alloc(&ctx->wide, (size_t)n_wide);
+        if (e == cudaSuccess) e = cudaMemcpy(ctx->wide, w32.data(), w32.size() * 4, cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess) e = dev_alloc(&ctx->tris, (size_t)sc->n_triangles);
     if (e == cudaSuccess && sc->n_triangles) e = cudaMemcpy(ctx->tris, t12.data(), t12.size() * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && point) {
@@ -366,7 +385,10 @@ int rg_upload_scene(rg_context *ctx, const rg_scene_desc *sc) {
     s.nodes = ctx->nodes;
     s.n_nodes = sc->n_nodes;
     s.depth = depth < 1 ? 1 : depth;
-    s.box_nan = host_boxes_have_nan(sc->nodes, sc->n_nodes) ? 1 : 0;
+    s.box_nan = box_nan ? 1 : 0;
+    s.wide = n_wide > 0 ? ctx->wide : nullptr;
+    s.n_wide = n_wide > 0 ? n_wide : 0;
+    s.wide_stack = n_wide > 0 ? wide_stack : 0;
     s.tris = ctx->tris;
     s.n_tris = sc->n_triangles;
     s.alias = ctx->alias;

@@ -297,8 +297,9 @@ void host_pack_nodes(const rg_aabb_tree_node *src, int32_t n, float *dst16) {
         }
         memcpy(&d[12], &s.left_child, 4);
         memcpy(&d[13], &s.right_child, 4);
-        d[14] = 0.0f;
-        d[15] = 0.0f;
+        const int32_t none = INT32_MIN;  // no third or fourth child (the walk shares the 4-wide code)
+        memcpy(&d[14], &none, 4);
+        memcpy(&d[15], &none, 4);
     }
 }
 
@@ -334,6 +335,111 @@ void host_pack_nodes_preorder(const rg_aabb_tree_node *src, int32_t n, float *ds
     std::vector<rg_aabb_tree_node> tmp((size_t)n);
     host_tree_preorder(src, n, tmp.data());
     host_pack_nodes(tmp.data(), n, dst16);
+}
+
+// ---------------------------------------------------------------- 4-wide copy
+// The tree collapsed to four children per node for shadow rays on the
+// filtered fast path.  A node of the copy holds the boxes of up to four
+// descendants of one binary node, chosen by expanding, while fewer than four
+// are held, the inner descendant with the largest box surface into its two
+// children (descendants kept in left-to-right order); leaves keep their
+// triangle links.  Every box is copied bit for bit from the reference's node
+// that stores it.  Skipping the expanded boxes keeps the any-hit answer when
+// each child box of a node lies inside the box its parent stores for it:
+// the reference's slab test is then monotone along every path (a box that
+// passes implies that every box containing it passes), so a triangle is
+// tested by the collapsed walk exactly when its whole box path passes, as in
+// the reference.  Returns the node count (preorder: a node's first inner
+// child follows it), or -1 when some child box is not inside its parent's
+// box (the copy is then not used).  Layout per node (32 floats): children 0,1
+// as in host_pack_nodes (per axis lo0 lo1 hi0 hi1), child links (4 ints,
+// kNoChild for empty slots, whose box repeats the last child's), children
+// 2,3 the same way, 4 unused.
+namespace {
+struct WEntry { float lo[3], hi[3]; int32_t ref; };
+constexpr int32_t kNoChild = INT32_MIN;
+
+bool box_inside(const float *lo, const float *hi, const float *plo, const float *phi) {
+    for (int a = 0; a < 3; ++a)
+        if (!(lo[a] >= plo[a] && hi[a] <= phi[a])) return false;
+    return true;
+}
+WEntry child_entry(const rg_aabb_tree_node &n, int side) {
+    WEntry e;
+    for (int a = 0; a < 3; ++a) {
+        e.lo[a] = side == 0 ? n.left_aabb_min[a] : n.right_aabb_min[a];
+        e.hi[a] = side == 0 ? n.left_aabb_max[a] : n.right_aabb_max[a];
+    }
+    e.ref = side == 0 ? n.left_child : n.right_child;
+    return e;
+}
+float surface(const WEntry &e) {
+    const float x = e.hi[0] - e.lo[0], y = e.hi[1] - e.lo[1], z = e.hi[2] - e.lo[2];
+    return x * y + x * z + y * z;
+}
+
+struct WideBuilder {
+    const rg_aabb_tree_node *src;
+    std::vector<float> *out;
+    int max_depth = 0;
+    bool ok = true;
+
+    int32_t build(int32_t x, int depth) {
+        max_depth = std::max(max_depth, depth);
+        WEntry e[4];
+        int n = 2;
+        e[0] = child_entry(src[x], 0);
+        e[1] = child_entry(src[x], 1);
+        while (n < 4) {
+            int pick = -1;
+            float best = -1.0f;
+            for (int k = 0; k < n; ++k)
+                if (e[k].ref >= 0 && surface(e[k]) > best) { best = surface(e[k]); pick = k; }
+            if (pick < 0) break;
+            const rg_aabb_tree_node &y = src[e[pick].ref];
+            const WEntry l = child_entry(y, 0), r = child_entry(y, 1);
+            if (!box_inside(l.lo, l.hi, e[pick].lo, e[pick].hi) || !box_inside(r.lo, r.hi, e[pick].lo, e[pick].hi))
+                ok = false;
+            for (int k = n; k > pick + 1; --k) e[k] = e[k - 1];
+            e[pick] = l;
+            e[pick + 1] = r;
+            ++n;
+        }
+        const int32_t me = (int32_t)(out->size() / 32);
+        out->resize(out->size() + 32, 0.0f);
+        int32_t links[4] = {kNoChild, kNoChild, kNoChild, kNoChild};
+        for (int k = 0; k < n; ++k) links[k] = e[k].ref < 0 ? e[k].ref : build(e[k].ref, depth + 1);
+        float *d = out->data() + 32 * (size_t)me;
+        for (int pair = 0; pair < 2; ++pair) {
+            float *q = d + (pair == 0 ? 0 : 16);
+            for (int a = 0; a < 3; ++a) {
+                for (int j = 0; j < 2; ++j) {
+                    const int k = 2 * pair + j;
+                    // an empty slot repeats the last child's box (its link is kNoChild, so
+                    // the result is ignored; a copy decides like its original)
+                    const WEntry &src_e = e[k < n ? k : n - 1];
+                    q[4 * a + j] = src_e.lo[a];
+                    q[4 * a + 2 + j] = src_e.hi[a];
+                }
+            }
+        }
+        memcpy(d + 12, links, sizeof(links));
+        return me;
+    }
+};
+}  // namespace
+
+int32_t host_pack_wide(const rg_aabb_tree_node *src, int32_t n, std::vector<float> &out, int *wide_depth) {
+    out.clear();
+    if (n <= 0) return 0;
+    WideBuilder b;
+    b.src = src;
+    b.out = &out;
+    out.reserve((size_t)32 * (size_t)(n / 2 + 1));
+    b.build(0, 1);
+    if (wide_depth) *wide_depth = b.max_depth;
+    if (!b.ok) return -1;
+    return (int32_t)(out.size() / 32);
 }
 
 // True when a child box coordinate of some node is NaN (e.g. a tree built

@@ -2,6 +2,8 @@
 #pragma once
 #include <stdint.h>
 
+#include <vector>
+
 #include "../../include/restir_gb300.h"
 
 int host_build_bvh(const float *xyz, int32_t n, rg_aabb_tree_node *out_nodes, rg_triangle *out_tris,
@@ -14,6 +16,9 @@ void host_pack_nodes_preorder(const rg_aabb_tree_node *src, int32_t n, float *ds
 void host_tree_preorder(const rg_aabb_tree_node *src, int32_t n, rg_aabb_tree_node *dst);
 bool host_boxes_have_nan(const rg_aabb_tree_node *nodes, int32_t n);
 void host_pack_tris(const rg_triangle *src, int32_t n, float *dst12);
+// The 4-wide copy of a valid tree (32 floats per node; see host.cpp): node
+// count, or -1 when some child box lies outside its parent's box.
+int32_t host_pack_wide(const rg_aabb_tree_node *src, int32_t n, std::vector<float> &out, int *wide_depth);
 void srgb_lut_host(float *out256);
 int host_trace_gbuffer(const float *nodes16, int32_t n_nodes, const float *tris12, int32_t n_tris,
                        const rg_material *mats, int32_t n_mats, const rg_camera &cam, int32_t w, int32_t h,

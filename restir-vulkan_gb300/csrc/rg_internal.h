@@ -33,11 +33,26 @@ struct AliasLight {
     float4 alias_pos;  // light[alias].pos.xyz, luminance
 };
 
+// WNode 128 B: the 4-wide copy of the tree (host_pack_wide) walked by shadow
+// rays on the filtered fast path; the first 64 bytes have GNode's layout
+// (children 0 and 1, then the links of all four children), so one walk reads
+// both copies.  Links: >= 0 node, < 0 triangle ~t, kWideNoChild = empty.
+struct WNode {
+    float4 a, b, c;   // children 0, 1: per axis lo0 lo1 hi0 hi1
+    int4 d;           // links of children 0..3
+    float4 e, f, g;   // children 2, 3 as a, b, c
+    float4 pad;
+};
+constexpr int32_t kWideNoChild = INT32_MIN;
+
 struct DevScene {
     const GNode *nodes;
     int32_t n_nodes;
     int32_t depth;                // validated tree depth (root = 1): traversal stack size
     int32_t box_nan;              // some node box coordinate is NaN: shadow rays use exact slab tests only
+    const WNode *wide;            // 4-wide copy, or null (containment failed, NaN boxes, too deep)
+    int32_t n_wide;
+    int32_t wide_stack;           // stack entries the 4-wide walk may need (3 per level)
     const GTri *tris;
     int32_t n_tris;
     const AliasLight *alias;      // point-light scenes

@@ -14,7 +14,14 @@
 // (src/shaders/include/softwareRaytracing.glsl:42-85): the any-hit answer is
 // an OR over every triangle whose whole box path passes the slab test, which
 // does not depend on the visiting order; every slab and triangle test uses
-// the exact arithmetic of rg_math.cuh.
+// the exact arithmetic of rg_math.cuh.  On the 4-wide copy of the tree a
+// path skips the boxes that the collapse expanded; for rays on the filtered
+// fast path (no zero, tiny or huge direction component, no NaN box) the
+// reference's slab test is monotone under box containment (t = RN((b-o)/d)
+// is monotone in b, so a contained box has a later entry and an earlier exit
+// on every axis), and the upload checks that every child box lies inside its
+// parent's, so a box that passes implies that the skipped boxes above it
+// pass: the set of triangles tested, and the answer, are unchanged.
 #pragma once
 #include "rg_internal.h"
 #include "rg_math.cuh"
@@ -221,6 +228,14 @@ struct TraceStats {
 // walk longer than one visit per node or a stack overflow (malformed tree;
 // not reachable for trees validated at upload).  Every thread of the block
 // must call it, and the block size must be a multiple of 32.
+//
+// Two copies of the tree are walked by the same code: rays on the filtered
+// fast path walk the 4-wide copy (DevScene::wide, when the upload built it),
+// the others the reference's binary tree with exact slab tests.  A node visit
+// reads children 0 and 1 and the four links (the first 64 bytes, GNode's
+// layout in both copies); children 2 and 3 only where the node has them.
+// Hit leaves are parked as a mask over the node's four links and tested in
+// the warp's triangle phase.
 template <typename Fetch, typename Endpoint, typename Emit>
 __device__ void trace_pool_f(const DevScene &s, Fetch fetch, int n, int *next, int *stack, int depth,
                              TraceStats &ts, Endpoint endpoint, Emit emit) {
@@ -237,10 +252,14 @@ __device__ void trace_pool_f(const DevScene &s, Fetch fetch, int n, int *next, i
     int cur = -1;          // pool index of this lane's segment, -1: none
     bool retired = false;  // the pool has no segment left for this lane
     int owner = 0, node = 0, sp = 0, visits = 0;
-    int leaf0 = -1, leaf1 = -1;  // parked triangle tests
-    bool walked = false;         // tree walk finished, only parked triangles remain
+    unsigned leafmask = 0; // parked triangle tests: links of leaf_node
+    int leaf_node = 0;
+    bool walked = false;   // tree walk finished, only parked triangles remain
     f3 o = mk(0.f, 0.f, 0.f), d = o, inv = o;
     bool fast = true;
+    const float4 *tree = reinterpret_cast<const float4 *>(s.nodes);  // this lane's copy of the tree
+    int stride = 4;        // float4 words per node: 4 binary, 8 four-wide
+    int limit = s.n_nodes, cap = depth;
     while (true) {
         // 1. refill idle lanes, several at a time
         const bool idle = !retired && cur < 0;
@@ -257,33 +276,48 @@ __device__ void trace_pool_f(const DevScene &s, Fetch fetch, int n, int *next, i
                     owner = fetch(k, p1);
                     rgm::shadow_segment(p1, endpoint(owner), o, d);
                     fast = ray_inverse(d, inv) && !s.box_nan;
+                    const bool wide = fast && s.wide != nullptr;
+                    tree = wide ? reinterpret_cast<const float4 *>(s.wide) : reinterpret_cast<const float4 *>(s.nodes);
+                    stride = wide ? 8 : 4;
+                    limit = wide ? s.n_wide : s.n_nodes;
+                    cap = wide ? s.wide_stack : depth;
                     node = 0;
                     sp = 0;
                     visits = 0;
-                    leaf0 = leaf1 = -1;
+                    leafmask = 0;
                     walked = false;
                     if (s.n_nodes <= 0) {  // single-triangle scene: no tree
-                        leaf0 = s.n_tris > 0 ? 0 : -1;
                         walked = true;
-                        if (leaf0 < 0) { emit(owner, false); cur = -1; }
+                        if (s.n_tris > 0) {
+                            bool hit = tri_hit(s.tris, 0, o, d);
+                            ++ts.tri_tests;
+                            emit(owner, hit);
+                        } else {
+                            emit(owner, false);
+                        }
+                        cur = -1;
                     }
                 }
             }
         }
         if (__all_sync(kFull, retired)) break;
         // 2. parked triangle tests
-        const bool has_leaf = cur >= 0 && leaf0 >= 0;
+        const bool has_leaf = cur >= 0 && leafmask != 0u;
         const unsigned m_leaf = __ballot_sync(kFull, has_leaf);
-        const unsigned m_walk = __ballot_sync(kFull, cur >= 0 && leaf0 < 0 && !walked);
+        const unsigned m_walk = __ballot_sync(kFull, cur >= 0 && leafmask == 0u && !walked);
         if (m_leaf != 0u && (__popc(m_leaf) >= RG_LEAF_MIN || m_walk == 0u)) {
             if (has_leaf) {
-                bool hit = tri_hit(s.tris, leaf0, o, d);
-                ++ts.tri_tests;
-                if (!hit && leaf1 >= 0) {
-                    hit = tri_hit(s.tris, leaf1, o, d);
-                    ++ts.tri_tests;
+                const int4 ch = __ldg(reinterpret_cast<const int4 *>(tree + (size_t)leaf_node * stride) + 3);
+                bool hit = false;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    if (!hit && (leafmask & (1u << k))) {
+                        const int link = k == 0 ? ch.x : k == 1 ? ch.y : k == 2 ? ch.z : ch.w;
+                        hit = tri_hit(s.tris, ~link, o, d);
+                        ++ts.tri_tests;
+                    }
                 }
-                leaf0 = leaf1 = -1;
+                leafmask = 0u;
                 if (hit || walked) {
                     emit(owner, hit);
                     cur = -1;
@@ -293,54 +327,68 @@ __device__ void trace_pool_f(const DevScene &s, Fetch fetch, int n, int *next, i
         }
         // 3. up to RG_WALK_STEPS nodes per walking lane
 #pragma unroll 1
-        for (int step = 0; step < RG_WALK_STEPS && cur >= 0 && leaf0 < 0 && !walked; ++step) {
+        for (int step = 0; step < RG_WALK_STEPS && cur >= 0 && leafmask == 0u && !walked; ++step) {
             ++ts.visits;
-            if (++visits > s.n_nodes) {
+            if (++visits > limit) {
                 ts.err = true;
                 emit(owner, false);
                 cur = -1;
                 continue;
             }
-            const GNode *np = s.nodes + node;
-            const float4 na = __ldg(&np->a), nb = __ldg(&np->b), nc = __ldg(&np->c);
-            const int4 ch = __ldg(&np->d);
-            // both filtered tests at once, then the rare exact retests
-            bool hl = false, hr = false;
-            if (!fast || boxes_filtered(o, inv, na, nb, nc, hl, hr)) {
+            const float4 *np = tree + (size_t)node * stride;
+            const float4 na = __ldg(np), nb = __ldg(np + 1), nc = __ldg(np + 2);
+            const int4 ch = __ldg(reinterpret_cast<const int4 *>(np) + 3);
+            // both filtered tests of a pair at once, then the rare exact retests
+            bool h0 = false, h1 = false, h2 = false, h3 = false;
+            if (!fast || boxes_filtered(o, inv, na, nb, nc, h0, h1)) {
                 const int e = boxes_exact(o, d, na, nb, nc);
-                hl = (e & 1) != 0;
-                hr = (e & 2) != 0;
+                h0 = (e & 1) != 0;
+                h1 = (e & 2) != 0;
             }
-            if (hl && ch.x < 0) leaf0 = ~ch.x;
-            if (hr && ch.y < 0) {
-                if (leaf0 < 0) leaf0 = ~ch.y;
-                else leaf1 = ~ch.y;
-            }
-            const bool il = hl && ch.x >= 0, ir = hr && ch.y >= 0;
-            if (il && ir) {
-                // left child first (measured faster than nearer-child-first,
-                // with as many node visits; with the device copy of the tree
-                // in preorder the left child is the next node in memory)
-                node = ch.x;
-                if (sp >= depth) {
-                    ts.err = true;
-                    emit(owner, false);
-                    cur = -1;
-                    leaf0 = leaf1 = -1;
-                    continue;
+            if (ch.z != kWideNoChild) {  // children 2 and 3 (4-wide copy: fast rays only)
+                const float4 ne = __ldg(np + 4), nf = __ldg(np + 5), ng = __ldg(np + 6);
+                if (boxes_filtered(o, inv, ne, nf, ng, h2, h3)) {
+                    const int e = boxes_exact(o, d, ne, nf, ng);
+                    h2 = (e & 1) != 0;
+                    h3 = (e & 2) != 0;
                 }
-                my_stack[sp * nthreads] = ch.y;
-                ++sp;
-            } else if (il) {
-                node = ch.x;
-            } else if (ir) {
-                node = ch.y;
+                h3 = h3 && ch.w != kWideNoChild;
+            }
+            leafmask = (h0 && ch.x < 0 ? 1u : 0u) | (h1 && ch.y < 0 ? 2u : 0u) | (h2 && ch.z < 0 ? 4u : 0u) |
+                       (h3 && ch.w < 0 ? 8u : 0u);
+            if (leafmask) leaf_node = node;
+            // inner children in link order: the first is walked next (with the
+            // nodes in preorder it is the next node in memory), the others pushed
+            int nxt = -1;
+            bool overflow = false;
+            if (h3 && ch.w >= 0) nxt = ch.w;
+            if (h2 && ch.z >= 0) {
+                if (nxt >= 0) { if (sp < cap) my_stack[(sp++) * nthreads] = nxt; else overflow = true; }
+                nxt = ch.z;
+            }
+            if (h1 && ch.y >= 0) {
+                if (nxt >= 0) { if (sp < cap) my_stack[(sp++) * nthreads] = nxt; else overflow = true; }
+                nxt = ch.y;
+            }
+            if (h0 && ch.x >= 0) {
+                if (nxt >= 0) { if (sp < cap) my_stack[(sp++) * nthreads] = nxt; else overflow = true; }
+                nxt = ch.x;
+            }
+            if (overflow) {
+                ts.err = true;
+                emit(owner, false);
+                cur = -1;
+                leafmask = 0u;
+                continue;
+            }
+            if (nxt >= 0) {
+                node = nxt;
             } else if (sp > 0) {
                 --sp;
                 node = my_stack[sp * nthreads];
             } else {
                 walked = true;
-                if (leaf0 < 0) {
+                if (leafmask == 0u) {
                     emit(owner, false);
                     cur = -1;
                 }

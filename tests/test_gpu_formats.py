@@ -148,8 +148,9 @@ def test_passes_read_every_reference_format(ctx, cuda, scenes_fmt, combo):
 
 def test_formats_change_the_decoded_values(scenes_fmt):
     """The re-encoded planes are not the default ones in disguise: the SNORM
-    normals and the D24 depth decode to other floats than the default planes
-    for most pixels (so the bit-exact runs above exercise each decoder)."""
+    normals decode to other floats than the default planes for most pixels,
+    the D24 depth for some (so the bit-exact runs above exercise each
+    decoder)."""
     s, gs = scenes_fmt["biased"]
     g = gs[0]
     e = encode(g, F["RGB16_SNORM"], 0, F["D24S8"])
@@ -157,7 +158,7 @@ def test_formats_change_the_decoded_values(scenes_fmt):
     n_snorm = np.maximum(e["normal"].view(np.int16).astype(np.float32) / np.float32(32767.0), -1.0)
     assert np.mean(np.any(n_half != n_snorm, -1)) > 0.5
     d24 = (e["depth"] & 0xFFFFFF).astype(np.float32) / np.float32(16777215.0)
-    assert np.mean(d24 != g["depth"]) > 0.5
+    assert np.mean(d24 != g["depth"]) > 0.01  # z/w near 1 is mostly on the 24-bit grid already
 
 
 def test_unknown_or_misaligned_formats_are_rejected(ctx, cuda, scenes_fmt, restir_lib):

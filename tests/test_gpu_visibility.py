@@ -130,3 +130,42 @@ def test_nan_box_bit_exact(ctx, cuda, cfg1_scene):
     assert np.array_equal(got, exp), f"{np.count_nonzero(got != exp)} of {len(got)} bits differ"
     _, exp_clean = _gpu_vs_oracle(ctx, cuda, s, p1, p2)
     assert np.count_nonzero(exp != exp_clean) > 0  # the NaN changed the answers
+
+
+def test_wide_copy_on_config3_bit_exact(ctx, cuda):
+    """1,048,588 triangles: the upload builds the 4-wide copy (every child box
+    nested in its parent's), and fast-path rays walk it; segments aimed at the
+    boxes of the reference's tree (among them the boxes the collapse skips)
+    and pixel-to-light style segments equal the oracle's bits."""
+    from restir_gb300 import scenes
+    s = scenes.config3(width=64, height=64, frames=1)
+    p1, p2 = _segments(s, seed=21, n=60_000)
+    rng = np.random.default_rng(22)
+    m = 200_000
+    q1 = np.zeros((m, 4), np.float32)
+    q2 = np.zeros((m, 4), np.float32)
+    q1[:, :3] = rng.uniform(0.0, 1.0, (m, 3))
+    q2[:, :3] = s.point_lights["pos"][rng.integers(0, len(s.point_lights), m), :3]
+    p1, p2 = np.concatenate([p1, q1]), np.concatenate([p2, q2])
+    got, exp = _gpu_vs_oracle(ctx, cuda, s, p1, p2)
+    assert ctx.stats().wide_nodes > 0
+    bad = np.nonzero(got != exp)[0]
+    assert len(bad) == 0, f"{len(bad)} of {len(got)} visibility bits differ, first at {bad[:8]}"
+    assert 0.05 < exp.mean() < 0.95
+
+
+def test_wide_copy_left_out_when_boxes_are_not_nested(ctx, cuda, cfg1_scene):
+    """A tree whose root stores a left box smaller than its left child's boxes
+    (possible for a tree handed to rg_upload_scene): skipping boxes would no
+    longer keep the answer, so no 4-wide copy is built and every ray walks
+    the reference's tree."""
+    s = cfg1_scene
+    nodes = s.nodes.copy()
+    nodes["lmax"][0, :3] -= np.float32(0.3)
+    sn = dataclasses.replace(s, nodes=nodes)
+    p1, p2 = _segments(s, seed=23, n=30_000)
+    got, exp = _gpu_vs_oracle(ctx, cuda, sn, p1, p2)
+    assert ctx.stats().wide_nodes == 0
+    assert np.array_equal(got, exp), f"{np.count_nonzero(got != exp)} of {len(got)} bits differ"
+    ctx.upload_scene(s)
+    assert ctx.stats().wide_nodes > 0
