@@ -228,16 +228,10 @@ struct TraceStats {
 // walk longer than one visit per node or a stack overflow (malformed tree;
 // not reachable for trees validated at upload).  Every thread of the block
 // must call it, and the block size must be a multiple of 32.
-//
-// Two copies of the tree are walked by the same code: rays on the filtered
-// fast path walk the 4-wide copy (DevScene::wide, when the upload built it),
-// the others the reference's binary tree with exact slab tests.  A node visit
-// reads children 0 and 1 and the four links (the first 64 bytes, GNode's
-// layout in both copies); children 2 and 3 only where the node has them.
-// Hit leaves are parked as a mask over the node's four links and tested in
-// the warp's triangle phase.
+// (The walk over the reference's binary tree, for scenes without the 4-wide
+// copy.)
 template <typename Fetch, typename Endpoint, typename Emit>
-__device__ void trace_pool_f(const DevScene &s, Fetch fetch, int n, int *next, int *stack, int depth,
+__device__ void trace_binary_loop(const DevScene &s, Fetch fetch, int n, int *next, int *stack, int depth,
                              TraceStats &ts, Endpoint endpoint, Emit emit) {
     constexpr unsigned kFull = 0xffffffffu;
 #if RG_STACK_LOCAL
@@ -252,14 +246,10 @@ __device__ void trace_pool_f(const DevScene &s, Fetch fetch, int n, int *next, i
     int cur = -1;          // pool index of this lane's segment, -1: none
     bool retired = false;  // the pool has no segment left for this lane
     int owner = 0, node = 0, sp = 0, visits = 0;
-    unsigned leafmask = 0; // parked triangle tests: links of leaf_node
-    int leaf_node = 0;
-    bool walked = false;   // tree walk finished, only parked triangles remain
+    int leaf0 = -1, leaf1 = -1;  // parked triangle tests
+    bool walked = false;         // tree walk finished, only parked triangles remain
     f3 o = mk(0.f, 0.f, 0.f), d = o, inv = o;
     bool fast = true;
-    const float4 *tree = reinterpret_cast<const float4 *>(s.nodes);  // this lane's copy of the tree
-    int stride = 4;        // float4 words per node: 4 binary, 8 four-wide
-    int limit = s.n_nodes, cap = depth;
     while (true) {
         // 1. refill idle lanes, several at a time
         const bool idle = !retired && cur < 0;
@@ -276,26 +266,176 @@ __device__ void trace_pool_f(const DevScene &s, Fetch fetch, int n, int *next, i
                     owner = fetch(k, p1);
                     rgm::shadow_segment(p1, endpoint(owner), o, d);
                     fast = ray_inverse(d, inv) && !s.box_nan;
-                    const bool wide = fast && s.wide != nullptr;
-                    tree = wide ? reinterpret_cast<const float4 *>(s.wide) : reinterpret_cast<const float4 *>(s.nodes);
-                    stride = wide ? 8 : 4;
-                    limit = wide ? s.n_wide : s.n_nodes;
-                    cap = wide ? s.wide_stack : depth;
                     node = 0;
                     sp = 0;
                     visits = 0;
-                    leafmask = 0;
+                    leaf0 = leaf1 = -1;
                     walked = false;
                     if (s.n_nodes <= 0) {  // single-triangle scene: no tree
+                        leaf0 = s.n_tris > 0 ? 0 : -1;
                         walked = true;
-                        if (s.n_tris > 0) {
-                            bool hit = tri_hit(s.tris, 0, o, d);
-                            ++ts.tri_tests;
-                            emit(owner, hit);
-                        } else {
-                            emit(owner, false);
-                        }
-                        cur = -1;
+                        if (leaf0 < 0) { emit(owner, false); cur = -1; }
+                    }
+                }
+            }
+        }
+        if (__all_sync(kFull, retired)) break;
+        // 2. parked triangle tests
+        const bool has_leaf = cur >= 0 && leaf0 >= 0;
+        const unsigned m_leaf = __ballot_sync(kFull, has_leaf);
+        const unsigned m_walk = __ballot_sync(kFull, cur >= 0 && leaf0 < 0 && !walked);
+        if (m_leaf != 0u && (__popc(m_leaf) >= RG_LEAF_MIN || m_walk == 0u)) {
+            if (has_leaf) {
+                bool hit = tri_hit(s.tris, leaf0, o, d);
+                ++ts.tri_tests;
+                if (!hit && leaf1 >= 0) {
+                    hit = tri_hit(s.tris, leaf1, o, d);
+                    ++ts.tri_tests;
+                }
+                leaf0 = leaf1 = -1;
+                if (hit || walked) {
+                    emit(owner, hit);
+                    cur = -1;
+                }
+            }
+            continue;
+        }
+        // 3. up to RG_WALK_STEPS nodes per walking lane
+#pragma unroll 1
+        for (int step = 0; step < RG_WALK_STEPS && cur >= 0 && leaf0 < 0 && !walked; ++step) {
+            ++ts.visits;
+            if (++visits > s.n_nodes) {
+                ts.err = true;
+                emit(owner, false);
+                cur = -1;
+                continue;
+            }
+            const GNode *np = s.nodes + node;
+            const float4 na = __ldg(&np->a), nb = __ldg(&np->b), nc = __ldg(&np->c);
+            const int4 ch = __ldg(&np->d);
+            // both filtered tests at once, then the rare exact retests
+            bool hl = false, hr = false;
+            if (!fast || boxes_filtered(o, inv, na, nb, nc, hl, hr)) {
+                const int e = boxes_exact(o, d, na, nb, nc);
+                hl = (e & 1) != 0;
+                hr = (e & 2) != 0;
+            }
+            if (hl && ch.x < 0) leaf0 = ~ch.x;
+            if (hr && ch.y < 0) {
+                if (leaf0 < 0) leaf0 = ~ch.y;
+                else leaf1 = ~ch.y;
+            }
+            const bool il = hl && ch.x >= 0, ir = hr && ch.y >= 0;
+            if (il && ir) {
+                // left child first (measured faster than nearer-child-first,
+                // with as many node visits; with the device copy of the tree
+                // in preorder the left child is the next node in memory)
+                node = ch.x;
+                if (sp >= depth) {
+                    ts.err = true;
+                    emit(owner, false);
+                    cur = -1;
+                    leaf0 = leaf1 = -1;
+                    continue;
+                }
+                my_stack[sp * nthreads] = ch.y;
+                ++sp;
+            } else if (il) {
+                node = ch.x;
+            } else if (ir) {
+                node = ch.y;
+            } else if (sp > 0) {
+                --sp;
+                node = my_stack[sp * nthreads];
+            } else {
+                walked = true;
+                if (leaf0 < 0) {
+                    emit(owner, false);
+                    cur = -1;
+                }
+            }
+        }
+    }
+}
+
+// The exact any-hit walk of one segment over the reference's binary tree, for
+// the rays the 4-wide walk does not take (a zero, tiny or huge direction
+// component): both child boxes tested by division, leaves at once.  Kept out
+// of line, so its registers do not weigh on the 4-wide loop.
+__device__ __noinline__ bool trace_exact_binary(const DevScene &s, f3 o, f3 d, TraceStats &ts) {
+    int stack[RG_MAX_TREE_DEPTH + 1];
+    int sp = 0, node = 0, visits = 0;
+    for (;;) {
+        ++ts.visits;
+        if (++visits > s.n_nodes) { ts.err = true; return false; }
+        const GNode *np = s.nodes + node;
+        const float4 na = __ldg(&np->a), nb = __ldg(&np->b), nc = __ldg(&np->c);
+        const int4 ch = __ldg(&np->d);
+        const int e = boxes_exact(o, d, na, nb, nc);
+        int nxt = -1;
+        if (e & 2) {
+            if (ch.y < 0) { ++ts.tri_tests; if (tri_hit(s.tris, ~ch.y, o, d)) return true; }
+            else nxt = ch.y;
+        }
+        if (e & 1) {
+            if (ch.x < 0) { ++ts.tri_tests; if (tri_hit(s.tris, ~ch.x, o, d)) return true; }
+            else {
+                if (nxt >= 0) {
+                    if (sp >= s.depth) { ts.err = true; return false; }
+                    stack[sp++] = nxt;
+                }
+                nxt = ch.x;
+            }
+        }
+        if (nxt >= 0) node = nxt;
+        else if (sp > 0) node = stack[--sp];
+        else return false;
+    }
+}
+
+// The same loop over the 4-wide copy of the tree (DevScene::wide): a node
+// visit tests its four child boxes as two packed pairs; hit leaves are parked
+// as a mask over the node's links and tested in the warp's triangle phase;
+// the first hit inner child is walked next (the next node in memory: the copy
+// is in preorder), the others pushed.  The stack needs at most three entries
+// per level of the copy, which the upload checks against its 64 entries, and
+// every node is visited at most once per segment (a tree).  Rays off the
+// filtered fast path take trace_exact_binary as soon as they are fetched.
+template <typename Fetch, typename Endpoint, typename Emit>
+__device__ void trace_wide_loop(const DevScene &s, Fetch fetch, int n, int *next, TraceStats &ts, Endpoint endpoint,
+                                Emit emit) {
+    constexpr unsigned kFull = 0xffffffffu;
+    int my_stack[RG_MAX_TREE_DEPTH + 1];
+    int cur = -1;          // pool index of this lane's segment, -1: none
+    bool retired = false;  // the pool has no segment left for this lane
+    int owner = 0, node = 0, sp = 0, visits = 0;
+    unsigned leafmask = 0; // parked triangle tests: links of leaf_node
+    int leaf_node = 0;
+    bool walked = false;   // tree walk finished, only parked triangles remain
+    f3 o = mk(0.f, 0.f, 0.f), d = o, inv = o;
+    while (true) {
+        // 1. refill idle lanes, several at a time
+        const bool idle = !retired && cur < 0;
+        const unsigned m_idle = __ballot_sync(kFull, idle);
+        const unsigned m_busy = __ballot_sync(kFull, cur >= 0);
+        if (m_idle != 0u && (__popc(m_idle) >= RG_FETCH_MIN || m_busy == 0u)) {
+            if (idle) {
+                const int k = atomicAdd(next, 1);
+                if (k >= n) {
+                    retired = true;
+                } else {
+                    f3 p1;
+                    owner = fetch(k, p1);
+                    rgm::shadow_segment(p1, endpoint(owner), o, d);
+                    if (ray_inverse(d, inv)) {
+                        cur = k;
+                        node = 0;
+                        sp = 0;
+                        visits = 0;
+                        leafmask = 0u;
+                        walked = false;
+                    } else {
+                        emit(owner, trace_exact_binary(s, o, d, ts));
                     }
                 }
             }
@@ -307,15 +447,13 @@ __device__ void trace_pool_f(const DevScene &s, Fetch fetch, int n, int *next, i
         const unsigned m_walk = __ballot_sync(kFull, cur >= 0 && leafmask == 0u && !walked);
         if (m_leaf != 0u && (__popc(m_leaf) >= RG_LEAF_MIN || m_walk == 0u)) {
             if (has_leaf) {
-                const int4 ch = __ldg(reinterpret_cast<const int4 *>(tree + (size_t)leaf_node * stride) + 3);
+                const int4 ch = __ldg(&s.wide[leaf_node].d);
                 bool hit = false;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    if (!hit && (leafmask & (1u << k))) {
-                        const int link = k == 0 ? ch.x : k == 1 ? ch.y : k == 2 ? ch.z : ch.w;
-                        hit = tri_hit(s.tris, ~link, o, d);
-                        ++ts.tri_tests;
-                    }
+                for (unsigned m = leafmask; m != 0u && !hit; m &= m - 1u) {
+                    const int k = __ffs(m) - 1;
+                    const int link = k == 0 ? ch.x : k == 1 ? ch.y : k == 2 ? ch.z : ch.w;
+                    hit = tri_hit(s.tris, ~link, o, d);
+                    ++ts.tri_tests;
                 }
                 leafmask = 0u;
                 if (hit || walked) {
@@ -329,63 +467,50 @@ __device__ void trace_pool_f(const DevScene &s, Fetch fetch, int n, int *next, i
 #pragma unroll 1
         for (int step = 0; step < RG_WALK_STEPS && cur >= 0 && leafmask == 0u && !walked; ++step) {
             ++ts.visits;
-            if (++visits > limit) {
+            if (++visits > s.n_wide) {
                 ts.err = true;
                 emit(owner, false);
                 cur = -1;
                 continue;
             }
-            const float4 *np = tree + (size_t)node * stride;
-            const float4 na = __ldg(np), nb = __ldg(np + 1), nc = __ldg(np + 2);
-            const int4 ch = __ldg(reinterpret_cast<const int4 *>(np) + 3);
-            // both filtered tests of a pair at once, then the rare exact retests
+            const WNode *np = s.wide + node;
+            const float4 na = __ldg(&np->a), nb = __ldg(&np->b), nc = __ldg(&np->c);
+            const int4 ch = __ldg(&np->d);
+            const float4 ne = __ldg(&np->e), nf = __ldg(&np->f), ng = __ldg(&np->g);
             bool h0 = false, h1 = false, h2 = false, h3 = false;
-            if (!fast || boxes_filtered(o, inv, na, nb, nc, h0, h1)) {
+            if (boxes_filtered(o, inv, na, nb, nc, h0, h1)) {
                 const int e = boxes_exact(o, d, na, nb, nc);
                 h0 = (e & 1) != 0;
                 h1 = (e & 2) != 0;
             }
-            if (ch.z != kWideNoChild) {  // children 2 and 3 (4-wide copy: fast rays only)
-                const float4 ne = __ldg(np + 4), nf = __ldg(np + 5), ng = __ldg(np + 6);
-                if (boxes_filtered(o, inv, ne, nf, ng, h2, h3)) {
-                    const int e = boxes_exact(o, d, ne, nf, ng);
-                    h2 = (e & 1) != 0;
-                    h3 = (e & 2) != 0;
-                }
-                h3 = h3 && ch.w != kWideNoChild;
+            if (boxes_filtered(o, inv, ne, nf, ng, h2, h3)) {
+                const int e = boxes_exact(o, d, ne, nf, ng);
+                h2 = (e & 1) != 0;
+                h3 = (e & 2) != 0;
             }
+            h2 = h2 && ch.z != kWideNoChild;
+            h3 = h3 && ch.w != kWideNoChild;
             leafmask = (h0 && ch.x < 0 ? 1u : 0u) | (h1 && ch.y < 0 ? 2u : 0u) | (h2 && ch.z < 0 ? 4u : 0u) |
                        (h3 && ch.w < 0 ? 8u : 0u);
             if (leafmask) leaf_node = node;
-            // inner children in link order: the first is walked next (with the
-            // nodes in preorder it is the next node in memory), the others pushed
             int nxt = -1;
-            bool overflow = false;
             if (h3 && ch.w >= 0) nxt = ch.w;
             if (h2 && ch.z >= 0) {
-                if (nxt >= 0) { if (sp < cap) my_stack[(sp++) * nthreads] = nxt; else overflow = true; }
+                if (nxt >= 0) my_stack[sp++] = nxt;
                 nxt = ch.z;
             }
             if (h1 && ch.y >= 0) {
-                if (nxt >= 0) { if (sp < cap) my_stack[(sp++) * nthreads] = nxt; else overflow = true; }
+                if (nxt >= 0) my_stack[sp++] = nxt;
                 nxt = ch.y;
             }
             if (h0 && ch.x >= 0) {
-                if (nxt >= 0) { if (sp < cap) my_stack[(sp++) * nthreads] = nxt; else overflow = true; }
+                if (nxt >= 0) my_stack[sp++] = nxt;
                 nxt = ch.x;
-            }
-            if (overflow) {
-                ts.err = true;
-                emit(owner, false);
-                cur = -1;
-                leafmask = 0u;
-                continue;
             }
             if (nxt >= 0) {
                 node = nxt;
             } else if (sp > 0) {
-                --sp;
-                node = my_stack[sp * nthreads];
+                node = my_stack[--sp];
             } else {
                 walked = true;
                 if (leafmask == 0u) {
@@ -395,6 +520,15 @@ __device__ void trace_pool_f(const DevScene &s, Fetch fetch, int n, int *next, i
             }
         }
     }
+}
+
+// The block's walk: over the 4-wide copy when the upload built one, else
+// over the reference's tree.
+template <typename Fetch, typename Endpoint, typename Emit>
+__device__ __forceinline__ void trace_pool_f(const DevScene &s, Fetch fetch, int n, int *next, int *stack, int depth,
+                                             TraceStats &ts, Endpoint endpoint, Emit emit) {
+    if (s.wide != nullptr) trace_wide_loop(s, fetch, n, next, ts, endpoint, emit);
+    else trace_binary_loop(s, fetch, n, next, stack, depth, ts, endpoint, emit);
 }
 
 // trace_pool_f over a pool of Ray entries (start point and owner stored).

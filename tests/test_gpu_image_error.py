@@ -1,0 +1,65 @@
+"""Image error of the benchmarked configurations against the FP64 judge.
+
+The judge (oracle or_brute_force_fp64: every light, exact visibility, double
+precision) of each configuration's last frame on the centred 64x64 crop is
+committed (tests/golden/judge_config{2,3}.npz, tests/golden/make_judge.py:
+about two billion shadow rays for config 3).  Here the GPU renders the
+configuration's frame sequence in the benchmark's pass order, and the error
+of the last frame's crop is pinned: the passes are bit-exact against the
+oracle, so the error is a fixed number for a fixed input, and a change of it
+means a change of the estimator.  Beside it, the reference's default
+sequence (one unbiased pass with NUM_NEIGHBORS = 3, unbiasedReuse.glsl:48) on
+the same frames: chaining unbiased passes darkens the image (each pass adds
+every neighbour's M but normalises W by the visibility-filtered count,
+unbiasedReuse.glsl:116,168-182), the single pass much less.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import bench
+
+pytestmark = pytest.mark.gpu
+
+# (relative RMSE, relative bias) of the last frame's crop, measured on a
+# GB300; the bit-exact passes make them reproducible to rounding of the
+# double-precision reductions.
+PINNED = {
+    "config3": {"benched": None, "reference_default": None},
+    "config2": {"benched": None, "reference_default": None},
+}
+
+
+def _render(ctx, name, cuda):
+    from restir_gb300 import scenes
+    from restir_gb300.passes import DeviceGBuffer
+    s = scenes.CONFIGS[name]()
+    j = bench.judge_fixture(name)
+    assert j is not None, f"tests/golden/judge_{name}.npz missing"
+    ctx.upload_scene(s)
+    dgs = []
+    for f in range(j["frame"] + 1):
+        d = DeviceGBuffer(s.width, s.height)
+        ctx.trace_gbuffer(s.cameras[f], d)
+        dgs.append(d)
+    assert bench.crop_digest(dgs[-1].to_host(), j["crop"]) == j["digest"], "the judged G-buffer differs"
+    stream = cuda.cuda.current_stream()
+    bench_img = bench._sequence_images(ctx, s, dgs, j["frame"] + 1, s.spatial_passes, s.neighbors, j["crop"], stream)
+    ref_img = bench._sequence_images(ctx, s, dgs, j["frame"] + 1, 1, 3, j["crop"], stream)
+    return bench.rmse_against(bench_img, j["rgb"]), bench.rmse_against(ref_img, j["rgb"])
+
+
+@pytest.mark.parametrize("name", ["config3", "config2"])
+def test_crop_error_against_fp64_judge(ctx, cuda, name):
+    got, ref = _render(ctx, name, cuda)
+    print(name, "benched", got, "reference default", ref)
+    for key, e in (("benched", got), ("reference_default", ref)):
+        assert np.isfinite(e["rel_rmse"]) and np.isfinite(e["rel_bias"])
+        pin = PINNED[name][key]
+        if pin is not None:
+            assert abs(e["rel_rmse"] - pin[0]) <= 1e-9 * max(1.0, abs(pin[0])), (key, e, pin)
+            assert abs(e["rel_bias"] - pin[1]) <= 1e-9, (key, e, pin)
+    # the measured property of the reference's method: chained passes darken
+    assert got["rel_bias"] < ref["rel_bias"]
+    assert got["rel_bias"] < -0.3

@@ -155,17 +155,18 @@ def test_wide_copy_on_config3_bit_exact(ctx, cuda):
 
 
 def test_wide_copy_left_out_when_boxes_are_not_nested(ctx, cuda, cfg1_scene):
-    """A tree whose root stores a left box smaller than its left child's boxes
-    (possible for a tree handed to rg_upload_scene): skipping boxes would no
-    longer keep the answer, so no 4-wide copy is built and every ray walks
-    the reference's tree."""
+    """A tree whose root stores boxes smaller than its children's boxes
+    (possible for a tree handed to rg_upload_scene): the collapse must skip
+    one of those boxes, which would no longer keep the answer, so no 4-wide
+    copy is built and every ray walks the reference's tree."""
     s = cfg1_scene
     nodes = s.nodes.copy()
     nodes["lmax"][0, :3] -= np.float32(0.3)
+    nodes["rmax"][0, :3] -= np.float32(0.3)
     sn = dataclasses.replace(s, nodes=nodes)
     p1, p2 = _segments(s, seed=23, n=30_000)
     got, exp = _gpu_vs_oracle(ctx, cuda, sn, p1, p2)
-    assert ctx.stats().wide_nodes == 0
     assert np.array_equal(got, exp), f"{np.count_nonzero(got != exp)} of {len(got)} bits differ"
+    assert ctx.stats().wide_nodes == 0
     ctx.upload_scene(s)
     assert ctx.stats().wide_nodes > 0
