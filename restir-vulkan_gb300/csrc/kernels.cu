@@ -596,109 +596,12 @@ __device__ __forceinline__ void spatial_biased_tile(const SpatialParams &p, int 
     store_resv(p.out, i, r);
 }
 
-// The same pass for one sample per reservoir with a one-neighbour lookahead.
-// Neighbour k+1's position depends on whether neighbour k's merge drew its
-// reservoir-update uniform (a draw only when the neighbour passes the depth
-// and normal tests and its weight is positive): of the next three PCG
-// outputs u0 u1 u2 after neighbour k's two draws, k+1 takes (u0, u1) without
-// that draw and (u1, u2) with it.  Both candidate positions are computed
-// while neighbour k is processed, their depth and normal loaded and their
-// reservoirs prefetched into L1, so the dependent memory round trips of
-// consecutive neighbours overlap; the draws, their order and the arithmetic
-// are those of spatial_biased_tile.
-__device__ __forceinline__ void prefetch_l1(const void *p) {
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-}
-struct BiasedCand {
-    size_t ni;
-    float depth;
-    f3 normal;
-};
-__device__ __forceinline__ BiasedCand biased_candidate(const SpatialParams &p, int x, int y, int W, int H, float ua,
-                                                       float ur) {
-    const float angle = ua * 2.0f * kPi;
-    const float radius = sqrtf(ur) * p.u.spatial_radius;
-    float sn, cs;
-    sincos_cw(angle, sn, cs);
-    const int nx = iclamp(x + (int)floorf(cs * radius), 0, W - 1);
-    const int ny = iclamp(y + (int)floorf(sn * radius), 0, H - 1);
-    BiasedCand c;
-    c.ni = (size_t)ny * (size_t)W + (size_t)nx;
-    c.depth = load_depth(p.g, c.ni);
-    c.normal = load_normal(p.g, c.ni);
-    prefetch_l1(reinterpret_cast<const float4 *>(p.in) + c.ni * 4);
-    return c;
-}
-template <bool MIS>
-__device__ __forceinline__ void spatial_biased_tile_lookahead(const SpatialParams &p, int bx, int by) {
-    const int x = bx * 32 + threadIdx.x;
-    const int y = by * 4 + threadIdx.y;
-    const int W = (int)p.u.screen_size[0], H = (int)p.u.screen_size[1];
-    if (x >= W || y >= H) return;
-    const size_t i = (size_t)y * (size_t)W + (size_t)x;
-    Texel t;
-    load_texel(p.g, i, t);
-    const float depth = load_depth(p.g, i);
-    const float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
-    const f3 cam = mk(p.u.camera_pos[0], p.u.camera_pos[1], p.u.camera_pos[2]);
-    const f3 wo = view_dir(cam, t.wpos);
-    ResV<1, MIS> r = load_resv<1, MIS>(p.in, i);
-    const bool swap_fix = (p.u.flags & RG_FLAG_MIS_SWAP_FIX) != 0;
-    Pcg rng = pcg_seed((uint64_t)(p.u.frame * 31u + (uint32_t)p.iter), (uint64_t)((uint32_t)y * 10007u + (uint32_t)x));
-    const uint32_t K = p.u.spatial_neighbors;
-    if (K == 0) {
-        store_resv(p.out, i, r);
-        return;
-    }
-    BiasedCand cur;
-    {
-        const float ua = rand_float(rng), ur = rand_float(rng);
-        cur = biased_candidate(p, x, y, W, H, ua, ur);
-    }
-    for (uint32_t k = 0; k < K; ++k) {
-        // the next neighbour's two candidates (without / with this merge's draw)
-        Pcg ahead = rng;
-        const float u0 = rand_float(ahead);
-        const uint64_t s1 = ahead.state;
-        const float u1 = rand_float(ahead);
-        const uint64_t s2 = ahead.state;
-        const float u2 = rand_float(ahead);
-        const uint64_t s3 = ahead.state;
-        (void)s1;
-        BiasedCand na, nb;
-        const bool more = k + 1 < K;
-        if (more) {
-            na = biased_candidate(p, x, y, W, H, u0, u1);
-            nb = biased_candidate(p, x, y, W, H, u1, u2);
-        }
-        bool drew = false;
-        if (!(fabsf(cur.depth - depth) > p.u.spatial_pos_threshold * fabsf(depth) || dot(cur.normal, t.normal) < p.cos_thr)) {
-            const ResV<1, MIS> rr = load_resv<1, MIS>(p.in, cur.ni);
-            float ph[1];
-            ph[0] = eval_phat_wo(t.wpos, xyz(rr.pos_lum[0]), wo, t.normal, xyz(rr.nrm[0]), rr.nrm[0].w > 0.5f,
-                                 albedo_lum, rr.pos_lum[0].w, t.roughness, t.metallic);
-            drew = ph[0] * rr.w[0] * (float)rr.m > 0.0f;  // combine_res draws exactly when this weight is positive
-            combine_res(r, rr, ph, swap_fix, rng);
-        }
-        if (more) {
-            cur = drew ? nb : na;
-            rng.state = drew ? s3 : s2;  // past the next neighbour's two draws
-        }
-    }
-    store_resv(p.out, i, r);
-}
-
-#ifndef RG_BIASED_LOOKAHEAD
-#define RG_BIASED_LOOKAHEAD 1
-#endif
-
 #ifndef RG_BIASED_MIN_BLOCKS
 #define RG_BIASED_MIN_BLOCKS 8
 #endif
 template <int R, bool MIS>
 __global__ void __launch_bounds__(128, RG_BIASED_MIN_BLOCKS) k_spatial_biased(const SpatialParams p) {
-    if (R == 1 && RG_BIASED_LOOKAHEAD) spatial_biased_tile_lookahead<MIS>(p, blockIdx.x, blockIdx.y);
-    else spatial_biased_tile<R, MIS>(p, blockIdx.x, blockIdx.y);
+    spatial_biased_tile<R, MIS>(p, blockIdx.x, blockIdx.y);
 }
 
 // ---------------------------------------------------------------- unbiased spatial (unbiasedReuse.glsl:50-185)
