@@ -279,6 +279,21 @@ int rg_trace_gbuffer_host(const rg_scene_desc *scene, const rg_camera *cam, int3
 int rg_set_reservoir_format(rg_context *ctx, int32_t samples, int32_t unbiased_mis);
 int rg_reservoir_bytes(rg_context *ctx);
 
+/* ---- device layout of the tree ----
+ * No counterpart in the reference.  RG_TREE_BINARY (the default): shadow
+ * rays walk the reference's own tree.  RG_TREE_WIDE4: rg_upload_scene also
+ * builds a copy collapsed to four children per node (each expanded box's
+ * children checked to lie inside it), which rays on the filtered slab test's
+ * fast path walk instead; results are unchanged (the slab test is monotone
+ * under box containment for those rays).  It halves the node visits per
+ * segment, but on a GB300 the binary walk measured faster (1080p, 1.05M
+ * triangles: 7.8 against 8.2 ms per unbiased spatial pass), hence the
+ * default.  Takes effect at the next upload;
+ * rg_stats.wide_nodes tells whether the copy was built. */
+#define RG_TREE_BINARY 0
+#define RG_TREE_WIDE4 1
+int rg_set_tree_layout(rg_context *ctx, int32_t layout);
+
 /* ---- scene upload (host pointers; copied to device, synchronous) ---- */
 int rg_upload_scene(rg_context *ctx, const rg_scene_desc *scene);
 

@@ -22,11 +22,7 @@
 #ifndef RG_NODE_PREORDER
 #define RG_NODE_PREORDER 1
 #endif
-// RG_WIDE_TREE: keep a 4-wide copy of the tree (host_pack_wide) for shadow
-// rays on the filtered fast path.
-#ifndef RG_WIDE_TREE
-#define RG_WIDE_TREE 1
-#endif
+
 
 namespace {
 
@@ -94,6 +90,7 @@ struct rg_context {
     int *mma_timeouts = nullptr;
     ProposalState *proposal = nullptr;  // learned proposal (proposal.cu), tied to the uploaded lights
     int res_samples = 1, res_mis = 0;   // reservoir format (rg_set_reservoir_format)
+    int tree_layout = RG_TREE_BINARY;   // rg_set_tree_layout, applied at the next upload
     size_t frame_bytes = 0;             // bytes per pixel of the frame driver's reservoir buffers
     // frame driver
     int fw = 0, fh = 0;
@@ -328,12 +325,13 @@ int rg_upload_scene(rg_context *ctx, const rg_scene_desc *sc) {
     host_pack_nodes(sc->nodes, sc->n_nodes, n16.data());
 #endif
     host_pack_tris(sc->triangles, sc->n_triangles, t12.data());
-    // the 4-wide copy for fast-path shadow rays (RG_WIDE_TREE=0 builds leave it out)
+    // the 4-wide copy for fast-path shadow rays (rg_set_tree_layout)
     const bool box_nan = host_boxes_have_nan(sc->nodes, sc->n_nodes);
     std::vector<float> w32;
     int wide_depth = 0;
     int32_t n_wide = -1;
-    if (RG_WIDE_TREE && sc->n_nodes > 0 && !box_nan) n_wide = host_pack_wide(sc->nodes, sc->n_nodes, w32, &wide_depth);
+    if (ctx->tree_layout == RG_TREE_WIDE4 && sc->n_nodes > 0 && !box_nan)
+        n_wide = host_pack_wide(sc->nodes, sc->n_nodes, w32, &wide_depth);
     const int wide_stack = 3 * wide_depth + 1;
     if (n_wide > 0 && wide_stack > RG_MAX_TREE_DEPTH + 1) n_wide = -1;
     e = dev_alloc(&ctx->nodes, (size_t)sc->n_nodes);
@@ -541,6 +539,15 @@ int rg_set_reservoir_format(rg_context *ctx, int32_t samples, int32_t unbiased_m
     ctx->res_mis = unbiased_mis;
     ctx->scene.res_samples = samples;
     ctx->scene.res_mis = unbiased_mis;
+    return RG_OK;
+}
+
+int rg_set_tree_layout(rg_context *ctx, int32_t layout) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (layout != RG_TREE_BINARY && layout != RG_TREE_WIDE4)
+        return fail(RG_ERR_INVALID_ARGUMENT, "tree layout must be RG_TREE_BINARY or RG_TREE_WIDE4");
+    ctx->tree_layout = layout;
     return RG_OK;
 }
 

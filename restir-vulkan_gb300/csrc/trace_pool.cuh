@@ -124,24 +124,6 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
     return y;
 }
 
-// min of three that is NaN when any operand is NaN
-__device__ __forceinline__ float min3nan(float a, float b, float c) {
-    float y;
-    asm("min.NaN.f32 %0, %1, %2, %3;" : "=f"(y) : "f"(a), "f"(b), "f"(c));
-    return y;
-}
-
-// RG_ARITH_DECISION: decide each of the six comparisons below by the sign of
-// a difference (IEEE subtraction with gradual underflow gives the sign of
-// a - b exactly, infinities included), so the three of a hit or a miss fold
-// into one three-input min or max and one compare: most of the work moves
-// from the integer/compare pipe to the FMA pipe.  A NaN difference decides
-// nothing: the hit's min propagates it (no hit), the miss's max drops it, as
-// the comparisons themselves do.
-#ifndef RG_ARITH_DECISION
-#define RG_ARITH_DECISION 1
-#endif
-
 // The filtered test's decision from a box's slab distances: sets hit or miss
 // when decided (never both), neither when undecided.
 __device__ __forceinline__ void filtered_decision(float rmin, float rmax, bool &hit, bool &miss) {
@@ -149,13 +131,8 @@ __device__ __forceinline__ void filtered_decision(float rmin, float rmax, bool &
     constexpr float kTiny = 8.0779356694631609e-28f; // 2^-90
     const float dd = rmax - rmin;
     const float ss = __fmaf_rn(kEps, fabsf(rmin) + fabsf(rmax), kTiny);
-#if RG_ARITH_DECISION
-    hit = min3nan((1.0f - kEps) - rmin, rmax - kTiny, dd - ss) > 0.0f;
-    miss = max3f(rmin - (1.0f + kEps), -kTiny - rmax, -ss - dd) > 0.0f;
-#else
     hit = rmin < 1.0f - kEps && rmax > kTiny && dd > ss;
     miss = rmin > 1.0f + kEps || rmax < -kTiny || dd < -ss;
-#endif
 }
 
 // The filtered test of both children of a node at once: lane .x of every

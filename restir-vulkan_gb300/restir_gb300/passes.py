@@ -188,6 +188,10 @@ class Context:
     def set_reservoir_format(self, samples: int, unbiased_mis: int):
         check(lib().rg_set_reservoir_format(self._h, samples, unbiased_mis))
 
+    def set_tree_layout(self, wide: bool):
+        """RG_TREE_WIDE4 (True) or RG_TREE_BINARY (False), from the next upload."""
+        check(lib().rg_set_tree_layout(self._h, 1 if wide else 0))
+
     def reservoir_bytes(self) -> int:
         return check(lib().rg_reservoir_bytes(self._h))
 

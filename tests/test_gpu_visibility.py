@@ -133,8 +133,9 @@ def test_nan_box_bit_exact(ctx, cuda, cfg1_scene):
 
 
 def test_wide_copy_on_config3_bit_exact(ctx, cuda):
-    """1,048,588 triangles: the upload builds the 4-wide copy (every child box
-    nested in its parent's), and fast-path rays walk it; segments aimed at the
+    """1,048,588 triangles with RG_TREE_WIDE4: the upload builds the 4-wide
+    copy (every expanded box's children nested in it), and fast-path rays
+    walk it; segments aimed at the
     boxes of the reference's tree (among them the boxes the collapse skips)
     and pixel-to-light style segments equal the oracle's bits."""
     from restir_gb300 import scenes
@@ -147,8 +148,12 @@ def test_wide_copy_on_config3_bit_exact(ctx, cuda):
     q1[:, :3] = rng.uniform(0.0, 1.0, (m, 3))
     q2[:, :3] = s.point_lights["pos"][rng.integers(0, len(s.point_lights), m), :3]
     p1, p2 = np.concatenate([p1, q1]), np.concatenate([p2, q2])
-    got, exp = _gpu_vs_oracle(ctx, cuda, s, p1, p2)
-    assert ctx.stats().wide_nodes > 0
+    ctx.set_tree_layout(True)
+    try:
+        got, exp = _gpu_vs_oracle(ctx, cuda, s, p1, p2)
+        assert ctx.stats().wide_nodes > 0
+    finally:
+        ctx.set_tree_layout(False)
     bad = np.nonzero(got != exp)[0]
     assert len(bad) == 0, f"{len(bad)} of {len(got)} visibility bits differ, first at {bad[:8]}"
     assert 0.05 < exp.mean() < 0.95
@@ -165,8 +170,12 @@ def test_wide_copy_left_out_when_boxes_are_not_nested(ctx, cuda, cfg1_scene):
     nodes["rmax"][0, :3] -= np.float32(0.3)
     sn = dataclasses.replace(s, nodes=nodes)
     p1, p2 = _segments(s, seed=23, n=30_000)
-    got, exp = _gpu_vs_oracle(ctx, cuda, sn, p1, p2)
-    assert np.array_equal(got, exp), f"{np.count_nonzero(got != exp)} of {len(got)} bits differ"
-    assert ctx.stats().wide_nodes == 0
-    ctx.upload_scene(s)
-    assert ctx.stats().wide_nodes > 0
+    ctx.set_tree_layout(True)
+    try:
+        got, exp = _gpu_vs_oracle(ctx, cuda, sn, p1, p2)
+        assert np.array_equal(got, exp), f"{np.count_nonzero(got != exp)} of {len(got)} bits differ"
+        assert ctx.stats().wide_nodes == 0
+        ctx.upload_scene(s)
+        assert ctx.stats().wide_nodes > 0
+    finally:
+        ctx.set_tree_layout(False)
