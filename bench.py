@@ -713,7 +713,14 @@ def learned_section(dev: int, iters: int = 10, width: int = 1920, height: int = 
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak_tf = float(peaks.get("bf16_tflops", 1900.0))
     tf = flops / (infer_ms / 1000.0) / 1e12
-    return {"workload": f"config 4: {s.width}x{s.height}, {len(s.point_lights):,} point lights in {clusters} k-means "
+    equal = {}
+    for key, name in (("config4", "config2"), ("config3_1M_lights", "config3")):
+        try:
+            equal[key] = learned_equal_rmse(name)
+        except Exception as ex:  # reported, never hides the rest
+            equal[key] = {"error": f"{type(ex).__name__}: {ex}"}
+    return {"time_to_equal_rmse": equal,
+            "workload": f"config 4: {s.width}x{s.height}, {len(s.point_lights):,} point lights in {clusters} k-means "
                         "clusters, MLP 9-64-64-64-4096 (bf16, FP32 accumulation in tensor memory), mix 0.9",
             "inference_ms": round(infer_ms, 3), "ris_learned_ms": round(ris_l, 3), "ris_plain_ms": round(ris_p, 3),
             "train_step_ms": round(train_ms, 3), "train_batch": 65_536, "last_loss": round(loss, 4),
@@ -721,6 +728,41 @@ def learned_section(dev: int, iters: int = 10, width: int = 1920, height: int = 
                                  "peak_source": "measured bf16 burst" if "bf16_tflops" in peaks else "fallback",
                                  "frac": round(tf / peak_tf, 4), "flops_per_inference": flops},
             "kmeans_host_seconds": round(kmeans_s, 2), "mma_timeouts": int(stats.mma_timeouts)}
+
+
+def learned_equal_rmse(name: str, frames: int = 64, steps_per_frame: int = 3, lr: float = 1e-2) -> dict:
+    """GPU time for the learned proposal to reach the plain proposal's RMSE
+    against the FP64 judge (tests/learned_rmse.py's experiment: static camera
+    at the judged frame, RIS + visibility reuse + final RIS weight, running
+    mean of the frames; the learned arm's time includes inference and its
+    Adam steps).  config2: config 4's workload (65,536 lights, 4096 k-means
+    clusters); config3: 1,048,576 lights in their 4096 generating clusters."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import learned_rmse
+
+    from restir_gb300 import scenes
+    j = judge_fixture(name)
+    if j is None:
+        return {"error": f"tests/golden/judge_{name}.npz missing"}
+    s = scenes.CONFIGS[name]()
+
+    def check(g):
+        if crop_digest(g, j["crop"]) != j["digest"]:
+            raise RuntimeError("the judged G-buffer differs from this run's")
+
+    r = learned_rmse.run(scene=s, cam=j["frame"], judge=j["rgb"], crop=j["crop"], judge_check=check,
+                         cluster_of=s.extra.get("light_cluster"), frames=frames, clusters=4096,
+                         steps_per_frame=steps_per_frame, lr=lr, log=log)
+    eq = r["equal_rmse"]
+    return {"workload": r["workload"], "estimator": r["estimator"],
+            "gpu_time_to_equal_rmse": eq["time_fraction"], "target": 0.5,
+            "learned_frame_reaching_plain_final_rmse": eq["learned_frame"],
+            "rmse_ratio_at_equal_frames": round(r["rmse_ratio_at_equal_frames"], 4),
+            "plain_ms_per_frame": round(r["plain"]["ms_per_frame"], 3),
+            "learned_ms_per_frame": round(r["learned"]["ms_per_frame"], 3),
+            "plain_final_rel_rmse": round(r["plain"]["final_rel_rmse"], 4),
+            "learned_final_rel_rmse": round(r["learned"]["final_rel_rmse"], 4),
+            "adam_steps_per_frame": steps_per_frame, "learning_rate": lr, "frames": frames}
 
 
 # ------------------------------------------------------------------ batched views (config 5 workload)

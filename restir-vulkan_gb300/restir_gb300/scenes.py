@@ -354,8 +354,11 @@ def config3(seed: int = 3, width: int = 1920, height: int = 1080, grid=(64, 32, 
     rgb = tint / luminance_f32(tint[:, 0], tint[:, 1], tint[:, 2])[:, None] * power[:, None] * 0.05
     lights = make_point_lights(lpos, rgb)
     cams = camera_path(rng, frames, width / height)
+    # the Gaussian cluster of each light: a light clustering for the learned
+    # proposal at this scale (k-means over 1M lights is slow on the host)
     return _finish("config3", tri_xyz, mats, lights, width, height, cams, uniform_pdf=False, candidates=32,
-                   unbiased=True, spatial_passes=3, neighbors=5, radius=30.0, temporal=True, temporal_mult=20)
+                   unbiased=True, spatial_passes=3, neighbors=5, radius=30.0, temporal=True, temporal_mult=20,
+                   extra={"light_cluster": which.astype(np.int32)})
 
 
 def config5(seed: int = 5, n_views: int = 64, n_tris: int = 100_000, n_lights: int = 65_536,

@@ -35,18 +35,18 @@ for p in (ROOT / "restir-vulkan_gb300", ROOT / "oracle", ROOT / "tests"):
         sys.path.insert(0, str(p))
 
 
-def _arm(ctx, s, dg, res, image, crop, judge, frames, learned, steps_per_frame, candidates=32):
+def _arm(ctx, s, dg, res, image, crop, judge, frames, learned, steps_per_frame, candidates=32, cam=0):
     import torch
     from restir_gb300 import _lib
     x0, y0, cw, ch = crop
     acc = torch.zeros((ch, cw, 3), dtype=torch.float64, device="cuda")
     jt = torch.from_numpy(judge).cuda()
-    lu = s.lighting_uniforms(0)
+    lu = s.lighting_uniforms(cam)
     stream = torch.cuda.current_stream()
     cum_ms, rmse, loss = [], [], []
     total = 0.0
     for f in range(1, frames + 1):
-        u = s.uniforms(0)
+        u = s.uniforms(cam)
         u.frame = f
         u.flags = _lib.RG_FLAG_VISIBILITY_REUSE | _lib.RG_FLAG_FINAL_RIS_WEIGHT
         if learned:
@@ -61,7 +61,7 @@ def _arm(ctx, s, dg, res, image, crop, judge, frames, learned, steps_per_frame, 
         ctx.shade(dg, res, lu, image, stream)
         if learned:
             for k in range(steps_per_frame):
-                ut = s.uniforms(0)
+                ut = s.uniforms(cam)
                 ut.frame = f * steps_per_frame + k
                 ctx.proposal_train(dg, ut, res.data_ptr(), stream)
         e1.record(stream)
@@ -78,34 +78,45 @@ def _arm(ctx, s, dg, res, image, crop, judge, frames, learned, steps_per_frame, 
 
 def run(width=1920, height=1080, frames=64, clusters=4096, n_tris=100_000, n_lights=65_536, crop_size=64,
         lr=3e-3, steps_per_frame=1, batch=65_536, kmeans_iters=8, seed=4, log=print, learned_candidates=32,
-        zero_w4=False):
+        zero_w4=False, scene=None, cam=0, judge=None, crop=None, cluster_of=None, judge_check=None):
+    """scene (default: config 2's at width x height), the static camera index
+    cam, and optionally a precomputed judge of that view on crop (with
+    judge_check(host G-buffer) raising if it was judged on other planes) and
+    a light clustering (default: k-means)."""
     import torch
 
-    import oracle_binding as ob
     from restir_gb300 import scenes
     from restir_gb300.passes import Context, DeviceGBuffer, cluster_lights, reservoirs
 
     t0 = time.perf_counter()
-    s = scenes.config2(width=width, height=height, n_tris=n_tris, n_lights=n_lights, frames=1)
+    s = scene if scene is not None else scenes.config2(width=width, height=height, n_tris=n_tris,
+                                                         n_lights=n_lights, frames=1)
+    width, height = s.width, s.height
     ctx = Context(0)
     ctx.upload_scene(s)
     dg = DeviceGBuffer(s.width, s.height)
-    ctx.trace_gbuffer(s.cameras[0], dg)
-    crop = ((width - crop_size) // 2, (height - crop_size) // 2, crop_size, crop_size)
-    judge = ob.brute_force(s, dg.to_host(), s.cameras[0].basis()[0], crop=crop)
+    ctx.trace_gbuffer(s.cameras[cam], dg)
+    if judge_check is not None:  # the precomputed judge must be of this G-buffer
+        judge_check(dg.to_host())
+    if judge is None:
+        import oracle_binding as ob
+        crop = ((width - crop_size) // 2, (height - crop_size) // 2, crop_size, crop_size)
+        judge = ob.brute_force(s, dg.to_host(), s.cameras[cam].basis()[0], crop=crop)
+    crop_size = crop[2]
     t_judge = time.perf_counter() - t0
     log(f"scene + judge {t_judge:.1f}s")
     t1 = time.perf_counter()
-    cluster_of, _ = cluster_lights(s.point_lights, clusters, iterations=kmeans_iters, seed=seed)
+    if cluster_of is None:
+        cluster_of, _ = cluster_lights(s.point_lights, clusters, iterations=kmeans_iters, seed=seed)
     t_kmeans = time.perf_counter() - t1
     n = s.width * s.height
     res = reservoirs(n)
     image = torch.zeros((s.height, s.width, 4), dtype=torch.float32, device="cuda")
     # warm both paths (module load, first-launch attributes), then start fresh
     ctx.create_proposal(cluster_of, clusters, mix=0.9, learning_rate=lr, batch=batch, seed=seed)
-    _arm(ctx, s, dg, res, image, crop, judge, 2, True, 1)
-    _arm(ctx, s, dg, res, image, crop, judge, 2, False, 1)
-    plain_ms, plain_rmse, _ = _arm(ctx, s, dg, res, image, crop, judge, frames, False, 1)
+    _arm(ctx, s, dg, res, image, crop, judge, 2, True, 1, cam=cam)
+    _arm(ctx, s, dg, res, image, crop, judge, 2, False, 1, cam=cam)
+    plain_ms, plain_rmse, _ = _arm(ctx, s, dg, res, image, crop, judge, frames, False, 1, cam=cam)
     ctx.create_proposal(cluster_of, clusters, mix=0.9, learning_rate=lr, batch=batch, seed=seed)
     if zero_w4:  # the untrained proposal is then exactly the power-proportional one (plus the mixture)
         params = ctx.proposal_params()
@@ -113,7 +124,7 @@ def run(width=1920, height=1080, frames=64, clusters=4096, n_tris=100_000, n_lig
         params[n123:n123 + 64 * clusters] = 0.0
         ctx.set_proposal_params(params)
     lrn_ms, lrn_rmse, loss = _arm(ctx, s, dg, res, image, crop, judge, frames, True, steps_per_frame,
-                                  learned_candidates)
+                                  learned_candidates, cam=cam)
     st = ctx.stats()
     ctx.close()
     target = plain_rmse[-1]
@@ -122,8 +133,8 @@ def run(width=1920, height=1080, frames=64, clusters=4096, n_tris=100_000, n_lig
     judge_mean = float(judge.mean())
     every = max(1, frames // 16)
     return {
-        "workload": f"config 4: config 2 scene {width}x{height}, {n_tris} random triangles, {n_lights} point lights, "
-                    f"{clusters} k-means clusters, static camera, {frames} frames",
+        "workload": f"{s.name} scene {width}x{height}, {len(s.triangles):,} triangles, {len(s.point_lights):,} point "
+                    f"lights, {clusters} light clusters, static camera {cam}, {frames} frames",
         "estimator": f"RIS (plain 32, learned {learned_candidates} candidates) + visibility reuse + final RIS weight, "
                      "shaded; running mean of frames",
         "judge": f"FP64 brute force (every light, exact visibility) on a {crop_size}x{crop_size} crop at {crop[:2]}",
