@@ -15,6 +15,17 @@ import numpy as np
 from . import _lib
 
 
+def _dot3(a, b):
+    f32 = np.float32
+    return f32(f32(f32(a[0] * b[0]) + f32(a[1] * b[1])) + f32(a[2] * b[2]))
+
+
+def _cross3(a, b):
+    f32 = np.float32
+    return np.array([f32(a[1] * b[2]) - f32(a[2] * b[1]), f32(a[2] * b[0]) - f32(a[0] * b[2]),
+                     f32(a[0] * b[1]) - f32(a[1] * b[0])], f32)
+
+
 @dataclass
 class CameraModel:
     position: np.ndarray
@@ -26,22 +37,27 @@ class CameraModel:
     world_up: tuple = (0.0, 1.0, 0.0)
 
     def basis(self):
+        """Position and unit right, up, forward vectors in float32.  Every
+        operation is one IEEE operation on scalars in a fixed order (no BLAS
+        dot product, whose order and fused multiply-adds differ between
+        machines), so the camera is bit-identical on every host."""
         f32 = np.float32
         pos = np.asarray(self.position, f32)
-        fwd = np.asarray(self.look_at, f32) - pos
-        fwd = (fwd / np.sqrt(np.dot(fwd, fwd))).astype(f32)
-        right = np.cross(fwd, np.asarray(self.world_up, f32)).astype(f32)
-        right = (right / np.sqrt(np.dot(right, right))).astype(f32)
-        up = np.cross(right, fwd).astype(f32)
+        fwd = (np.asarray(self.look_at, f32) - pos).astype(f32)
+        fwd = (fwd / f32(np.sqrt(_dot3(fwd, fwd)))).astype(f32)
+        right = _cross3(fwd, np.asarray(self.world_up, f32))
+        right = (right / f32(np.sqrt(_dot3(right, right)))).astype(f32)
+        up = _cross3(right, fwd)
         return pos, right, up, fwd
 
     def view(self) -> np.ndarray:
         pos, right, up, fwd = self.basis()
         rot = np.stack([right, -up, fwd]).astype(np.float64)
-        off = -(rot @ pos.astype(np.float64))
         v = np.eye(4)
         v[:3, :3] = rot
-        v[:3, 3] = off
+        p = pos.astype(np.float64)
+        for i in range(3):  # -(rot @ pos), summed left to right
+            v[i, 3] = -((rot[i, 0] * p[0] + rot[i, 1] * p[1]) + rot[i, 2] * p[2])
         return v
 
     def projection(self) -> np.ndarray:
@@ -56,8 +72,14 @@ class CameraModel:
         return p
 
     def projection_view_colmajor(self) -> np.ndarray:
-        """P*V as 16 float32 in column-major order (GLSL mat4 memory layout)."""
-        return (self.projection() @ self.view()).astype(np.float32).T.reshape(16).copy()
+        """P*V as 16 float32 in column-major order (GLSL mat4 memory layout);
+        the product is summed left to right in double (no BLAS)."""
+        pm, vm = self.projection(), self.view()
+        pv = np.zeros((4, 4))
+        for i in range(4):
+            for j in range(4):
+                pv[i, j] = ((pm[i, 0] * vm[0, j] + pm[i, 1] * vm[1, j]) + pm[i, 2] * vm[2, j]) + pm[i, 3] * vm[3, j]
+        return pv.astype(np.float32).T.reshape(16).copy()
 
     def to_c(self) -> _lib.Camera:
         pos, right, up, fwd = self.basis()

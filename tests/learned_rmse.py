@@ -35,12 +35,13 @@ for p in (ROOT / "restir-vulkan_gb300", ROOT / "oracle", ROOT / "tests"):
         sys.path.insert(0, str(p))
 
 
-def _arm(ctx, s, dg, res, image, crop, judge, frames, learned, steps_per_frame, candidates=32, cam=0):
+def _arm(ctx, s, dg, res, image, crop, judge, frames, learned, steps_per_frame, candidates=32, cam=0, mask=None):
     import torch
     from restir_gb300 import _lib
     x0, y0, cw, ch = crop
     acc = torch.zeros((ch, cw, 3), dtype=torch.float64, device="cuda")
     jt = torch.from_numpy(judge).cuda()
+    mt = torch.from_numpy(np.ones(judge.shape[:2], bool) if mask is None else mask).cuda()
     lu = s.lighting_uniforms(cam)
     stream = torch.cuda.current_stream()
     cum_ms, rmse, loss = [], [], []
@@ -70,7 +71,7 @@ def _arm(ctx, s, dg, res, image, crop, judge, frames, learned, steps_per_frame, 
         acc += image[y0:y0 + ch, x0:x0 + cw, :3].double()
         err = acc / f - jt
         cum_ms.append(total)
-        rmse.append(float(torch.sqrt((err * err).mean())))
+        rmse.append(float(torch.sqrt((err[mt] ** 2).mean())))
         if learned:
             loss.append(ctx.proposal_last_loss()[0])
     return cum_ms, rmse, loss
@@ -78,11 +79,12 @@ def _arm(ctx, s, dg, res, image, crop, judge, frames, learned, steps_per_frame, 
 
 def run(width=1920, height=1080, frames=64, clusters=4096, n_tris=100_000, n_lights=65_536, crop_size=64,
         lr=3e-3, steps_per_frame=1, batch=65_536, kmeans_iters=8, seed=4, log=print, learned_candidates=32,
-        zero_w4=False, scene=None, cam=0, judge=None, crop=None, cluster_of=None, judge_check=None):
+        zero_w4=False, scene=None, cam=0, judge=None, crop=None, cluster_of=None, judge_check=None, mask=None):
     """scene (default: config 2's at width x height), the static camera index
     cam, and optionally a precomputed judge of that view on crop (with
     judge_check(host G-buffer) raising if it was judged on other planes) and
-    a light clustering (default: k-means)."""
+    a light clustering (default: k-means); mask selects the crop pixels the
+    RMSE is taken over (default: all)."""
     import torch
 
     from restir_gb300 import scenes
@@ -114,9 +116,9 @@ def run(width=1920, height=1080, frames=64, clusters=4096, n_tris=100_000, n_lig
     image = torch.zeros((s.height, s.width, 4), dtype=torch.float32, device="cuda")
     # warm both paths (module load, first-launch attributes), then start fresh
     ctx.create_proposal(cluster_of, clusters, mix=0.9, learning_rate=lr, batch=batch, seed=seed)
-    _arm(ctx, s, dg, res, image, crop, judge, 2, True, 1, cam=cam)
-    _arm(ctx, s, dg, res, image, crop, judge, 2, False, 1, cam=cam)
-    plain_ms, plain_rmse, _ = _arm(ctx, s, dg, res, image, crop, judge, frames, False, 1, cam=cam)
+    _arm(ctx, s, dg, res, image, crop, judge, 2, True, 1, cam=cam, mask=mask)
+    _arm(ctx, s, dg, res, image, crop, judge, 2, False, 1, cam=cam, mask=mask)
+    plain_ms, plain_rmse, _ = _arm(ctx, s, dg, res, image, crop, judge, frames, False, 1, cam=cam, mask=mask)
     ctx.create_proposal(cluster_of, clusters, mix=0.9, learning_rate=lr, batch=batch, seed=seed)
     if zero_w4:  # the untrained proposal is then exactly the power-proportional one (plus the mixture)
         params = ctx.proposal_params()
@@ -124,13 +126,13 @@ def run(width=1920, height=1080, frames=64, clusters=4096, n_tris=100_000, n_lig
         params[n123:n123 + 64 * clusters] = 0.0
         ctx.set_proposal_params(params)
     lrn_ms, lrn_rmse, loss = _arm(ctx, s, dg, res, image, crop, judge, frames, True, steps_per_frame,
-                                  learned_candidates, cam=cam)
+                                  learned_candidates, cam=cam, mask=mask)
     st = ctx.stats()
     ctx.close()
     target = plain_rmse[-1]
     hit = next((i for i, r in enumerate(lrn_rmse) if r <= target), None)
     frac = (lrn_ms[hit] / plain_ms[-1]) if hit is not None else None
-    judge_mean = float(judge.mean())
+    judge_mean = float(judge[mask].mean()) if mask is not None else float(judge.mean())
     every = max(1, frames // 16)
     return {
         "workload": f"{s.name} scene {width}x{height}, {len(s.triangles):,} triangles, {len(s.point_lights):,} point "

@@ -22,13 +22,14 @@ import bench
 
 pytestmark = pytest.mark.gpu
 
-# (relative RMSE, relative bias) of the last frame's crop, measured on a
-# GB300; the bit-exact passes make them reproducible to rounding of the
-# double-precision reductions.
+# (relative RMSE, log-luminance RMSE, median luminance ratio) of the last
+# frame's crop, measured on a GB300; the bit-exact passes make them
+# reproducible up to the rounding of the double-precision reductions.
 PINNED = {
     "config3": {"benched": None, "reference_default": None},
     "config2": {"benched": None, "reference_default": None},
 }
+KEYS = ("rel_rmse", "log_rmse", "median_ratio")
 
 
 def _render(ctx, name, cuda):
@@ -58,8 +59,8 @@ def test_crop_error_against_fp64_judge(ctx, cuda, name):
         assert np.isfinite(e["rel_rmse"]) and np.isfinite(e["rel_bias"])
         pin = PINNED[name][key]
         if pin is not None:
-            assert abs(e["rel_rmse"] - pin[0]) <= 1e-9 * max(1.0, abs(pin[0])), (key, e, pin)
-            assert abs(e["rel_bias"] - pin[1]) <= 1e-9, (key, e, pin)
+            for k, v in zip(KEYS, pin):
+                assert abs(e[k] - v) <= 1e-9 * max(1.0, abs(v)), (key, k, e, pin)
     # the measured property of the reference's method: chained passes darken
-    assert got["rel_bias"] < ref["rel_bias"]
-    assert got["rel_bias"] < -0.3
+    # the typical pixel more than its default single pass
+    assert got["median_ratio"] < ref["median_ratio"]
