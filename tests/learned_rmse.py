@@ -129,7 +129,10 @@ def run(width=1920, height=1080, frames=64, clusters=4096, n_tris=100_000, n_lig
                                   learned_candidates, cam=cam, mask=mask)
     st = ctx.stats()
     ctx.close()
-    target = plain_rmse[-1]
+    # the plain arm's final error, taken as its lowest over the last quarter of
+    # its frames, so that a late spike of its running mean (heavy-tailed
+    # estimates) does not make the target easier to reach
+    target = min(plain_rmse[-max(1, frames // 4):])
     hit = next((i for i, r in enumerate(lrn_rmse) if r <= target), None)
     frac = (lrn_ms[hit] / plain_ms[-1]) if hit is not None else None
     judge_mean = float(judge[mask].mean()) if mask is not None else float(judge.mean())
@@ -141,8 +144,8 @@ def run(width=1920, height=1080, frames=64, clusters=4096, n_tris=100_000, n_lig
                      "shaded; running mean of frames",
         "judge": f"FP64 brute force (every light, exact visibility) on a {crop_size}x{crop_size} crop at {crop[:2]}",
         "judge_mean_radiance": judge_mean,
-        "plain": {"ms_per_frame": plain_ms[-1] / frames, "final_rmse": target,
-                  "final_rel_rmse": target / judge_mean,
+        "plain": {"ms_per_frame": plain_ms[-1] / frames, "final_rmse": plain_rmse[-1], "target_rmse": target,
+                  "final_rel_rmse": plain_rmse[-1] / judge_mean, "target_rel_rmse": target / judge_mean,
                   "rmse_every": plain_rmse[::every], "cum_ms_every": plain_ms[::every]},
         "learned": {"ms_per_frame": lrn_ms[-1] / frames, "final_rmse": lrn_rmse[-1],
                     "final_rel_rmse": lrn_rmse[-1] / judge_mean,
@@ -152,7 +155,7 @@ def run(width=1920, height=1080, frames=64, clusters=4096, n_tris=100_000, n_lig
         "equal_rmse": {"learned_frame": None if hit is None else hit + 1,
                        "learned_ms": None if hit is None else lrn_ms[hit], "plain_ms": plain_ms[-1],
                        "time_fraction": frac},
-        "rmse_ratio_at_equal_frames": lrn_rmse[-1] / target,
+        "rmse_ratio_at_equal_frames": lrn_rmse[-1] / plain_rmse[-1],
         "kmeans_seconds_host": t_kmeans,
         "mma_timeouts": int(st.mma_timeouts),
     }
