@@ -740,7 +740,13 @@ def learned_section(dev: int, iters: int = 10, width: int = 1920, height: int = 
     equal = {}
     for key, name in (("config4", "config2"), ("config3_1M_lights", "config3")):
         try:
-            equal[key] = learned_equal_rmse(name)
+            e = learned_equal_rmse(name)
+            if e.get("learned_frame_reaching_plain_final_rmse"):
+                # the fraction if inference and training were free: the frames the
+                # learned arm needs, each at the learned RIS pass's cost
+                e["floor_without_inference_and_training"] = round(
+                    e["learned_frame_reaching_plain_final_rmse"] / e["frames"] * ris_l / ris_p, 4)
+            equal[key] = e
         except Exception as ex:  # reported, never hides the rest
             equal[key] = {"error": f"{type(ex).__name__}: {ex}"}
     return {"time_to_equal_rmse": equal,
