@@ -232,6 +232,7 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
     t_setup = time.perf_counter()
     s = make_scene(args.config, args.width, args.height, args.frames)
     ctx = Context(dev)
+    ctx.set_tree_layout(args.tree == "wide")
     ctx.upload_scene(s)
     n = s.width * s.height
     dgs = []
@@ -1028,6 +1029,8 @@ def main(argv=None):
     ap.add_argument("--height", type=int, default=None)
     ap.add_argument("--frames", type=int, default=None)
     ap.add_argument("--cpu-crop", type=int, default=0, help="0: the whole frame")
+    ap.add_argument("--tree", choices=["binary", "wide"], default="binary",
+                    help="device tree layout: the reference's binary tree or the opt-in 4-wide copy")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the learned-proposal and batched-view sections")
