@@ -376,7 +376,7 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
                       "triangle_tests_per_ray": round(st.triangle_tests / max(st.rays_traced, 1), 2),
                       "tree": ("4-wide copy of the reference's tree, %d nodes" % st.wide_nodes
                                if st.wide_nodes else "the reference's binary tree"),
-                      "note": "node visits of the frame's walks (fast-path rays on the 4-wide copy)"},
+                      "note": "node visits and triangle tests per segment over the timed frames' walks"},
         "passes_ms_mean": {k: round(sum(v) / len(v), 4) for k, v in per_kind.items()},
         "roofline": roofline,
         "gpu_launches": len(kinds) * args.steps,
