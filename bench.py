@@ -232,7 +232,7 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
     t_setup = time.perf_counter()
     s = make_scene(args.config, args.width, args.height, args.frames)
     ctx = Context(dev)
-    ctx.set_tree_layout(args.tree == "wide")
+    ctx.set_tree_layout(args.tree)
     ctx.upload_scene(s)
     n = s.width * s.height
     dgs = []
@@ -374,8 +374,7 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
         "rays_per_step": rays_total / args.steps / world,
         "traversal": {"node_visits_per_ray": round(st.node_visits / max(st.rays_traced, 1), 2),
                       "triangle_tests_per_ray": round(st.triangle_tests / max(st.rays_traced, 1), 2),
-                      "tree": ("4-wide copy of the reference's tree, %d nodes" % st.wide_nodes
-                               if st.wide_nodes else "the reference's binary tree"),
+                      "tree": tree_desc(st),
                       "note": "node visits and triangle tests per segment over the timed frames' walks"},
         "passes_ms_mean": {k: round(sum(v) / len(v), 4) for k, v in per_kind.items()},
         "roofline": roofline,
@@ -512,11 +511,23 @@ def launch_traversal(ctx, s, dgs, res, tmp, stream) -> dict:
     torch.cuda.synchronize()
     st = ctx.stats(reset=True)
     rays = max(int(st.rays_traced), 1)
-    per_visit = 112 if st.wide_nodes > 0 else 64
-    tree_bytes = per_visit * int(st.node_visits) + 48 * int(st.triangle_tests)
+    # bytes a node visit and a triangle test fetch: binary node 64 B and
+    # triangle 48 B; exact 4-wide node 64 B plus 48 B for its second pair
+    # (nearly always present); quantized node 64 B and leaf record 64 B
+    per_visit, per_tri = {0: (64, 48), 1: (112, 48), 2: (64, 64)}[int(st.tree_layout)]
+    tree_bytes = per_visit * int(st.node_visits) + per_tri * int(st.triangle_tests)
     return {"rays": rays, "visits_per_ray": round(st.node_visits / rays, 2),
             "tris_per_ray": round(st.triangle_tests / rays, 2), "tree_bytes": tree_bytes,
             "wide_nodes": int(st.wide_nodes)}
+
+
+def tree_desc(st) -> str:
+    layout = int(st.tree_layout)
+    if layout == 1:
+        return "4-wide copy of the reference's tree, %d nodes" % st.wide_nodes
+    if layout == 2:
+        return "quantized 4-wide copy of the reference's tree, %d nodes" % st.wide_nodes
+    return "the reference's binary tree"
 
 
 def measure_l2_gbs(mib: int = 32, iters: int = 200) -> float:
@@ -1029,8 +1040,8 @@ def main(argv=None):
     ap.add_argument("--height", type=int, default=None)
     ap.add_argument("--frames", type=int, default=None)
     ap.add_argument("--cpu-crop", type=int, default=0, help="0: the whole frame")
-    ap.add_argument("--tree", choices=["binary", "wide"], default="binary",
-                    help="device tree layout: the reference's binary tree or the opt-in 4-wide copy")
+    ap.add_argument("--tree", choices=["binary", "wide", "quant"], default="quant",
+                    help="device tree layout: the reference's binary tree, or its exact or quantized 4-wide copy")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the learned-proposal and batched-view sections")

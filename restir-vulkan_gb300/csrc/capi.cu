@@ -80,6 +80,8 @@ struct rg_context {
     bool has_scene = false;
     GNode *nodes = nullptr;
     WNode *wide = nullptr;
+    QNode *qnodes = nullptr;
+    QLeaf *qleaves = nullptr;
     GTri *tris = nullptr;
     AliasLight *alias = nullptr;
     float4 *pl_color = nullptr;
@@ -90,7 +92,7 @@ struct rg_context {
     int *mma_timeouts = nullptr;
     ProposalState *proposal = nullptr;  // learned proposal (proposal.cu), tied to the uploaded lights
     int res_samples = 1, res_mis = 0;   // reservoir format (rg_set_reservoir_format)
-    int tree_layout = RG_TREE_BINARY;   // rg_set_tree_layout, applied at the next upload
+    int tree_layout = RG_TREE_QUANT4;   // rg_set_tree_layout, applied at the next upload
     size_t frame_bytes = 0;             // bytes per pixel of the frame driver's reservoir buffers
     // frame driver
     int fw = 0, fh = 0;
@@ -103,7 +105,7 @@ struct rg_context {
     void release_scene() {
         proposal_release(proposal);
         proposal = nullptr;
-        dev_free(nodes); dev_free(wide); dev_free(tris); dev_free(alias); dev_free(pl_color); dev_free(tri_lights);
+        dev_free(nodes); dev_free(wide); dev_free(qnodes); dev_free(qleaves); dev_free(tris); dev_free(alias); dev_free(pl_color); dev_free(tri_lights);
         dev_free(tri_alias); dev_free(materials);
         has_scene = false;
     }
@@ -225,7 +227,10 @@ int rg_get_stats(rg_context *ctx, rg_stats *out, int32_t reset) {
     int to = 0;
     RG_CUDA(cudaMemcpy(&to, ctx->mma_timeouts, sizeof(int), cudaMemcpyDeviceToHost), "rg_get_stats");
     out->mma_timeouts = (uint64_t)to;
-    out->wide_nodes = ctx->has_scene ? (uint64_t)ctx->scene.n_wide : 0u;
+    out->wide_nodes = !ctx->has_scene ? 0u : ctx->scene.qnodes ? (uint64_t)ctx->scene.n_qnodes
+                                                                : (uint64_t)ctx->scene.n_wide;
+    out->tree_layout = !ctx->has_scene ? RG_TREE_BINARY : ctx->scene.qnodes ? RG_TREE_QUANT4
+                                                        : ctx->scene.wide ? RG_TREE_WIDE4 : RG_TREE_BINARY;
     if (reset) RG_CUDA(cudaMemset(ctx->mma_timeouts, 0, sizeof(int)), "rg_get_stats");
     if (reset) RG_CUDA(cudaMemset(ctx->counters, 0, sizeof(c)), "rg_get_stats");
     return RG_OK;
@@ -334,11 +339,24 @@ int rg_upload_scene(rg_context *ctx, const rg_scene_desc *sc) {
         n_wide = host_pack_wide(sc->nodes, sc->n_nodes, w32, &wide_depth);
     const int wide_stack = 3 * wide_depth + 1;
     if (n_wide > 0 && wide_stack > RG_MAX_TREE_DEPTH + 1) n_wide = -1;
+    std::vector<uint32_t> q16;
+    std::vector<float> ql16;
+    int q_depth = 0;
+    int32_t n_q = -1;
+    if (ctx->tree_layout == RG_TREE_QUANT4 && sc->n_nodes > 0 && !box_nan)
+        n_q = host_pack_quant(sc->nodes, sc->n_nodes, t12.data(), q16, ql16, &q_depth);
+    if (n_q > 0 && 3 * q_depth + 1 > RG_MAX_TREE_DEPTH + 1) n_q = -1;
     e = dev_alloc(&ctx->nodes, (size_t)sc->n_nodes);
     if (e == cudaSuccess && sc->n_nodes) e = cudaMemcpy(ctx->nodes, n16.data(), n16.size() * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && n_wide > 0) {
         e = dev_alloc(&ctx->wide, (size_t)n_wide);
         if (e == cudaSuccess) e = cudaMemcpy(ctx->wide, w32.data(), w32.size() * 4, cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess && n_q > 0) {
+        e = dev_alloc(&ctx->qnodes, (size_t)n_q);
+        if (e == cudaSuccess) e = cudaMemcpy(ctx->qnodes, q16.data(), q16.size() * 4, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = dev_alloc(&ctx->qleaves, ql16.size() / 16);
+        if (e == cudaSuccess) e = cudaMemcpy(ctx->qleaves, ql16.data(), ql16.size() * 4, cudaMemcpyHostToDevice);
     }
     if (e == cudaSuccess) e = dev_alloc(&ctx->tris, (size_t)sc->n_triangles);
     if (e == cudaSuccess && sc->n_triangles) e = cudaMemcpy(ctx->tris, t12.data(), t12.size() * 4, cudaMemcpyHostToDevice);
@@ -387,6 +405,10 @@ int rg_upload_scene(rg_context *ctx, const rg_scene_desc *sc) {
     s.wide = n_wide > 0 ? ctx->wide : nullptr;
     s.n_wide = n_wide > 0 ? n_wide : 0;
     s.wide_stack = n_wide > 0 ? wide_stack : 0;
+    s.qnodes = n_q > 0 ? ctx->qnodes : nullptr;
+    s.qleaves = n_q > 0 ? ctx->qleaves : nullptr;
+    s.n_qnodes = n_q > 0 ? n_q : 0;
+    if (n_q > 0) s.wide_stack = 3 * q_depth + 1;
     s.tris = ctx->tris;
     s.n_tris = sc->n_triangles;
     s.alias = ctx->alias;
@@ -545,8 +567,8 @@ int rg_set_reservoir_format(rg_context *ctx, int32_t samples, int32_t unbiased_m
 int rg_set_tree_layout(rg_context *ctx, int32_t layout) {
     int rc = check_ctx(ctx, false);
     if (rc) return rc;
-    if (layout != RG_TREE_BINARY && layout != RG_TREE_WIDE4)
-        return fail(RG_ERR_INVALID_ARGUMENT, "tree layout must be RG_TREE_BINARY or RG_TREE_WIDE4");
+    if (layout != RG_TREE_BINARY && layout != RG_TREE_WIDE4 && layout != RG_TREE_QUANT4)
+        return fail(RG_ERR_INVALID_ARGUMENT, "tree layout must be RG_TREE_BINARY, RG_TREE_WIDE4 or RG_TREE_QUANT4");
     ctx->tree_layout = layout;
     return RG_OK;
 }

@@ -378,6 +378,31 @@ float surface(const WEntry &e) {
     return x * y + x * z + y * z;
 }
 
+// The up to four descendants of binary node x that one node of a 4-wide copy
+// holds (expansion by largest surface, left-to-right order); clears ok when an
+// expanded box does not contain its children's.  Returns their count.
+int expand4(const rg_aabb_tree_node *src, int32_t x, WEntry e[4], bool &ok) {
+    int n = 2;
+    e[0] = child_entry(src[x], 0);
+    e[1] = child_entry(src[x], 1);
+    while (n < 4) {
+        int pick = -1;
+        float best = -1.0f;
+        for (int k = 0; k < n; ++k)
+            if (e[k].ref >= 0 && surface(e[k]) > best) { best = surface(e[k]); pick = k; }
+        if (pick < 0) break;
+        const rg_aabb_tree_node &y = src[e[pick].ref];
+        const WEntry l = child_entry(y, 0), r = child_entry(y, 1);
+        if (!box_inside(l.lo, l.hi, e[pick].lo, e[pick].hi) || !box_inside(r.lo, r.hi, e[pick].lo, e[pick].hi))
+            ok = false;
+        for (int k = n; k > pick + 1; --k) e[k] = e[k - 1];
+        e[pick] = l;
+        e[pick + 1] = r;
+        ++n;
+    }
+    return n;
+}
+
 struct WideBuilder {
     const rg_aabb_tree_node *src;
     std::vector<float> *out;
@@ -387,24 +412,7 @@ struct WideBuilder {
     int32_t build(int32_t x, int depth) {
         max_depth = std::max(max_depth, depth);
         WEntry e[4];
-        int n = 2;
-        e[0] = child_entry(src[x], 0);
-        e[1] = child_entry(src[x], 1);
-        while (n < 4) {
-            int pick = -1;
-            float best = -1.0f;
-            for (int k = 0; k < n; ++k)
-                if (e[k].ref >= 0 && surface(e[k]) > best) { best = surface(e[k]); pick = k; }
-            if (pick < 0) break;
-            const rg_aabb_tree_node &y = src[e[pick].ref];
-            const WEntry l = child_entry(y, 0), r = child_entry(y, 1);
-            if (!box_inside(l.lo, l.hi, e[pick].lo, e[pick].hi) || !box_inside(r.lo, r.hi, e[pick].lo, e[pick].hi))
-                ok = false;
-            for (int k = n; k > pick + 1; --k) e[k] = e[k - 1];
-            e[pick] = l;
-            e[pick + 1] = r;
-            ++n;
-        }
+        const int n = expand4(src, x, e, ok);
         const int32_t me = (int32_t)(out->size() / 32);
         out->resize(out->size() + 32, 0.0f);
         int32_t links[4] = {kNoChild, kNoChild, kNoChild, kNoChild};
@@ -440,6 +448,144 @@ int32_t host_pack_wide(const rg_aabb_tree_node *src, int32_t n, std::vector<floa
     if (wide_depth) *wide_depth = b.max_depth;
     if (!b.ok) return -1;
     return (int32_t)(out.size() / 32);
+}
+
+// ---------------------------------------------------------------- quantized 4-wide copy
+// The same collapse with each node's child boxes stored as 8-bit offsets
+// from the node's box (64-byte nodes: a third of the binary tree's bytes).
+// Per axis a node stores an origin o (its box's lower bound) and a power of
+// two s = 2^e; a child bound q decodes to RN(o + q*s) (q*s is exact, so an
+// FMA and an add of the product give the same float), and q is chosen so that
+// the decoded box contains the child's box: the largest q whose decoded value
+// is <= the lower bound, the smallest whose decoded value is >= the upper
+// bound.  e is the smallest exponent for which q = 255 decodes to at least
+// the node's upper bound.  Leaf slots link (as ~index) to leaf records that
+// hold the triangle's exact box from the reference's tree and the triangle
+// itself (host_pack_tris form).
+//
+// The walk tests the decoded boxes only for a sure miss (a decoded box
+// contains the exact one, and the slab test is monotone under containment),
+// and gates each reached triangle with its exact box.  That answer equals the
+// reference's when every child box of the reference's tree lies inside the
+// box its parent stores for it (then a triangle's exact box passing implies
+// its whole box path passes); host_tree_nested checks that.
+//
+// Node (16 words): origin xyz (float) and biased exponents (bytes 0-2 of word
+// 3), then per axis a word of lower bounds and a word of upper bounds (byte k
+// = child k; x, y in words 4-7, z in words 8-9; 10-11 unused), then 4 links
+// (node index, ~leaf record index, or kNoChild).  Leaf record (16 floats):
+// lo.xyz hi.xyz, p1.xyz e1.xyz e2.xyz, 0.
+namespace {
+// RN(o + q * 2^(eb - 127)), the decode the device computes
+inline float qdecode(float o, int q, int eb) {
+    float s;
+    const uint32_t bits = (uint32_t)eb << 23;
+    memcpy(&s, &bits, 4);
+    const float qs = (float)q * s;  // exact: q < 256 and s a normal power of two
+    return o + qs;
+}
+
+struct QuantBuilder {
+    const rg_aabb_tree_node *src;
+    const float *tris12;
+    std::vector<uint32_t> *nodes;
+    std::vector<float> *leaves;
+    int max_depth = 0;
+    bool ok = true;
+
+    int32_t build(int32_t x, int depth) {
+        max_depth = std::max(max_depth, depth);
+        WEntry e[4];
+        const int n = expand4(src, x, e, ok);
+        const int32_t me = (int32_t)(nodes->size() / 16);
+        nodes->resize(nodes->size() + 16, 0u);
+        uint32_t w[16] = {0};
+        float org[3];
+        int eb[3];
+        for (int a = 0; a < 3; ++a) {
+            float lo = e[0].lo[a], hi = e[0].hi[a];
+            for (int k = 1; k < n; ++k) { lo = std::min(lo, e[k].lo[a]); hi = std::max(hi, e[k].hi[a]); }
+            if (!std::isfinite(lo) || !std::isfinite(hi)) { ok = false; lo = hi = 0.0f; }
+            org[a] = lo;
+            // smallest biased exponent in [1, 246] (255 * s stays finite) that reaches hi
+            int b = 1;
+            const double ext = (double)hi - (double)lo;
+            if (ext > 0.0) b = std::max(1, std::min(246, (int)std::ceil(std::log2(ext / 255.0)) + 127));
+            while (b > 1 && qdecode(lo, 255, b - 1) >= hi) --b;
+            while (b < 246 && !(qdecode(lo, 255, b) >= hi)) ++b;
+            if (!(qdecode(lo, 255, b) >= hi) || !std::isfinite(qdecode(lo, 255, b))) ok = false;
+            eb[a] = b;
+            memcpy(&w[a], &org[a], 4);
+        }
+        w[3] = (uint32_t)eb[0] | ((uint32_t)eb[1] << 8) | ((uint32_t)eb[2] << 16);
+        for (int k = 0; k < 4; ++k) {
+            const WEntry &c = e[k < n ? k : n - 1];  // an empty slot repeats the last child (ignored)
+            for (int a = 0; a < 3; ++a) {
+                const double sa = std::ldexp(1.0, eb[a] - 127);
+                int ql = (int)std::floor(((double)c.lo[a] - (double)org[a]) / sa);
+                ql = std::max(0, std::min(255, ql));
+                while (ql > 0 && qdecode(org[a], ql, eb[a]) > c.lo[a]) --ql;
+                while (ql < 255 && qdecode(org[a], ql + 1, eb[a]) <= c.lo[a]) ++ql;
+                int qh = (int)std::ceil(((double)c.hi[a] - (double)org[a]) / sa);
+                qh = std::max(0, std::min(255, qh));
+                while (qh < 255 && qdecode(org[a], qh, eb[a]) < c.hi[a]) ++qh;
+                while (qh > 0 && qdecode(org[a], qh - 1, eb[a]) >= c.hi[a]) --qh;
+                if (!(qdecode(org[a], ql, eb[a]) <= c.lo[a]) || !(qdecode(org[a], qh, eb[a]) >= c.hi[a])) ok = false;
+                w[4 + 2 * a] |= (uint32_t)ql << (8 * k);
+                w[5 + 2 * a] |= (uint32_t)qh << (8 * k);
+            }
+        }
+        int32_t links[4] = {kNoChild, kNoChild, kNoChild, kNoChild};
+        for (int k = 0; k < n; ++k) {
+            if (e[k].ref < 0) {
+                const int32_t rec = (int32_t)(leaves->size() / 16);
+                const float *t = tris12 + 12 * (size_t)(~e[k].ref);
+                const float r[16] = {e[k].lo[0], e[k].lo[1], e[k].lo[2], e[k].hi[0], e[k].hi[1], e[k].hi[2],
+                                     t[0], t[1], t[2], t[3], t[4], t[5], t[6], t[7], t[8], 0.0f};
+                leaves->insert(leaves->end(), r, r + 16);
+                links[k] = ~rec;
+            }
+        }
+        for (int k = 0; k < n; ++k)
+            if (e[k].ref >= 0) links[k] = build(e[k].ref, depth + 1);
+        memcpy(&w[12], links, sizeof(links));
+        memcpy(nodes->data() + 16 * (size_t)me, w, sizeof(w));
+        return me;
+    }
+};
+}  // namespace
+
+// True when every child box of every inner node lies inside the box that the
+// node's parent stores for it (the root's children have no enclosing box).
+bool host_tree_nested(const rg_aabb_tree_node *src, int32_t n) {
+    for (int32_t i = 0; i < n; ++i) {
+        for (int side = 0; side < 2; ++side) {
+            const WEntry c = child_entry(src[i], side);
+            if (c.ref < 0) continue;
+            const WEntry l = child_entry(src[c.ref], 0), r = child_entry(src[c.ref], 1);
+            if (!box_inside(l.lo, l.hi, c.lo, c.hi) || !box_inside(r.lo, r.hi, c.lo, c.hi)) return false;
+        }
+    }
+    return true;
+}
+
+int32_t host_pack_quant(const rg_aabb_tree_node *src, int32_t n, const float *tris12, std::vector<uint32_t> &nodes,
+                        std::vector<float> &leaves, int *wide_depth) {
+    nodes.clear();
+    leaves.clear();
+    if (n <= 0) return 0;
+    if (!host_tree_nested(src, n)) return -1;
+    QuantBuilder b;
+    b.src = src;
+    b.tris12 = tris12;
+    b.nodes = &nodes;
+    b.leaves = &leaves;
+    nodes.reserve((size_t)16 * (size_t)(n / 3 + 1));
+    leaves.reserve((size_t)16 * (size_t)(n + 1));
+    b.build(0, 1);
+    if (wide_depth) *wide_depth = b.max_depth;
+    if (!b.ok) return -1;
+    return (int32_t)(nodes.size() / 16);
 }
 
 // True when a child box coordinate of some node is NaN (e.g. a tree built

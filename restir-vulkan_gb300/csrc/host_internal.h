@@ -19,6 +19,12 @@ void host_pack_tris(const rg_triangle *src, int32_t n, float *dst12);
 // The 4-wide copy of a valid tree (32 floats per node; see host.cpp): node
 // count, or -1 when some child box lies outside its parent's box.
 int32_t host_pack_wide(const rg_aabb_tree_node *src, int32_t n, std::vector<float> &out, int *wide_depth);
+// The quantized 4-wide copy (16 words per node, 16 floats per leaf record;
+// see host.cpp) over packed triangles: node count, or -1 when the tree is not
+// nested (host_tree_nested) or a box cannot be quantized (non-finite bounds).
+bool host_tree_nested(const rg_aabb_tree_node *src, int32_t n);
+int32_t host_pack_quant(const rg_aabb_tree_node *src, int32_t n, const float *tris12, std::vector<uint32_t> &nodes,
+                        std::vector<float> &leaves, int *wide_depth);
 void srgb_lut_host(float *out256);
 int host_trace_gbuffer(const float *nodes16, int32_t n_nodes, const float *tris12, int32_t n_tris,
                        const rg_material *mats, int32_t n_mats, const rg_camera &cam, int32_t w, int32_t h,

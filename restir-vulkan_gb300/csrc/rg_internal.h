@@ -45,6 +45,26 @@ struct WNode {
 };
 constexpr int32_t kWideNoChild = INT32_MIN;
 
+// QNode 64 B: the quantized 4-wide copy (host_pack_quant).  Per axis an
+// origin and a power of two s (biased exponent bytes in org.w); child k's
+// bounds are byte k of the axis' lower and upper words, decoding to
+// RN(origin + q * s), a box containing the child's exact box.  Links: >= 0
+// node, < 0 leaf record ~r, kWideNoChild = empty.
+struct QNode {
+    float4 org;  // origin.xyz, exponent bytes (x, y, z)
+    uint4 qxy;   // lo x, hi x, lo y, hi y (byte k: child k)
+    uint4 qz;    // lo z, hi z, 0, 0
+    int4 d;      // links of children 0..3
+};
+// QLeaf 64 B: a leaf of the quantized copy, the triangle's exact box from
+// the reference's tree and the triangle in GTri form.
+struct QLeaf {
+    float4 a;  // lo.xyz hi.x
+    float4 b;  // hi.y hi.z p1.x p1.y
+    float4 c;  // p1.z e1.xyz
+    float4 d;  // e2.xyz 0
+};
+
 struct DevScene {
     const GNode *nodes;
     int32_t n_nodes;
@@ -53,6 +73,9 @@ struct DevScene {
     const WNode *wide;            // 4-wide copy, or null (containment failed, NaN boxes, too deep)
     int32_t n_wide;
     int32_t wide_stack;           // stack entries the 4-wide walk may need (3 per level)
+    const QNode *qnodes;          // quantized 4-wide copy, or null (not nested, NaN or huge boxes, too deep)
+    const QLeaf *qleaves;
+    int32_t n_qnodes;
     const GTri *tris;
     int32_t n_tris;
     const AliasLight *alias;      // point-light scenes

@@ -522,12 +522,191 @@ __device__ void trace_wide_loop(const DevScene &s, Fetch fetch, int n, int *next
     }
 }
 
-// The block's walk: over the 4-wide copy when the upload built one, else
-// over the reference's tree.
+// Bytes sel0, sel1 of a word of 8-bit bounds decoded to RN(origin + q * sc)
+// as a packed pair: 2^23 + q is built from the byte's bits, 2^23 taken off
+// (exact), then one FMA (q * sc is exact, so the FMA rounds once, like the
+// host's add of the product).
+__device__ __forceinline__ float2 qdecode2(unsigned w, unsigned sel0, unsigned sel1, float2 sc, float2 org) {
+    const float2 f = make_float2(__uint_as_float(__byte_perm(w, 0x4B000000u, sel0)),
+                                 __uint_as_float(__byte_perm(w, 0x4B000000u, sel1)));
+    return __ffma2_rn(__fadd2_rn(f, make_float2(-8388608.0f, -8388608.0f)), sc, org);
+}
+
+// Children 2p, 2p+1 of a quantized node: the filtered test's sure-miss
+// decision on their decoded boxes (bit 0 / bit 1 set when not surely missed).
+__device__ __forceinline__ unsigned qpair_live(f3 o, f3 inv, const float4 &org, const uint4 &qa, const uint4 &qb,
+                                               float2 sx, float2 sy, float2 sz, int p) {
+    const unsigned s0 = 0x7440u + 2u * (unsigned)p, s1 = s0 + 1u;
+    const float2 ox = make_float2(org.x, org.x), oy = make_float2(org.y, org.y), oz = make_float2(org.z, org.z);
+    const float2 nox = make_float2(-o.x, -o.x), noy = make_float2(-o.y, -o.y), noz = make_float2(-o.z, -o.z);
+    const float2 ix = make_float2(inv.x, inv.x), iy = make_float2(inv.y, inv.y), iz = make_float2(inv.z, inv.z);
+    const float2 t0x = __fmul2_rn(__fadd2_rn(qdecode2(qa.x, s0, s1, sx, ox), nox), ix);
+    const float2 t1x = __fmul2_rn(__fadd2_rn(qdecode2(qa.y, s0, s1, sx, ox), nox), ix);
+    const float2 t0y = __fmul2_rn(__fadd2_rn(qdecode2(qa.z, s0, s1, sy, oy), noy), iy);
+    const float2 t1y = __fmul2_rn(__fadd2_rn(qdecode2(qa.w, s0, s1, sy, oy), noy), iy);
+    const float2 t0z = __fmul2_rn(__fadd2_rn(qdecode2(qb.x, s0, s1, sz, oz), noz), iz);
+    const float2 t1z = __fmul2_rn(__fadd2_rn(qdecode2(qb.y, s0, s1, sz, oz), noz), iz);
+    const float rminl = max3f(fminf(t0x.x, t1x.x), fminf(t0y.x, t1y.x), fminf(t0z.x, t1z.x));
+    const float rmaxl = min3f(fmaxf(t0x.x, t1x.x), fmaxf(t0y.x, t1y.x), fmaxf(t0z.x, t1z.x));
+    const float rminr = max3f(fminf(t0x.y, t1x.y), fminf(t0y.y, t1y.y), fminf(t0z.y, t1z.y));
+    const float rmaxr = min3f(fmaxf(t0x.y, t1x.y), fmaxf(t0y.y, t1y.y), fmaxf(t0z.y, t1z.y));
+    bool hl, ml, hr, mr;
+    filtered_decision(rminl, rmaxl, hl, ml);
+    filtered_decision(rminr, rmaxr, hr, mr);
+    return (ml ? 0u : 1u) | (mr ? 0u : 2u);
+}
+
+// The exact slab test of a leaf record's box (undecided filtered tests only).
+__device__ __noinline__ bool leaf_box_exact(f3 o, f3 d, float4 a, float4 b) {
+    return box_hit(o, d, mk(a.x, a.y, a.z), mk(a.w, b.x, b.y));
+}
+
+// A leaf of the quantized copy: the reference's slab test of the triangle's
+// exact box (filtered, exact where undecided), then its triangle test.
+__device__ __forceinline__ bool qleaf_hit(const QLeaf *lp, f3 o, f3 d, f3 inv) {
+    const float4 a = __ldg(&lp->a), b = __ldg(&lp->b), c = __ldg(&lp->c), e = __ldg(&lp->d);
+    const float2 tx = __fmul2_rn(__fadd2_rn(make_float2(a.x, a.w), make_float2(-o.x, -o.x)), make_float2(inv.x, inv.x));
+    const float2 ty = __fmul2_rn(__fadd2_rn(make_float2(a.y, b.x), make_float2(-o.y, -o.y)), make_float2(inv.y, inv.y));
+    const float2 tz = __fmul2_rn(__fadd2_rn(make_float2(a.z, b.y), make_float2(-o.z, -o.z)), make_float2(inv.z, inv.z));
+    const float rmin = max3f(fminf(tx.x, tx.y), fminf(ty.x, ty.y), fminf(tz.x, tz.y));
+    const float rmax = min3f(fmaxf(tx.x, tx.y), fmaxf(ty.x, ty.y), fmaxf(tz.x, tz.y));
+    bool hit, miss;
+    filtered_decision(rmin, rmax, hit, miss);
+    if (!hit && !miss) hit = leaf_box_exact(o, d, a, b);
+    return hit && rgm::ray_tri(mk(b.z, b.w, c.x), mk(c.y, c.z, c.w), mk(e.x, e.y, e.z), o, d);
+}
+
+// The loop over the quantized 4-wide copy (DevScene::qnodes): a node visit
+// decodes its four child boxes and drops those the filtered test surely
+// misses (a decoded box contains the exact one, so the reference's test
+// misses the exact box too); the rest are walked (inner) or parked (leaves).
+// A parked leaf is tested with its exact box, then its triangle, so a
+// triangle is tested exactly when the reference's test passes its box,
+// which on a nested tree implies its whole box path passes, as in the
+// reference's walk.  Stack and order as in trace_wide_loop.
+template <typename Fetch, typename Endpoint, typename Emit>
+__device__ void trace_quant_loop(const DevScene &s, Fetch fetch, int n, int *next, TraceStats &ts, Endpoint endpoint,
+                                 Emit emit) {
+    constexpr unsigned kFull = 0xffffffffu;
+    int my_stack[RG_MAX_TREE_DEPTH + 1];
+    int cur = -1;          // pool index of this lane's segment, -1: none
+    bool retired = false;  // the pool has no segment left for this lane
+    int owner = 0, node = 0, sp = 0, visits = 0;
+    unsigned leafmask = 0; // parked leaves: links of leaf_node
+    int leaf_node = 0;
+    bool walked = false;   // tree walk finished, only parked leaves remain
+    f3 o = mk(0.f, 0.f, 0.f), d = o, inv = o;
+    while (true) {
+        // 1. refill idle lanes, several at a time
+        const bool idle = !retired && cur < 0;
+        const unsigned m_idle = __ballot_sync(kFull, idle);
+        const unsigned m_busy = __ballot_sync(kFull, cur >= 0);
+        if (m_idle != 0u && (__popc(m_idle) >= RG_FETCH_MIN || m_busy == 0u)) {
+            if (idle) {
+                const int k = atomicAdd(next, 1);
+                if (k >= n) {
+                    retired = true;
+                } else {
+                    f3 p1;
+                    owner = fetch(k, p1);
+                    rgm::shadow_segment(p1, endpoint(owner), o, d);
+                    if (ray_inverse(d, inv)) {
+                        cur = k;
+                        node = 0;
+                        sp = 0;
+                        visits = 0;
+                        leafmask = 0u;
+                        walked = false;
+                    } else {
+                        emit(owner, trace_exact_binary(s, o, d, ts));
+                    }
+                }
+            }
+        }
+        if (__all_sync(kFull, retired)) break;
+        // 2. parked leaves
+        const bool has_leaf = cur >= 0 && leafmask != 0u;
+        const unsigned m_leaf = __ballot_sync(kFull, has_leaf);
+        const unsigned m_walk = __ballot_sync(kFull, cur >= 0 && leafmask == 0u && !walked);
+        if (m_leaf != 0u && (__popc(m_leaf) >= RG_LEAF_MIN || m_walk == 0u)) {
+            if (has_leaf) {
+                const int4 ch = __ldg(&s.qnodes[leaf_node].d);
+                bool hit = false;
+                for (unsigned m = leafmask; m != 0u && !hit; m &= m - 1u) {
+                    const int k = __ffs(m) - 1;
+                    const int link = k == 0 ? ch.x : k == 1 ? ch.y : k == 2 ? ch.z : ch.w;
+                    hit = qleaf_hit(s.qleaves + ~link, o, d, inv);
+                    ++ts.tri_tests;
+                }
+                leafmask = 0u;
+                if (hit || walked) {
+                    emit(owner, hit);
+                    cur = -1;
+                }
+            }
+            continue;
+        }
+        // 3. up to RG_WALK_STEPS nodes per walking lane
+#pragma unroll 1
+        for (int step = 0; step < RG_WALK_STEPS && cur >= 0 && leafmask == 0u && !walked; ++step) {
+            ++ts.visits;
+            if (++visits > s.n_qnodes) {
+                ts.err = true;
+                emit(owner, false);
+                cur = -1;
+                continue;
+            }
+            const QNode *np = s.qnodes + node;
+            const float4 org = __ldg(&np->org);
+            const uint4 qa = __ldg(&np->qxy), qb = __ldg(&np->qz);
+            const int4 ch = __ldg(&np->d);
+            const unsigned eb = __float_as_uint(org.w);
+            const float ex = __uint_as_float((eb & 0xffu) << 23), ey = __uint_as_float(((eb >> 8) & 0xffu) << 23),
+                        ez = __uint_as_float(((eb >> 16) & 0xffu) << 23);
+            const float2 sx = make_float2(ex, ex), sy = make_float2(ey, ey), sz = make_float2(ez, ez);
+            const unsigned live = qpair_live(o, inv, org, qa, qb, sx, sy, sz, 0) |
+                                  (qpair_live(o, inv, org, qa, qb, sx, sy, sz, 1) << 2);
+            const bool h0 = (live & 1u) != 0u, h1 = (live & 2u) != 0u;
+            const bool h2 = (live & 4u) != 0u && ch.z != kWideNoChild, h3 = (live & 8u) != 0u && ch.w != kWideNoChild;
+            leafmask = (h0 && ch.x < 0 ? 1u : 0u) | (h1 && ch.y < 0 ? 2u : 0u) | (h2 && ch.z < 0 ? 4u : 0u) |
+                       (h3 && ch.w < 0 ? 8u : 0u);
+            if (leafmask) leaf_node = node;
+            int nxt = -1;
+            if (h3 && ch.w >= 0) nxt = ch.w;
+            if (h2 && ch.z >= 0) {
+                if (nxt >= 0) my_stack[sp++] = nxt;
+                nxt = ch.z;
+            }
+            if (h1 && ch.y >= 0) {
+                if (nxt >= 0) my_stack[sp++] = nxt;
+                nxt = ch.y;
+            }
+            if (h0 && ch.x >= 0) {
+                if (nxt >= 0) my_stack[sp++] = nxt;
+                nxt = ch.x;
+            }
+            if (nxt >= 0) {
+                node = nxt;
+            } else if (sp > 0) {
+                node = my_stack[--sp];
+            } else {
+                walked = true;
+                if (leafmask == 0u) {
+                    emit(owner, false);
+                    cur = -1;
+                }
+            }
+        }
+    }
+}
+
+// The block's walk: over the quantized or the exact 4-wide copy when the
+// upload built one, else over the reference's tree.
 template <typename Fetch, typename Endpoint, typename Emit>
 __device__ __forceinline__ void trace_pool_f(const DevScene &s, Fetch fetch, int n, int *next, int *stack, int depth,
                                              TraceStats &ts, Endpoint endpoint, Emit emit) {
-    if (s.wide != nullptr) trace_wide_loop(s, fetch, n, next, ts, endpoint, emit);
+    if (s.qnodes != nullptr) trace_quant_loop(s, fetch, n, next, ts, endpoint, emit);
+    else if (s.wide != nullptr) trace_wide_loop(s, fetch, n, next, ts, endpoint, emit);
     else trace_binary_loop(s, fetch, n, next, stack, depth, ts, endpoint, emit);
 }
 

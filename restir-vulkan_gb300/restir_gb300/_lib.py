@@ -99,7 +99,8 @@ class FrameParams(C.Structure):
 
 class Stats(C.Structure):
     _fields_ = [("rays_traced", C.c_uint64), ("traversal_errors", C.c_uint64), ("node_visits", C.c_uint64),
-                ("triangle_tests", C.c_uint64), ("mma_timeouts", C.c_uint64), ("wide_nodes", C.c_uint64)]
+                ("triangle_tests", C.c_uint64), ("mma_timeouts", C.c_uint64), ("wide_nodes", C.c_uint64),
+                ("tree_layout", C.c_uint64)]
 
 
 class View(C.Structure):

@@ -188,9 +188,15 @@ class Context:
     def set_reservoir_format(self, samples: int, unbiased_mis: int):
         check(lib().rg_set_reservoir_format(self._h, samples, unbiased_mis))
 
-    def set_tree_layout(self, wide: bool):
-        """RG_TREE_WIDE4 (True) or RG_TREE_BINARY (False), from the next upload."""
-        check(lib().rg_set_tree_layout(self._h, 1 if wide else 0))
+    TREE_LAYOUTS = {"binary": 0, "wide": 1, "quant": 2}
+
+    def set_tree_layout(self, layout):
+        """The shadow-ray tree from the next upload: "binary" (RG_TREE_BINARY),
+        "wide" (RG_TREE_WIDE4) or "quant" (RG_TREE_QUANT4); True / False mean
+        "wide" / "binary"."""
+        if isinstance(layout, bool):
+            layout = "wide" if layout else "binary"
+        check(lib().rg_set_tree_layout(self._h, self.TREE_LAYOUTS[layout]))
 
     def reservoir_bytes(self) -> int:
         return check(lib().rg_reservoir_bytes(self._h))

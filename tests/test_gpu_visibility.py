@@ -110,9 +110,15 @@ def _gpu_vs_oracle(ctx, cuda, s, p1, p2):
     return got, exp
 
 
-def test_grazing_segments_bit_exact(ctx, cuda, cfg1_scene):
+@pytest.mark.parametrize("layout", ["binary", "quant"])
+def test_grazing_segments_bit_exact(ctx, cuda, cfg1_scene, layout):
     p1, p2 = _segments(cfg1_scene)
-    got, exp = _gpu_vs_oracle(ctx, cuda, cfg1_scene, p1, p2)
+    ctx.set_tree_layout(layout)
+    try:
+        got, exp = _gpu_vs_oracle(ctx, cuda, cfg1_scene, p1, p2)
+        assert (ctx.stats().tree_layout == 2) == (layout == "quant")
+    finally:
+        ctx.set_tree_layout("quant")
     bad = np.nonzero(got != exp)[0]
     assert len(bad) == 0, f"{len(bad)} of {len(got)} visibility bits differ, first at {bad[:8]}"
     assert 0.02 < exp.mean() < 0.98
@@ -132,12 +138,14 @@ def test_nan_box_bit_exact(ctx, cuda, cfg1_scene):
     assert np.count_nonzero(exp != exp_clean) > 0  # the NaN changed the answers
 
 
-def test_wide_copy_on_config3_bit_exact(ctx, cuda):
-    """1,048,588 triangles with RG_TREE_WIDE4: the upload builds the 4-wide
-    copy (every expanded box's children nested in it), and fast-path rays
-    walk it; segments aimed at the
-    boxes of the reference's tree (among them the boxes the collapse skips)
-    and pixel-to-light style segments equal the oracle's bits."""
+@pytest.mark.parametrize("layout", ["wide", "quant"])
+def test_wide_copy_on_config3_bit_exact(ctx, cuda, layout):
+    """1,048,588 triangles with RG_TREE_WIDE4 or RG_TREE_QUANT4: the upload
+    builds the 4-wide copy (exact boxes, every expanded box's children nested
+    in it; or 8-bit boxes containing the exact ones over a tree nested
+    throughout), and fast-path rays walk it; segments aimed at the boxes of
+    the reference's tree (among them the boxes the collapse skips) and
+    pixel-to-light style segments equal the oracle's bits."""
     from restir_gb300 import scenes
     s = scenes.config3(width=64, height=64, frames=1)
     p1, p2 = _segments(s, seed=21, n=60_000)
@@ -148,18 +156,45 @@ def test_wide_copy_on_config3_bit_exact(ctx, cuda):
     q1[:, :3] = rng.uniform(0.0, 1.0, (m, 3))
     q2[:, :3] = s.point_lights["pos"][rng.integers(0, len(s.point_lights), m), :3]
     p1, p2 = np.concatenate([p1, q1]), np.concatenate([p2, q2])
-    ctx.set_tree_layout(True)
+    ctx.set_tree_layout(layout)
     try:
         got, exp = _gpu_vs_oracle(ctx, cuda, s, p1, p2)
-        assert ctx.stats().wide_nodes > 0
+        st = ctx.stats()
+        assert st.wide_nodes > 0 and st.tree_layout == ctx.TREE_LAYOUTS[layout]
     finally:
-        ctx.set_tree_layout(False)
+        ctx.set_tree_layout("quant")
     bad = np.nonzero(got != exp)[0]
     assert len(bad) == 0, f"{len(bad)} of {len(got)} visibility bits differ, first at {bad[:8]}"
     assert 0.05 < exp.mean() < 0.95
 
 
-def test_wide_copy_left_out_when_boxes_are_not_nested(ctx, cuda, cfg1_scene):
+def test_quant_copy_left_out_when_a_deep_box_is_not_nested(ctx, cuda, cfg1_scene):
+    """The quantized copy tests only a triangle's own exact box, which keeps
+    the answer only when every box of the tree lies inside its parent's:
+    one inner node whose stored box is shrunk below its children's boxes
+    (at any depth, where the exact 4-wide copy may not mind) and no
+    quantized copy is built; the answers stay exact."""
+    s = cfg1_scene
+    nodes = s.nodes.copy()
+    # a node two levels down whose left child is an inner node: shrink the
+    # box it stores for that child
+    pick = next(i for i in range(3, len(nodes)) if nodes["left"][i] >= 0)
+    nodes["lmax"][pick, :3] -= np.float32(0.05) * (nodes["lmax"][pick, :3] - nodes["lmin"][pick, :3])
+    sn = dataclasses.replace(s, nodes=nodes)
+    p1, p2 = _segments(s, seed=24, n=30_000)
+    ctx.set_tree_layout("quant")
+    try:
+        got, exp = _gpu_vs_oracle(ctx, cuda, sn, p1, p2)
+        assert np.array_equal(got, exp), f"{np.count_nonzero(got != exp)} of {len(got)} bits differ"
+        assert ctx.stats().wide_nodes == 0 and ctx.stats().tree_layout == 0
+        ctx.upload_scene(s)
+        assert ctx.stats().tree_layout == 2
+    finally:
+        ctx.set_tree_layout("quant")
+
+
+@pytest.mark.parametrize("layout", ["wide", "quant"])
+def test_wide_copy_left_out_when_boxes_are_not_nested(ctx, cuda, cfg1_scene, layout):
     """A tree whose root stores boxes smaller than its children's boxes
     (possible for a tree handed to rg_upload_scene): the collapse must skip
     one of those boxes, which would no longer keep the answer, so no 4-wide
@@ -170,7 +205,7 @@ def test_wide_copy_left_out_when_boxes_are_not_nested(ctx, cuda, cfg1_scene):
     nodes["rmax"][0, :3] -= np.float32(0.3)
     sn = dataclasses.replace(s, nodes=nodes)
     p1, p2 = _segments(s, seed=23, n=30_000)
-    ctx.set_tree_layout(True)
+    ctx.set_tree_layout(layout)
     try:
         got, exp = _gpu_vs_oracle(ctx, cuda, sn, p1, p2)
         assert np.array_equal(got, exp), f"{np.count_nonzero(got != exp)} of {len(got)} bits differ"
@@ -178,4 +213,4 @@ def test_wide_copy_left_out_when_boxes_are_not_nested(ctx, cuda, cfg1_scene):
         ctx.upload_scene(s)
         assert ctx.stats().wide_nodes > 0
     finally:
-        ctx.set_tree_layout(False)
+        ctx.set_tree_layout("quant")
