@@ -451,17 +451,19 @@ int32_t host_pack_wide(const rg_aabb_tree_node *src, int32_t n, std::vector<floa
 }
 
 // ---------------------------------------------------------------- quantized 4-wide copy
-// The same collapse with each node's child boxes stored as 8-bit offsets
-// from the node's box (64-byte nodes: a third of the binary tree's bytes).
-// Per axis a node stores an origin o (its box's lower bound) and a power of
-// two s = 2^e; a child bound q decodes to RN(o + q*s) (q*s is exact, so an
-// FMA and an add of the product give the same float), and q is chosen so that
-// the decoded box contains the child's box: the largest q whose decoded value
-// is <= the lower bound, the smallest whose decoded value is >= the upper
-// bound.  e is the smallest exponent for which q = 255 decodes to at least
-// the node's upper bound.  Leaf slots link (as ~index) to leaf records that
-// hold the triangle's exact box from the reference's tree and the triangle
-// itself (host_pack_tris form).
+// The same collapse with each node's child boxes stored as 8-bit codes (64-
+// byte nodes: a third of the binary tree's bytes).  Per axis a node stores a
+// base c and a power of two s = 2^e; code q decodes to
+//   D(q) = RN((2^23 + q) * s + c),
+// one FMA on the float whose bits are 0x4B000000 | q (= 2^23 + q).  D is
+// non-decreasing in q.  c is the largest float with D(0) <= the node's lower
+// bound, e the smallest exponent with D(255) >= its upper bound, and per child
+// the lower code is the largest q with D(q) <= the child's lower bound, the
+// upper code the smallest with D(q) >= its upper bound, so the decoded box
+// contains the child's box.  The host evaluates D with fmaf, which rounds like
+// the device's FMA.  Leaf slots link (as ~index) to leaf records that hold the
+// triangle's exact box from the reference's tree and the triangle itself
+// (host_pack_tris form).
 //
 // The walk tests the decoded boxes only for a sure miss (a decoded box
 // contains the exact one, and the slab test is monotone under containment),
@@ -470,19 +472,39 @@ int32_t host_pack_wide(const rg_aabb_tree_node *src, int32_t n, std::vector<floa
 // box its parent stores for it (then a triangle's exact box passing implies
 // its whole box path passes); host_tree_nested checks that.
 //
-// Node (16 words): origin xyz (float) and biased exponents (bytes 0-2 of word
-// 3), then per axis a word of lower bounds and a word of upper bounds (byte k
-// = child k; x, y in words 4-7, z in words 8-9; 10-11 unused), then 4 links
+// Node (16 words): bases xyz (float) and biased exponents (bytes 0-2 of word
+// 3), then per axis a word of lower codes and a word of upper codes (byte k =
+// child k; x, y in words 4-7, z in words 8-9; 10-11 unused), then 4 links
 // (node index, ~leaf record index, or kNoChild).  Leaf record (16 floats):
 // lo.xyz hi.xyz, p1.xyz e1.xyz e2.xyz, 0.
 namespace {
-// RN(o + q * 2^(eb - 127)), the decode the device computes
-inline float qdecode(float o, int q, int eb) {
+inline float pow2f(int eb) {
     float s;
     const uint32_t bits = (uint32_t)eb << 23;
     memcpy(&s, &bits, 4);
-    const float qs = (float)q * s;  // exact: q < 256 and s a normal power of two
-    return o + qs;
+    return s;
+}
+// D(q) for biased exponent eb and base c
+inline float qdecode(int q, int eb, float c) { return fmaf(8388608.0f + (float)q, pow2f(eb), c); }
+
+// Base and biased exponent of one axis of a node with bounds [lo, hi]; false
+// when no exponent up to 246 (255 * s finite) reaches hi.
+bool quant_axis(float lo, float hi, float &c, int &eb) {
+    const double ext = (double)hi - (double)lo;
+    eb = 1;
+    if (ext > 0.0) eb = std::max(1, std::min(246, (int)std::ceil(std::log2(ext / 254.0)) + 127));
+    for (; eb <= 246; ++eb) {
+        const float s = pow2f(eb);
+        float cc = (float)((double)lo - std::ldexp(1.0, eb - 127 + 23));
+        while (fmaf(8388608.0f, s, cc) > lo) cc = std::nextafter(cc, -INFINITY);
+        while (fmaf(8388608.0f, s, std::nextafter(cc, INFINITY)) <= lo) cc = std::nextafter(cc, INFINITY);
+        const float top = qdecode(255, eb, cc);
+        if (std::isfinite(cc) && std::isfinite(top) && top >= hi) {
+            c = cc;
+            return true;
+        }
+    }
+    return false;
 }
 
 struct QuantBuilder {
@@ -500,37 +522,27 @@ struct QuantBuilder {
         const int32_t me = (int32_t)(nodes->size() / 16);
         nodes->resize(nodes->size() + 16, 0u);
         uint32_t w[16] = {0};
-        float org[3];
-        int eb[3];
+        float base[3] = {0.0f, 0.0f, 0.0f};
+        int eb[3] = {1, 1, 1};
         for (int a = 0; a < 3; ++a) {
             float lo = e[0].lo[a], hi = e[0].hi[a];
             for (int k = 1; k < n; ++k) { lo = std::min(lo, e[k].lo[a]); hi = std::max(hi, e[k].hi[a]); }
-            if (!std::isfinite(lo) || !std::isfinite(hi)) { ok = false; lo = hi = 0.0f; }
-            org[a] = lo;
-            // smallest biased exponent in [1, 246] (255 * s stays finite) that reaches hi
-            int b = 1;
-            const double ext = (double)hi - (double)lo;
-            if (ext > 0.0) b = std::max(1, std::min(246, (int)std::ceil(std::log2(ext / 255.0)) + 127));
-            while (b > 1 && qdecode(lo, 255, b - 1) >= hi) --b;
-            while (b < 246 && !(qdecode(lo, 255, b) >= hi)) ++b;
-            if (!(qdecode(lo, 255, b) >= hi) || !std::isfinite(qdecode(lo, 255, b))) ok = false;
-            eb[a] = b;
-            memcpy(&w[a], &org[a], 4);
+            if (!std::isfinite(lo) || !std::isfinite(hi) || !quant_axis(lo, hi, base[a], eb[a])) ok = false;
+            memcpy(&w[a], &base[a], 4);
         }
         w[3] = (uint32_t)eb[0] | ((uint32_t)eb[1] << 8) | ((uint32_t)eb[2] << 16);
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < 4 && ok; ++k) {
             const WEntry &c = e[k < n ? k : n - 1];  // an empty slot repeats the last child (ignored)
             for (int a = 0; a < 3; ++a) {
-                const double sa = std::ldexp(1.0, eb[a] - 127);
-                int ql = (int)std::floor(((double)c.lo[a] - (double)org[a]) / sa);
-                ql = std::max(0, std::min(255, ql));
-                while (ql > 0 && qdecode(org[a], ql, eb[a]) > c.lo[a]) --ql;
-                while (ql < 255 && qdecode(org[a], ql + 1, eb[a]) <= c.lo[a]) ++ql;
-                int qh = (int)std::ceil(((double)c.hi[a] - (double)org[a]) / sa);
-                qh = std::max(0, std::min(255, qh));
-                while (qh < 255 && qdecode(org[a], qh, eb[a]) < c.hi[a]) ++qh;
-                while (qh > 0 && qdecode(org[a], qh - 1, eb[a]) >= c.hi[a]) --qh;
-                if (!(qdecode(org[a], ql, eb[a]) <= c.lo[a]) || !(qdecode(org[a], qh, eb[a]) >= c.hi[a])) ok = false;
+                // start from the real-valued estimate, then step to the exact codes
+                const double s = std::ldexp(1.0, eb[a] - 127), o = (double)base[a] + 8388608.0 * s;
+                int ql = (int)std::max(0.0, std::min(255.0, std::floor(((double)c.lo[a] - o) / s)));
+                int qh = (int)std::max(0.0, std::min(255.0, std::ceil(((double)c.hi[a] - o) / s)));
+                while (ql > 0 && qdecode(ql, eb[a], base[a]) > c.lo[a]) --ql;
+                while (ql < 255 && qdecode(ql + 1, eb[a], base[a]) <= c.lo[a]) ++ql;
+                while (qh < 255 && qdecode(qh, eb[a], base[a]) < c.hi[a]) ++qh;
+                while (qh > 0 && qdecode(qh - 1, eb[a], base[a]) >= c.hi[a]) --qh;
+                if (!(qdecode(ql, eb[a], base[a]) <= c.lo[a]) || !(qdecode(qh, eb[a], base[a]) >= c.hi[a])) ok = false;
                 w[4 + 2 * a] |= (uint32_t)ql << (8 * k);
                 w[5 + 2 * a] |= (uint32_t)qh << (8 * k);
             }

@@ -45,13 +45,13 @@ struct WNode {
 };
 constexpr int32_t kWideNoChild = INT32_MIN;
 
-// QNode 64 B: the quantized 4-wide copy (host_pack_quant).  Per axis an
-// origin and a power of two s (biased exponent bytes in org.w); child k's
-// bounds are byte k of the axis' lower and upper words, decoding to
-// RN(origin + q * s), a box containing the child's exact box.  Links: >= 0
-// node, < 0 leaf record ~r, kWideNoChild = empty.
+// QNode 64 B: the quantized 4-wide copy (host_pack_quant).  Per axis a base
+// c and a power of two s (biased exponent bytes in base.w); child k's bounds
+// are byte k of the axis' lower and upper code words, code q decoding to
+// RN((2^23 + q) * s + c), a box containing the child's exact box.  Links:
+// >= 0 node, < 0 leaf record ~r, kWideNoChild = empty.
 struct QNode {
-    float4 org;  // origin.xyz, exponent bytes (x, y, z)
+    float4 base; // c.xyz, exponent bytes (x, y, z)
     uint4 qxy;   // lo x, hi x, lo y, hi y (byte k: child k)
     uint4 qz;    // lo z, hi z, 0, 0
     int4 d;      // links of children 0..3

@@ -522,37 +522,60 @@ __device__ void trace_wide_loop(const DevScene &s, Fetch fetch, int n, int *next
     }
 }
 
-// Bytes sel0, sel1 of a word of 8-bit bounds decoded to RN(origin + q * sc)
-// as a packed pair: 2^23 + q is built from the byte's bits, 2^23 taken off
-// (exact), then one FMA (q * sc is exact, so the FMA rounds once, like the
-// host's add of the product).
-__device__ __forceinline__ float2 qdecode2(unsigned w, unsigned sel0, unsigned sel1, float2 sc, float2 org) {
+// Codes sel0, sel1 (byte selectors) of a word decoded as a packed pair:
+// D(q) = RN((2^23 + q) * s + c), one FMA on the float whose bits are
+// 0x4B000000 | q.
+__device__ __forceinline__ float2 qdecode2(unsigned w, unsigned sel0, unsigned sel1, float2 sc, float2 base) {
     const float2 f = make_float2(__uint_as_float(__byte_perm(w, 0x4B000000u, sel0)),
                                  __uint_as_float(__byte_perm(w, 0x4B000000u, sel1)));
-    return __ffma2_rn(__fadd2_rn(f, make_float2(-8388608.0f, -8388608.0f)), sc, org);
+    return __ffma2_rn(f, sc, base);
 }
 
-// Children 2p, 2p+1 of a quantized node: the filtered test's sure-miss
-// decision on their decoded boxes (bit 0 / bit 1 set when not surely missed).
-__device__ __forceinline__ unsigned qpair_live(f3 o, f3 inv, const float4 &org, const uint4 &qa, const uint4 &qb,
-                                               float2 sx, float2 sy, float2 sz, int p) {
+// Per-ray and per-node operands of the quantized box tests.  Each axis' near
+// and far code words are picked by the sign of the ray's direction (near =
+// lower bounds where it is positive), so the slab distances come out ordered:
+// t(near) <= t(far), because b - o and the product with 1/d round
+// monotonically; they equal the min and max of the two distances.
+struct QAxes {
+    unsigned nx, fx, ny, fy, nz, fz;  // near / far code words
+};
+__device__ __forceinline__ QAxes qaxes(f3 inv, const uint4 &qa, const uint4 &qb) {
+    QAxes a;
+    const bool sx = inv.x < 0.0f, sy = inv.y < 0.0f, sz = inv.z < 0.0f;
+    a.nx = sx ? qa.y : qa.x; a.fx = sx ? qa.x : qa.y;
+    a.ny = sy ? qa.w : qa.z; a.fy = sy ? qa.z : qa.w;
+    a.nz = sz ? qb.y : qb.x; a.fz = sz ? qb.x : qb.y;
+    return a;
+}
+
+// The sure-miss part of the filtered decision with a constant difference
+// margin: where rmin~ <= 1 + E and rmax~ >= -T, a difference below -SS
+// needs rmax~ < rmin~, so both lie in [-T, 1 + E] and E (|rmin~| + |rmax~|)
+// + T < 2^-17 = SS; the test is therefore never looser than
+// filtered_decision's.
+__device__ __forceinline__ bool filtered_miss(float rmin, float rmax) {
+    constexpr float kEps = 1.9073486328125e-6f;     // 2^-19
+    constexpr float kTiny = 8.0779356694631609e-28f; // 2^-90
+    constexpr float kSS = 7.62939453125e-6f;         // 2^-17
+    return rmin > 1.0f + kEps || rmax < -kTiny || rmax - rmin < -kSS;
+}
+
+// Children 2p, 2p+1 of a quantized node: bit 0 / bit 1 set when the filtered
+// test does not surely miss their decoded boxes.
+__device__ __forceinline__ unsigned qpair_live(f3 o, f3 inv, const float4 &base, const QAxes &w, float2 sx,
+                                               float2 sy, float2 sz, int p) {
     const unsigned s0 = 0x7440u + 2u * (unsigned)p, s1 = s0 + 1u;
-    const float2 ox = make_float2(org.x, org.x), oy = make_float2(org.y, org.y), oz = make_float2(org.z, org.z);
+    const float2 cx = make_float2(base.x, base.x), cy = make_float2(base.y, base.y), cz = make_float2(base.z, base.z);
     const float2 nox = make_float2(-o.x, -o.x), noy = make_float2(-o.y, -o.y), noz = make_float2(-o.z, -o.z);
     const float2 ix = make_float2(inv.x, inv.x), iy = make_float2(inv.y, inv.y), iz = make_float2(inv.z, inv.z);
-    const float2 t0x = __fmul2_rn(__fadd2_rn(qdecode2(qa.x, s0, s1, sx, ox), nox), ix);
-    const float2 t1x = __fmul2_rn(__fadd2_rn(qdecode2(qa.y, s0, s1, sx, ox), nox), ix);
-    const float2 t0y = __fmul2_rn(__fadd2_rn(qdecode2(qa.z, s0, s1, sy, oy), noy), iy);
-    const float2 t1y = __fmul2_rn(__fadd2_rn(qdecode2(qa.w, s0, s1, sy, oy), noy), iy);
-    const float2 t0z = __fmul2_rn(__fadd2_rn(qdecode2(qb.x, s0, s1, sz, oz), noz), iz);
-    const float2 t1z = __fmul2_rn(__fadd2_rn(qdecode2(qb.y, s0, s1, sz, oz), noz), iz);
-    const float rminl = max3f(fminf(t0x.x, t1x.x), fminf(t0y.x, t1y.x), fminf(t0z.x, t1z.x));
-    const float rmaxl = min3f(fmaxf(t0x.x, t1x.x), fmaxf(t0y.x, t1y.x), fmaxf(t0z.x, t1z.x));
-    const float rminr = max3f(fminf(t0x.y, t1x.y), fminf(t0y.y, t1y.y), fminf(t0z.y, t1z.y));
-    const float rmaxr = min3f(fmaxf(t0x.y, t1x.y), fmaxf(t0y.y, t1y.y), fmaxf(t0z.y, t1z.y));
-    bool hl, ml, hr, mr;
-    filtered_decision(rminl, rmaxl, hl, ml);
-    filtered_decision(rminr, rmaxr, hr, mr);
+    const float2 tnx = __fmul2_rn(__fadd2_rn(qdecode2(w.nx, s0, s1, sx, cx), nox), ix);
+    const float2 tfx = __fmul2_rn(__fadd2_rn(qdecode2(w.fx, s0, s1, sx, cx), nox), ix);
+    const float2 tny = __fmul2_rn(__fadd2_rn(qdecode2(w.ny, s0, s1, sy, cy), noy), iy);
+    const float2 tfy = __fmul2_rn(__fadd2_rn(qdecode2(w.fy, s0, s1, sy, cy), noy), iy);
+    const float2 tnz = __fmul2_rn(__fadd2_rn(qdecode2(w.nz, s0, s1, sz, cz), noz), iz);
+    const float2 tfz = __fmul2_rn(__fadd2_rn(qdecode2(w.fz, s0, s1, sz, cz), noz), iz);
+    const bool ml = filtered_miss(max3f(tnx.x, tny.x, tnz.x), min3f(tfx.x, tfy.x, tfz.x));
+    const bool mr = filtered_miss(max3f(tnx.y, tny.y, tnz.y), min3f(tfx.y, tfy.y, tfz.y));
     return (ml ? 0u : 1u) | (mr ? 0u : 2u);
 }
 
@@ -657,15 +680,16 @@ __device__ void trace_quant_loop(const DevScene &s, Fetch fetch, int n, int *nex
                 continue;
             }
             const QNode *np = s.qnodes + node;
-            const float4 org = __ldg(&np->org);
+            const float4 base = __ldg(&np->base);
             const uint4 qa = __ldg(&np->qxy), qb = __ldg(&np->qz);
             const int4 ch = __ldg(&np->d);
-            const unsigned eb = __float_as_uint(org.w);
+            const unsigned eb = __float_as_uint(base.w);
             const float ex = __uint_as_float((eb & 0xffu) << 23), ey = __uint_as_float(((eb >> 8) & 0xffu) << 23),
                         ez = __uint_as_float(((eb >> 16) & 0xffu) << 23);
             const float2 sx = make_float2(ex, ex), sy = make_float2(ey, ey), sz = make_float2(ez, ez);
-            const unsigned live = qpair_live(o, inv, org, qa, qb, sx, sy, sz, 0) |
-                                  (qpair_live(o, inv, org, qa, qb, sx, sy, sz, 1) << 2);
+            const QAxes w = qaxes(inv, qa, qb);
+            const unsigned live = qpair_live(o, inv, base, w, sx, sy, sz, 0) |
+                                  (qpair_live(o, inv, base, w, sx, sy, sz, 1) << 2);
             const bool h0 = (live & 1u) != 0u, h1 = (live & 2u) != 0u;
             const bool h2 = (live & 4u) != 0u && ch.z != kWideNoChild, h3 = (live & 8u) != 0u && ch.w != kWideNoChild;
             leafmask = (h0 && ch.x < 0 ? 1u : 0u) | (h1 && ch.y < 0 ? 2u : 0u) | (h2 && ch.z < 0 ? 4u : 0u) |
