@@ -51,7 +51,7 @@ constexpr int32_t kWideNoChild = INT32_MIN;
 // RN((2^23 + q) * s + c), a box containing the child's exact box.  Links:
 // >= 0 node, < 0 leaf record ~r, kWideNoChild = empty.
 struct QNode {
-    float4 base; // c.xyz, exponent bytes (x, y, z)
+    float4 base; // c.xyz, exponent bytes (x, y, z) and slot masks (leaf bits 0-3, inner bits 4-7)
     uint4 qxy;   // lo x, hi x, lo y, hi y (byte k: child k)
     uint4 qz;    // lo z, hi z, 0, 0
     int4 d;      // links of children 0..3
