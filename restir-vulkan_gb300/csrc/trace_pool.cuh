@@ -623,6 +623,28 @@ __device__ __forceinline__ bool qleaf_hit(const QLeaf *lp, f3 o, f3 d, f3 inv) {
     return hit && rgm::ray_tri(mk(b.z, b.w, c.x), mk(c.y, c.z, c.w), mk(e.x, e.y, e.z), o, d);
 }
 
+// RG_LEAF_SLOTS: parked leaf sets a lane may hold in the quantized walk (1
+// or 2).  With two, a lane that parks a node's leaves keeps walking until it
+// parks a second set, so fewer lanes sit idle in the walk phase and the leaf
+// phase tests more lanes at once.
+#ifndef RG_LEAF_SLOTS
+#define RG_LEAF_SLOTS 2
+#endif
+
+// The parked leaves of one node ((node << 4) | mask of its leaf slots): the
+// exact box gate and the triangle test of each until one hits.
+__device__ __forceinline__ bool qparked_hit(const DevScene &s, unsigned e, f3 o, f3 d, f3 inv, TraceStats &ts) {
+    const int4 ch = __ldg(&s.qnodes[e >> 4].d);
+    bool hit = false;
+    for (unsigned m = e & 15u; m != 0u && !hit; m &= m - 1u) {
+        const int k = __ffs(m) - 1;
+        const int link = k == 0 ? ch.x : k == 1 ? ch.y : k == 2 ? ch.z : ch.w;
+        hit = qleaf_hit(s.qleaves + ~link, o, d, inv);
+        ++ts.tri_tests;
+    }
+    return hit;
+}
+
 // The loop over the quantized 4-wide copy (DevScene::qnodes): a node visit
 // decodes its four child boxes and drops those the filtered test surely
 // misses (a decoded box contains the exact one, so the reference's test
@@ -639,8 +661,7 @@ __device__ void trace_quant_loop(const DevScene &s, Fetch fetch, int n, int *nex
     int cur = -1;          // pool index of this lane's segment, -1: none
     bool retired = false;  // the pool has no segment left for this lane
     int owner = 0, node = 0, sp = 0, visits = 0;
-    unsigned leafmask = 0; // parked leaves: links of leaf_node
-    int leaf_node = 0;
+    unsigned park0 = 0u, park1 = 0u;  // parked leaves, (node << 4) | leaf slot mask; 0: none
     bool walked = false;   // tree walk finished, only parked leaves remain
     f3 o = mk(0.f, 0.f, 0.f), d = o, inv = o;
     while (true) {
@@ -662,7 +683,7 @@ __device__ void trace_quant_loop(const DevScene &s, Fetch fetch, int n, int *nex
                         node = 0;
                         sp = 0;
                         visits = 0;
-                        leafmask = 0u;
+                        park0 = park1 = 0u;
                         walked = false;
                     } else {
                         emit(owner, trace_exact_binary(s, o, d, ts));
@@ -671,21 +692,16 @@ __device__ void trace_quant_loop(const DevScene &s, Fetch fetch, int n, int *nex
             }
         }
         if (__all_sync(kFull, retired)) break;
-        // 2. parked leaves
-        const bool has_leaf = cur >= 0 && leafmask != 0u;
-        const unsigned m_leaf = __ballot_sync(kFull, has_leaf);
-        const unsigned m_walk = __ballot_sync(kFull, cur >= 0 && leafmask == 0u && !walked);
-        if (m_leaf != 0u && (__popc(m_leaf) >= RG_LEAF_MIN || m_walk == 0u)) {
-            if (has_leaf) {
-                const int4 ch = __ldg(&s.qnodes[leaf_node].d);
-                bool hit = false;
-                for (unsigned m = leafmask; m != 0u && !hit; m &= m - 1u) {
-                    const int k = __ffs(m) - 1;
-                    const int link = k == 0 ? ch.x : k == 1 ? ch.y : k == 2 ? ch.z : ch.w;
-                    hit = qleaf_hit(s.qleaves + ~link, o, d, inv);
-                    ++ts.tri_tests;
-                }
-                leafmask = 0u;
+        // 2. parked leaves, once enough lanes cannot walk on (walk ended or
+        //    every slot taken) or none can; every lane holding some tests them
+        const bool blocked = cur >= 0 && (walked || (RG_LEAF_SLOTS == 1 ? park0 : park1) != 0u);
+        const unsigned m_block = __ballot_sync(kFull, blocked);
+        const unsigned m_walk = __ballot_sync(kFull, cur >= 0 && !blocked);
+        if (m_block != 0u && (__popc(m_block) >= RG_LEAF_MIN || m_walk == 0u)) {
+            if (cur >= 0 && park0 != 0u) {
+                bool hit = qparked_hit(s, park0, o, d, inv, ts);
+                if (!hit && park1 != 0u) hit = qparked_hit(s, park1, o, d, inv, ts);
+                park0 = park1 = 0u;
                 if (hit || walked) {
                     emit(owner, hit);
                     cur = -1;
@@ -695,7 +711,9 @@ __device__ void trace_quant_loop(const DevScene &s, Fetch fetch, int n, int *nex
         }
         // 3. up to RG_WALK_STEPS nodes per walking lane
 #pragma unroll 1
-        for (int step = 0; step < RG_WALK_STEPS && cur >= 0 && leafmask == 0u && !walked; ++step) {
+        for (int step = 0; step < RG_WALK_STEPS && cur >= 0 && !walked &&
+                           (RG_LEAF_SLOTS == 1 ? park0 : park1) == 0u;
+             ++step) {
             ++ts.visits;
             if (++visits > s.n_qnodes) {
                 ts.err = true;
@@ -714,8 +732,12 @@ __device__ void trace_quant_loop(const DevScene &s, Fetch fetch, int n, int *nex
             const QAxes w = qaxes(inv, qa, qb);
             const unsigned live = qpair_live(o, inv, base, w, sx, sy, sz, 0) |
                                   (qpair_live(o, inv, base, w, sx, sy, sz, 1) << 2);
-            leafmask = live & (eb >> 24) & 15u;
-            if (leafmask) leaf_node = node;
+            const unsigned leafmask = live & (eb >> 24) & 15u;
+            if (leafmask != 0u) {
+                const unsigned e = ((unsigned)node << 4) | leafmask;
+                if (park0 == 0u) park0 = e;
+                else park1 = e;
+            }
             const unsigned im = live & (eb >> 28);
             if (im != 0u) {
                 // the first inner child is walked next, the others pushed
@@ -729,7 +751,7 @@ __device__ void trace_quant_loop(const DevScene &s, Fetch fetch, int n, int *nex
                 node = my_stack[--sp];
             } else {
                 walked = true;
-                if (leafmask == 0u) {
+                if (park0 == 0u) {
                     emit(owner, false);
                     cur = -1;
                 }
