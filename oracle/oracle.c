@@ -827,11 +827,11 @@ int or_spatial_unbiased(const or_scene *sc, const or_gbuffer *g, const or_reserv
     const v3 cam = f4xyz(u->camera_pos);
     const int vis = (u->flags & OR_FLAG_VISIBILITY) != 0;
     trav_count tot = {0, 0, 0, 0};
-    uint64_t rays = 0;
+    uint64_t rays = 0, unobs = 0;
 #pragma omp parallel
     {
         trav_count tc = {0, 0, 0, 0};
-        uint64_t my_rays = 0;
+        uint64_t my_rays = 0, my_unobs = 0;
 #pragma omp for schedule(dynamic, 64)
         for (int64_t pi = 0; pi < (int64_t)cw * ch; ++pi) {
             int x = x0 + (int)(pi % cw), y = y0 + (int)(pi / cw);
@@ -885,10 +885,12 @@ int or_spatial_unbiased(const or_scene *sc, const or_gbuffer *g, const or_reserv
 #else
                 uint32_t ns = in[ri].m;  /* the reservoir's own count before the merges */
 #endif
+                uint64_t neighbour_rays = 0;
                 for (int j = 0; j < num_neighbors; ++j) {
                     if (vdot(vsub(lpos, nt[j].wpos), nt[j].normal) < 0.0f) continue;
                     if (vis) {
                         ++my_rays;
+                        ++neighbour_rays;
                         if (test_visibility(sc, nt[j].wpos, lpos, &tc)) continue;
                     }
 #if OR_MIS
@@ -900,6 +902,7 @@ int or_spatial_unbiased(const or_scene *sc, const or_gbuffer *g, const or_reserv
                 if (vis) {
                     ++my_rays;
                     if (test_visibility(sc, t.wpos, lpos, &tc)) {
+                        my_unobs += neighbour_rays;
 #if OR_MIS
                         sum_phat = 0.0f;
 #else
@@ -932,9 +935,11 @@ int or_spatial_unbiased(const or_scene *sc, const or_gbuffer *g, const or_reserv
             tot.node_visits += tc.node_visits; tot.box_tests += tc.box_tests;
             tot.tri_tests += tc.tri_tests; tot.overflows += tc.overflows;
             rays += my_rays;
+            unobs += my_unobs;
         }
     }
     stats_add(st, &tot, rays);
+    if (st) st->rays_unobservable += unobs;
     return 0;
 }
 

@@ -128,6 +128,9 @@ typedef struct {
     uint64_t box_tests;
     uint64_t tri_tests;
     uint64_t stack_overflows;
+    uint64_t rays_unobservable; /* unbiased pass: neighbour segments of a sample whose own segment is
+                                   shadowed (the count is then reset, so their answers never reach
+                                   the output) */
 } or_stats;
 
 /* ---- primitives ---- */

@@ -53,7 +53,7 @@ class GBuffer(C.Structure):
 
 class Stats(C.Structure):
     _fields_ = [("rays", C.c_uint64), ("node_visits", C.c_uint64), ("box_tests", C.c_uint64),
-                ("tri_tests", C.c_uint64), ("stack_overflows", C.c_uint64)]
+                ("tri_tests", C.c_uint64), ("stack_overflows", C.c_uint64), ("rays_unobservable", C.c_uint64)]
 
 
 _oracle = None

@@ -248,8 +248,12 @@ __device__ __forceinline__ void count_block_rays(const DevScene &s, int rays, co
     const unsigned errs = __popc(__ballot_sync(kFull, ts.err));
     const unsigned visits = __reduce_add_sync(kFull, ts.visits);
     const unsigned tris = __reduce_add_sync(kFull, ts.tri_tests);
+    const unsigned skipped = __reduce_add_sync(kFull, ts.skipped);
     const int tid = threadIdx.x + threadIdx.y * blockDim.x;
     if ((tid & 31) == 0) {
+        // segments the pool skipped are not traced: subtracted from the
+        // block's count (modular 64-bit addition; the total stays exact)
+        if (skipped) atomicAdd(&s.counters[0], 0ull - (unsigned long long)skipped);
         if (errs) atomicAdd(&s.counters[1], (unsigned long long)errs);
         if (visits) atomicAdd(&s.counters[2], (unsigned long long)visits);
         if (tris) atomicAdd(&s.counters[3], (unsigned long long)tris);
@@ -713,13 +717,19 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
         for (int q = 0; q < R; ++q) lpos[q] = xyz(r.pos_lum[q]);
         store_resv(p.out, i, r);
     }
-    // A pixel's segments (one per neighbour whose hemisphere holds the sample,
-    // and its own) share the sample's light as their end point: they go to the
-    // pool consecutively, so the lanes that take them trace similar paths.
+    // Each pixel's own segment goes to the front of the pool, so lanes take
+    // those first.  When the pixel's own segment is shadowed, its count is
+    // reset whatever its neighbours' segments answer (unbiasedReuse.glsl:
+    // 168-176), so a lane that takes a neighbour's segment whose pixel's own
+    // answer is already known shadowed skips it.  A pixel's neighbour
+    // segments (one per neighbour whose hemisphere holds the sample) share the
+    // sample's light as their end point: they follow consecutively, so the
+    // lanes that take them trace similar paths.
+    uint32_t wantm[R];  // bit k: neighbour k's segment
 #pragma unroll
     for (int q = 0; q < R; ++q) {
         endp[q * BT + tid] = make_float4(lpos[q].x, lpos[q].y, lpos[q].z, 0.0f);
-        uint32_t wantm = 0;  // bit k: neighbour k's segment; bit K: the pixel's own
+        wantm[q] = 0u;
         for (int k = 0; k < K; ++k) {
             bool excluded = true;
             if (valid) {
@@ -727,14 +737,20 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
                 const f3 nw = load_wpos(p.g, ni);
                 const f3 nn = load_normal(p.g, ni);
                 excluded = dot(lpos[q] - nw, nn) < 0.0f;
-                if (!excluded && vis) wantm |= 1u << k;
+                if (!excluded && vis) wantm[q] |= 1u << k;
             }
             flag[(q * slots + k) * BT + tid] = excluded ? 1 : 0;
         }
         flag[(q * slots + K) * BT + tid] = 0;
-        if (valid && vis) wantm |= 1u << K;
-        int slot = rgpool::append_range(&s_count, __popc(wantm));
-        for (uint32_t m = wantm; m != 0u; m &= m - 1u) {
+        const bool own = valid && vis;
+        const int slot = rgpool::append_range(&s_count, own ? 1 : 0);
+        if (own) pool[slot] = (q * slots + K) * BT + tid;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+        int slot = rgpool::append_range(&s_count, __popc(wantm[q]));
+        for (uint32_t m = wantm[q]; m != 0u; m &= m - 1u) {
             const int k = __ffs(m) - 1;
             pool[slot++] = (q * slots + k) * BT + tid;
         }
@@ -747,6 +763,8 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
             const int owner = pool[slot];
             const int r = owner % (slots * BT);
             const int k = r / BT, t = r % BT;
+            if (k < K && reinterpret_cast<volatile const uint8_t *>(flag)[(owner / (slots * BT) * slots + K) * BT + t])
+                return -1;  // the pixel's own segment is shadowed: this answer is unobservable
             const size_t pi = k < K ? (size_t)nidx[k * BT + t]
                                     : (size_t)(by * (BT / TW) + t / TW) * (size_t)W + (size_t)(bx * TW + t % TW);
             p1 = load_wpos(p.g, pi);

@@ -220,11 +220,13 @@ struct TraceStats {
     bool err = false;        // walk exceeded one visit per node or the stack (malformed tree)
     unsigned visits = 0;     // tree nodes visited
     unsigned tri_tests = 0;  // triangle tests
+    unsigned skipped = 0;    // pool segments the fetch declined (answer unobservable)
 };
 
 // Traces pool slots 0..n-1 with all threads of the block; `fetch(k, p1)`
-// returns slot k's owner tag and sets its segment start p1; reports shadowed
-// (1) / unoccluded (0) through `emit(owner, shadowed)`.  `stack` points at
+// returns slot k's owner tag and sets its segment start p1, or returns a
+// negative tag to skip the slot (no trace, no emit); reports shadowed (1) /
+// unoccluded (0) through `emit(owner, shadowed)`.  `stack` points at
 // blockDim.x * blockDim.y * depth ints of shared memory.  Sets ts.err on a
 // walk longer than one visit per node or a stack overflow (malformed tree;
 // not reachable for trees validated at upload).  Every thread of the block
@@ -259,12 +261,13 @@ __device__ void trace_binary_loop(const DevScene &s, Fetch fetch, int n, int *ne
         if (m_idle != 0u && (__popc(m_idle) >= RG_FETCH_MIN || m_busy == 0u)) {
             if (idle) {
                 const int k = atomicAdd(next, 1);
+                f3 p1;
                 if (k >= n) {
                     retired = true;
+                } else if ((owner = fetch(k, p1)) < 0) {
+                    ++ts.skipped;
                 } else {
                     cur = k;
-                    f3 p1;
-                    owner = fetch(k, p1);
                     rgm::shadow_segment(p1, endpoint(owner), o, d);
                     fast = ray_inverse(d, inv) && !s.box_nan;
                     node = 0;
@@ -422,11 +425,12 @@ __device__ void trace_wide_loop(const DevScene &s, Fetch fetch, int n, int *next
         if (m_idle != 0u && (__popc(m_idle) >= RG_FETCH_MIN || m_busy == 0u)) {
             if (idle) {
                 const int k = atomicAdd(next, 1);
+                f3 p1;
                 if (k >= n) {
                     retired = true;
+                } else if ((owner = fetch(k, p1)) < 0) {
+                    ++ts.skipped;
                 } else {
-                    f3 p1;
-                    owner = fetch(k, p1);
                     rgm::shadow_segment(p1, endpoint(owner), o, d);
                     if (ray_inverse(d, inv)) {
                         cur = k;
@@ -678,11 +682,12 @@ __device__ void trace_quant_loop(const DevScene &s, Fetch fetch, int n, int *nex
         if (m_idle != 0u && (__popc(m_idle) >= RG_FETCH_MIN || m_busy == 0u)) {
             if (idle) {
                 const int k = atomicAdd(next, 1);
+                f3 p1;
                 if (k >= n) {
                     retired = true;
+                } else if ((owner = fetch(k, p1)) < 0) {
+                    ++ts.skipped;
                 } else {
-                    f3 p1;
-                    owner = fetch(k, p1);
                     rgm::shadow_segment(p1, endpoint(owner), o, d);
                     if (ray_inverse(d, inv)) {
                         cur = k;

@@ -151,7 +151,12 @@ def test_unbiased_pass_counts_rays(ctx, cfg2_small, cuda):
     ctx.stats(reset=True)
     ctx.spatial_unbiased(dg, reservoirs_from_numpy(r0), out, u, 3, 0)
     assert mismatch(reservoirs_to_numpy(out), r1) == 0
-    assert ctx.stats().rays_traced == st.rays
+    # every segment whose answer reaches the output is traced; a neighbour's
+    # segment whose pixel's own segment is shadowed may be skipped (the count
+    # is reset whatever it answers), depending on which finishes first
+    got = ctx.stats().rays_traced
+    assert st.rays - st.rays_unobservable <= got <= st.rays, (got, st.rays, st.rays_unobservable)
+    assert st.rays_unobservable > 0
 
 
 @pytest.mark.parametrize("crop", [(0, 0, 64, 64), (928, 508, 64, 64), (1856, 1016, 64, 64)])
