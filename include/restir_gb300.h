@@ -302,6 +302,22 @@ int rg_reservoir_bytes(rg_context *ctx);
 #define RG_TREE_QUANT4 2
 int rg_set_tree_layout(rg_context *ctx, int32_t layout);
 
+/* ---- visibility cache between ray passes ----
+ * No counterpart in the reference, which traces every segment.  With the
+ * cache on (the default), rg_initial_temporal and rg_spatial_unbiased record
+ * the answer of each pixel's own visibility segment (its world position to
+ * its sample's light) together with the segment's two end points, and the
+ * next of those passes takes the answer of any segment equal to a recorded
+ * one bit for bit instead of tracing it (a pixel that kept its sample meets
+ * its own segment again; one that took a neighbour's sample meets that
+ * neighbour's own segment).  Results are unchanged: an answer depends only on
+ * the scene and the two points, and an upload clears the record.  The record
+ * lives in the context (32 bytes per pixel and sample, two buffers), so
+ * passes of one context must run in order: on one stream, or with the
+ * caller synchronising between streams; turn the cache off otherwise.  The
+ * batched-view and allocation-free entry points do not use it. */
+int rg_set_visibility_cache(rg_context *ctx, int32_t enable);
+
 /* ---- scene upload (host pointers; copied to device, synchronous) ---- */
 int rg_upload_scene(rg_context *ctx, const rg_scene_desc *scene);
 

@@ -101,6 +101,13 @@ struct rg_context {
     float4 *image = nullptr;
     GBufSlot gslot[2];
     bool gslot_valid[2] = {false, false};
+    // visibility cache of own-segment answers between ray passes (VisCache)
+    float4 *vc_buf[2] = {nullptr, nullptr};
+    size_t vc_cap = 0;        // entries per buffer
+    int vc_cur = 0;           // the buffer the last ray pass wrote
+    uint32_t vc_tag = 0;
+    bool vc_on = true;        // rg_set_visibility_cache
+    bool vc_dirty = true;     // clear before the next use (new scene, new buffers)
 
     void release_scene() {
         proposal_release(proposal);
@@ -209,6 +216,8 @@ int rg_destroy(rg_context *ctx) {
     ctx->release_frame();
     dev_free(ctx->counters);
     dev_free(ctx->mma_timeouts);
+    dev_free(ctx->vc_buf[0]);
+    dev_free(ctx->vc_buf[1]);
     delete ctx;
     return RG_OK;
 }
@@ -426,6 +435,53 @@ int rg_upload_scene(rg_context *ctx, const rg_scene_desc *sc) {
     s.res_samples = ctx->res_samples;
     s.res_mis = ctx->res_mis;
     ctx->has_scene = true;
+    ctx->vc_dirty = true;  // cached answers belong to the previous scene
+    return RG_OK;
+}
+
+namespace {
+// The cache buffers of the next ray pass over `pixels` pixels: reads what the
+// previous ray pass wrote, writes the other buffer.  Entries hold whole
+// segments, so a pass never takes an answer for another segment, whatever
+// ran before it; the buffers are cleared after a scene upload.
+int vcache_next(rg_context *ctx, size_t pixels, cudaStream_t st, VisCache *vc) {
+    *vc = VisCache{};
+    const size_t entries = pixels * (size_t)ctx->res_samples;
+    if (!ctx->vc_on || entries == 0) return RG_OK;
+    if (entries > ctx->vc_cap) {
+        dev_free(ctx->vc_buf[0]);
+        dev_free(ctx->vc_buf[1]);
+        ctx->vc_cap = 0;
+        cudaError_t e = dev_alloc(&ctx->vc_buf[0], 2 * entries);
+        if (e == cudaSuccess) e = dev_alloc(&ctx->vc_buf[1], 2 * entries);
+        if (e != cudaSuccess) {
+            dev_free(ctx->vc_buf[0]);
+            return cuda_fail(e, "visibility cache");
+        }
+        ctx->vc_cap = entries;
+        ctx->vc_dirty = true;
+    }
+    if (ctx->vc_dirty) {
+        for (int b = 0; b < 2; ++b) RG_CUDA(cudaMemsetAsync(ctx->vc_buf[b], 0, ctx->vc_cap * 32, st), "visibility cache");
+        ctx->vc_dirty = false;
+    }
+    ctx->vc_tag = ctx->vc_tag >= 0x7fffffffu ? 1u : ctx->vc_tag + 1u;  // a reused tag is harmless: it only
+                                                                       // pairs an entry's two halves
+    vc->in = ctx->vc_buf[ctx->vc_cur];
+    vc->out = ctx->vc_buf[1 - ctx->vc_cur];
+    vc->tag = ctx->vc_tag;
+    vc->n = (uint32_t)pixels;
+    ctx->vc_cur = 1 - ctx->vc_cur;
+    return RG_OK;
+}
+}  // namespace
+
+int rg_set_visibility_cache(rg_context *ctx, int32_t enable) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (enable != 0 && enable != 1) return fail(RG_ERR_INVALID_ARGUMENT, "enable must be 0 or 1");
+    if (enable && !ctx->vc_on) ctx->vc_dirty = true;
+    ctx->vc_on = enable != 0;
     return RG_OK;
 }
 
@@ -450,8 +506,10 @@ int rg_initial_temporal(rg_context *ctx, const rg_gbuffer *cur, const rg_gbuffer
         pv = make_view(prev);
     }
     const GBufView cv = make_view(cur);
+    VisCache vc;
+    if ((rc = vcache_next(ctx, (size_t)u->screen_size[0] * u->screen_size[1], (cudaStream_t)stream, &vc))) return rc;
     RG_CUDA(launch_initial_temporal(ctx->scene, cv, temporal ? &pv : nullptr, temporal ? prev_res : nullptr, out, *u,
-                                    learned.cand ? &learned : nullptr, (cudaStream_t)stream),
+                                    learned.cand ? &learned : nullptr, (cudaStream_t)stream, &vc),
             "k_initial_temporal");
     return RG_OK;
 }
@@ -479,8 +537,10 @@ int rg_spatial_unbiased(rg_context *ctx, const rg_gbuffer *g, const rg_reservoir
     if ((rc = check_res(in, "in")) || (rc = check_res(out, "out"))) return rc;
     if (in == out) return fail(RG_ERR_INVALID_ARGUMENT, "in and out must differ");
     if (num_neighbors < 0 || num_neighbors > 16) return fail(RG_ERR_INVALID_ARGUMENT, "num_neighbors must be 0..16");
+    VisCache vc;
+    if ((rc = vcache_next(ctx, (size_t)u->screen_size[0] * u->screen_size[1], (cudaStream_t)stream, &vc))) return rc;
     RG_CUDA(launch_spatial_unbiased(ctx->scene, make_view(g), in, out, *u, num_neighbors, pass_index,
-                                    (cudaStream_t)stream),
+                                    (cudaStream_t)stream, &vc),
             "k_spatial_unbiased");
     return RG_OK;
 }

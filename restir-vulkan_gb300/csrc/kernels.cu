@@ -289,7 +289,30 @@ struct InitialParams {
     rg_reservoir *out;
     rg_restir_uniforms u;
     mlp::LearnedRis learned;  // learned.cand == nullptr: the plain alias-table proposal
+    VisCache vc{};            // own-segment answers written for the next ray pass
 };
+
+// The cached answer of segment a -> b in entry e (0 unshadowed, 1
+// shadowed), or -1 when the entry holds another segment or none.
+__device__ __forceinline__ int vcache_find(const VisCache &vc, size_t e, f3 a, f3 b) {
+    const float4 s = __ldg(vc.in + 2 * e), t = __ldg(vc.in + 2 * e + 1);
+    const uint32_t tag = __float_as_uint(s.w), tt = __float_as_uint(t.w);
+    if (tag == 0u || (tt >> 1) != tag) return -1;
+    if (__float_as_uint(s.x) != __float_as_uint(a.x) || __float_as_uint(s.y) != __float_as_uint(a.y) ||
+        __float_as_uint(s.z) != __float_as_uint(a.z) || __float_as_uint(t.x) != __float_as_uint(b.x) ||
+        __float_as_uint(t.y) != __float_as_uint(b.y) || __float_as_uint(t.z) != __float_as_uint(b.z))
+        return -1;
+    return (int)(tt & 1u);
+}
+// Entry e := segment a -> b with its answer (ans 0/1), or empty (ans < 0).
+__device__ __forceinline__ void vcache_put(const VisCache &vc, size_t e, f3 a, f3 b, int ans) {
+    if (ans < 0) {
+        vc.out[2 * e] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    vc.out[2 * e] = make_float4(a.x, a.y, a.z, __uint_as_float(vc.tag));
+    vc.out[2 * e + 1] = make_float4(b.x, b.y, b.z, __uint_as_float(2u * vc.tag + (uint32_t)ans));
+}
 
 // Initial RIS (restirOmni.glsl:86-145).  With the learned proposal, candidate
 // c of the pixel comes from its candidate slot: a cluster drawn from q(.|x)
@@ -473,7 +496,7 @@ __device__ __forceinline__ void initial_temporal_tile(const InitialParams &p, in
 #pragma unroll
         for (int q = 0; q < R; ++q) {
             const int owner = (j * 128 + tid) * R + q;
-            shadow[owner] = 0;
+            shadow[owner] = want ? 0 : 2;  // 2: no segment
             endp[owner] = lpos[q];
             const int slot = rgpool::append_slot(&s_count, want);
             if (want) rgpool::put_ray(pool, slot, wpos, owner);
@@ -494,10 +517,16 @@ __device__ __forceinline__ void initial_temporal_tile(const InitialParams &p, in
         ResV<R, MIS> r = load_resv<R, MIS>(p.out, i);
 #pragma unroll
         for (int q = 0; q < R; ++q) {
-            if (shadow[(j * 128 + tid) * R + q]) {
+            const int owner = (j * 128 + tid) * R + q;
+            if (shadow[owner] == 1) {
                 r.w[q] = 0.0f;
                 r.sum_w[q] = 0.0f;
                 if (MIS) r.sum_phat[q] = 0.0f;
+            }
+            if (p.vc.out) {
+                const float4 e = endp[owner];
+                vcache_put(p.vc, (size_t)q * p.vc.n + i, load_wpos(p.cur, i), mk(e.x, e.y, e.z),
+                           shadow[owner] == 2 ? -1 : (int)shadow[owner]);
             }
         }
         if ((p.u.flags & RG_FLAG_TEMPORAL_REUSE) && p.has_prev) {
@@ -559,6 +588,7 @@ struct SpatialParams {
     int iter;           // biased: push-constant iter; unbiased: pass index
     int num_neighbors;  // unbiased: NUM_NEIGHBORS
     float cos_thr;
+    VisCache vc{};      // unbiased: own-segment answers of the previous ray pass in, this pass's out
 };
 
 // One 32 x 4 pixel tile.
@@ -668,6 +698,7 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
 #pragma unroll
     for (int q = 0; q < R; ++q) lpos[q] = mk(0.f, 0.f, 0.f);
     uint32_t orig_m = 0;
+    f3 own_wpos = mk(0.f, 0.f, 0.f);
     float orig_sp[MIS ? R : 1];
 #pragma unroll
     for (int q = 0; q < (MIS ? R : 1); ++q) orig_sp[q] = 0.0f;
@@ -677,6 +708,7 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
         const float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
         const f3 cam = mk(p.u.camera_pos[0], p.u.camera_pos[1], p.u.camera_pos[2]);
         const f3 wo = view_dir(cam, t.wpos);
+        own_wpos = t.wpos;
         ResV<R, MIS> r = load_resv<R, MIS>(p.in, i);
         orig_m = r.m;
         if (MIS) {
@@ -725,11 +757,17 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
     // segments (one per neighbour whose hemisphere holds the sample) share the
     // sample's light as their end point: they follow consecutively, so the
     // lanes that take them trace similar paths.
+    // Segments whose answer the previous ray pass left in the cache (a pixel
+    // that kept its sample meets its own segment again; one that took a
+    // neighbour's sample meets that neighbour's own segment) are not traced,
+    // and a pixel whose own segment is cached as shadowed traces nothing.
     uint32_t wantm[R];  // bit k: neighbour k's segment
 #pragma unroll
     for (int q = 0; q < R; ++q) {
         endp[q * BT + tid] = make_float4(lpos[q].x, lpos[q].y, lpos[q].z, 0.0f);
         wantm[q] = 0u;
+        const int own_known =
+            valid && vis && p.vc.in ? vcache_find(p.vc, (size_t)q * p.vc.n + i, own_wpos, lpos[q]) : -1;
         for (int k = 0; k < K; ++k) {
             bool excluded = true;
             if (valid) {
@@ -737,12 +775,16 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
                 const f3 nw = load_wpos(p.g, ni);
                 const f3 nn = load_normal(p.g, ni);
                 excluded = dot(lpos[q] - nw, nn) < 0.0f;
-                if (!excluded && vis) wantm[q] |= 1u << k;
+                if (!excluded && vis && own_known != 1) {
+                    const int known = p.vc.in ? vcache_find(p.vc, (size_t)q * p.vc.n + ni, nw, lpos[q]) : -1;
+                    if (known < 0) wantm[q] |= 1u << k;
+                    else excluded = known == 1;  // a cached shadowed answer counts like an exclusion
+                }
             }
             flag[(q * slots + k) * BT + tid] = excluded ? 1 : 0;
         }
-        flag[(q * slots + K) * BT + tid] = 0;
-        const bool own = valid && vis;
+        flag[(q * slots + K) * BT + tid] = own_known == 1 ? 1 : 0;
+        const bool own = valid && vis && own_known < 0;
         const int slot = rgpool::append_range(&s_count, own ? 1 : 0);
         if (own) pool[slot] = (q * slots + K) * BT + tid;
     }
@@ -779,9 +821,14 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
     __syncthreads();
     if (valid) {
         ResV<R, MIS> r = load_resv<R, MIS>(p.out, i);
+        const f3 wp = p.vc.out ? load_wpos(p.g, i) : mk(0.f, 0.f, 0.f);
 #pragma unroll
         for (int q = 0; q < R; ++q) {
             const uint8_t *fq = flag + q * slots * BT;
+            if (p.vc.out) {
+                const float4 e = endp[q * BT + tid];
+                vcache_put(p.vc, (size_t)q * p.vc.n + i, wp, mk(e.x, e.y, e.z), vis ? (int)fq[K * BT + tid] : -1);
+            }
             if (MIS) {
                 float sp = orig_sp[q];
                 for (int k = 0; k < K; ++k)
@@ -1062,8 +1109,9 @@ GBufView make_view(const rg_gbuffer *g) {
 
 cudaError_t launch_initial_temporal(const DevScene &s, const GBufView &cur, const GBufView *prev,
                                     const rg_reservoir *prev_res, rg_reservoir *out, const rg_restir_uniforms &u,
-                                    const mlp::LearnedRis *learned, cudaStream_t st) {
+                                    const mlp::LearnedRis *learned, cudaStream_t st, const VisCache *vc) {
     InitialParams p;
+    if (vc) p.vc = *vc;
     p.learned = learned ? *learned : mlp::LearnedRis{};
     p.s = s;
     p.cur = cur;
@@ -1107,9 +1155,11 @@ cudaError_t launch_spatial_biased(const DevScene &s, const GBufView &g, const rg
 }
 
 cudaError_t launch_spatial_unbiased(const DevScene &s, const GBufView &g, const rg_reservoir *in, rg_reservoir *out,
-                                    const rg_restir_uniforms &u, int num_neighbors, int pass_index, cudaStream_t st) {
+                                    const rg_restir_uniforms &u, int num_neighbors, int pass_index, cudaStream_t st,
+                                    const VisCache *vc) {
     if (num_neighbors < 0 || num_neighbors > kMaxNeighbors) return cudaErrorInvalidValue;
     SpatialParams p;
+    if (vc) p.vc = *vc;
     p.s = s;
     p.g = g;
     p.in = in;

@@ -108,17 +108,33 @@ struct GBufView {
 // True when every plane of g is in the default layout.
 inline bool default_formats(const GBufView &g) { return g.nfmt == 0 && g.pfmt == 0 && g.dfmt == 0; }
 
+// Answers of the pixels' own visibility segments (a pixel's world position
+// to its sample's light position) kept between ray passes, keyed by the
+// segment's end points: an entry is two float4, (start.xyz, tag) and
+// (end.xyz, 2 * tag + shadowed), tag 0 = empty, one entry per (sample slot,
+// pixel).  A pass reads the entries the previous ray pass wrote (`in`) and
+// writes its own (`out`, another buffer); a segment whose end points equal
+// an entry's bit for bit has that entry's answer (the answer depends on the
+// scene and the two points only).  Null pointers: no cache.
+struct VisCache {
+    const float4 *in = nullptr;
+    float4 *out = nullptr;
+    uint32_t tag = 0;     // this launch's tag, 1 .. 2^31 - 1
+    uint32_t n = 0;       // entries per sample slot (the pass's pixel count)
+};
+
 GBufView make_view(const rg_gbuffer *g);
 
 // launchers (kernels.cu); return cudaGetLastError()
 namespace mlp { struct LearnedRis; struct ProposalDev; }
 cudaError_t launch_initial_temporal(const DevScene &s, const GBufView &cur, const GBufView *prev,
                                     const rg_reservoir *prev_res, rg_reservoir *out, const rg_restir_uniforms &u,
-                                    const mlp::LearnedRis *learned, cudaStream_t st);
+                                    const mlp::LearnedRis *learned, cudaStream_t st, const VisCache *vc = nullptr);
 cudaError_t launch_spatial_biased(const DevScene &s, const GBufView &g, const rg_reservoir *in, rg_reservoir *out,
                                   const rg_restir_uniforms &u, int iter, cudaStream_t st);
 cudaError_t launch_spatial_unbiased(const DevScene &s, const GBufView &g, const rg_reservoir *in, rg_reservoir *out,
-                                    const rg_restir_uniforms &u, int num_neighbors, int pass_index, cudaStream_t st);
+                                    const rg_restir_uniforms &u, int num_neighbors, int pass_index, cudaStream_t st,
+                                    const VisCache *vc = nullptr);
 cudaError_t launch_shade(const DevScene &s, const GBufView &g, const rg_reservoir *res, const rg_lighting_uniforms &u,
                          float4 *out, cudaStream_t st);
 cudaError_t launch_visibility_batch(const DevScene &s, const float4 *p1, const float4 *p2, uint8_t *out, int n,

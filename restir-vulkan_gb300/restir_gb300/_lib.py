@@ -184,6 +184,7 @@ _SIGNATURES = {
                                                     C.POINTER(RestirUniforms), C.c_int32, C.c_int32, C.c_void_p]),
     "rg_set_reservoir_format": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "rg_set_tree_layout": (C.c_int, [C.c_void_p, C.c_int32]),
+    "rg_set_visibility_cache": (C.c_int, [C.c_void_p, C.c_int32]),
     "rg_reservoir_bytes": (C.c_int, [C.c_void_p]),
     "rg_build_bvh_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
                                       C.POINTER(C.c_int32), C.c_void_p]),

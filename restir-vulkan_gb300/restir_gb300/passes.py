@@ -198,6 +198,10 @@ class Context:
             layout = "wide" if layout else "binary"
         check(lib().rg_set_tree_layout(self._h, self.TREE_LAYOUTS[layout]))
 
+    def set_visibility_cache(self, enable: bool):
+        """rg_set_visibility_cache: reuse own-segment answers between ray passes."""
+        check(lib().rg_set_visibility_cache(self._h, 1 if enable else 0))
+
     def reservoir_bytes(self) -> int:
         return check(lib().rg_reservoir_bytes(self._h))
 

@@ -148,8 +148,12 @@ def test_unbiased_pass_counts_rays(ctx, cfg2_small, cuda):
     ob.spatial_unbiased(s, g, r0, r1, u, 3, 0, stats=st)  # the reference's NUM_NEIGHBORS
     dg = DeviceGBuffer.from_host(g)
     out = reservoirs(n)
-    ctx.stats(reset=True)
-    ctx.spatial_unbiased(dg, reservoirs_from_numpy(r0), out, u, 3, 0)
+    ctx.set_visibility_cache(False)
+    try:
+        ctx.stats(reset=True)
+        ctx.spatial_unbiased(dg, reservoirs_from_numpy(r0), out, u, 3, 0)
+    finally:
+        ctx.set_visibility_cache(True)
     assert mismatch(reservoirs_to_numpy(out), r1) == 0
     # every segment whose answer reaches the output is traced; a neighbour's
     # segment whose pixel's own segment is shadowed may be skipped (the count
