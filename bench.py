@@ -353,10 +353,11 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
                     "triangle_tests_per_segment": trav["tris_per_ray"],
                     "segments_per_s": round(trav["rays"] / (mean_ms / 1000.0)),
                     "hbm": hbm,
-                    "note": ("achieved = tree and triangle bytes the walk fetches per launch (64 B per node visit, "
-                             "+48 B where a 4-wide node has a third child, 48 B per triangle test) over the "
-                             "launch time, against the measured L2 copy rate; the walk is bound by the latency of "
-                             "dependent node loads, so neither HBM (hbm.frac) nor L2 bandwidth is saturated; "
+                    "note": ("achieved = tree bytes the walk fetches per launch (node visits x node bytes and "
+                             "triangle tests x leaf bytes of the layout in use: 64 B quantized 4-wide node and "
+                             "64 B leaf record by default) over the launch time, against the measured L2 copy "
+                             "rate; most of those bytes are L1 hits and the walk is bound by instruction issue "
+                             "and load latency, so neither HBM (hbm.frac) nor L2 bandwidth is saturated; "
                              "traffic = DRAM bytes per launch from the ncu capture in profiles/, scaled per pixel")}
     else:
         roofline = {"kernel": dom, "bound": "hbm", "traffic": traffic, "mean_launch_ms": round(mean_ms, 4),
@@ -446,6 +447,17 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
         line["cpu_baseline"] = {"value": cb["value"], "unit": UNIT, "cores": cb["threads"], "kind": "port",
                                 "sample": cb["sample"], "measured_seconds": round(cb["measured_seconds"], 2),
                                 "full_frame_seconds_estimate": round(cb["frame_seconds_estimate"], 2)}
+        if args.cpu_crop <= 0 and s.unbiased:
+            # segments the reference traces for frame 1 (the oracle's count over the
+            # whole frame) against those this library traces for the same frame
+            traced = frame1_segments(ctx, s, dgs, res, tmp, stream)
+            ref_rays = int(cb["rays_in_sample"])
+            line["traversal"]["segments_frame1"] = {
+                "traced": traced, "reference": ref_rays, "ratio": round(traced / max(ref_rays, 1), 4),
+                "note": ("frames 0 then 1 as the CPU leg runs them; segments not traced are unobservable "
+                         "(a neighbour's segment of a pixel whose own segment is shadowed) or equal bit for bit "
+                         "to a segment the previous ray pass traced (visibility cache)")}
+            line["reference_equivalent_mrays_per_s"] = round(mrays * ref_rays / max(traced, 1), 1)
     ctx.close()
     return line
 
@@ -519,6 +531,29 @@ def launch_traversal(ctx, s, dgs, res, tmp, stream) -> dict:
     return {"rays": rays, "visits_per_ray": round(st.node_visits / rays, 2),
             "tris_per_ray": round(st.triangle_tests / rays, 2), "tree_bytes": tree_bytes,
             "wide_nodes": int(st.wide_nodes)}
+
+
+def frame1_segments(ctx, s, dgs, res, tmp, stream) -> int:
+    """Segments traced for frame 1 after frame 0 (the CPU leg's sequence),
+    through the same passes as the timed frames."""
+    import torch
+    count = 0
+    prev = None
+    for f in range(2):
+        u = s.uniforms(f)
+        torch.cuda.synchronize()
+        ctx.stats(reset=True)
+        cur = res[f % 2]
+        ctx.initial_temporal(dgs[f], dgs[f - 1] if f else None, prev, tmp, u, stream)
+        src = tmp
+        for p in range(s.spatial_passes):
+            dst = cur if src is tmp else tmp
+            ctx.spatial_unbiased(dgs[f], src, dst, u, s.neighbors, p, stream)
+            src = dst
+        torch.cuda.synchronize()
+        count = int(ctx.stats(reset=True).rays_traced)
+        prev = src
+    return count
 
 
 def tree_desc(st) -> str:

@@ -327,6 +327,7 @@ __device__ __forceinline__ ResV<R, MIS> ris(const DevScene &s, const Texel &t, f
     ResV<R, MIS> r = empty_resv<R, MIS>();
     if (zero_normal) return r;
     const f3 wo = view_dir(cam, t.wpos);
+    const PhatPx pp = phat_px(t.wpos, wo, t.normal, albedo_lum, t.roughness, t.metallic);
     const int count = s.n_alias;
     if (!lr.cand && s.n_point_lights != 0 && count_c > 0) {
         // The plain point-light proposal with a one-candidate lookahead.  A
@@ -359,8 +360,7 @@ __device__ __forceinline__ ResV<R, MIS> ris(const DevScene &s, const Texel &t, f
             const float4 pos_lum = keep ? own : ali;
             const float prob = keep ? cc.z : cc.w;
             const int32_t lidx = keep ? col : __float_as_int(cc.y);
-            const float ph = eval_phat_wo(t.wpos, xyz(pos_lum), wo, t.normal, xyz(nrm0), false, albedo_lum,
-                                          pos_lum.w, t.roughness, t.metallic);
+            const float ph = eval_phat_px(pp, xyz(pos_lum), xyz(nrm0), false, pos_lum.w);
             add_sample_u(r, pos_lum, nrm0, lidx, ph, prob, u);
             r2 = r2n;
             col = coln;
@@ -428,8 +428,7 @@ __device__ __forceinline__ ResV<R, MIS> ris(const DevScene &s, const Texel &t, f
             nrm = make_float4(nn.x, nn.y, nn.z, 1.0f);
             lidx = -1 - sel;
         }
-        const float ph = eval_phat_wo(t.wpos, xyz(pos_lum), wo, t.normal, xyz(nrm), nrm.w > 0.5f, albedo_lum,
-                                      pos_lum.w, t.roughness, t.metallic);
+        const float ph = eval_phat_px(pp, xyz(pos_lum), xyz(nrm), nrm.w > 0.5f, pos_lum.w);
         add_sample(r, pos_lum, nrm, lidx, ph, prob, rng);
     }
     if (flags & RG_FLAG_FINAL_RIS_WEIGHT) {
@@ -604,7 +603,7 @@ __device__ __forceinline__ void spatial_biased_tile(const SpatialParams &p, int 
     const float depth = load_depth(p.g, i);
     const float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
     const f3 cam = mk(p.u.camera_pos[0], p.u.camera_pos[1], p.u.camera_pos[2]);
-    const f3 wo = view_dir(cam, t.wpos);
+    const PhatPx pp = phat_px(t.wpos, view_dir(cam, t.wpos), t.normal, albedo_lum, t.roughness, t.metallic);
     ResV<R, MIS> r = load_resv<R, MIS>(p.in, i);
     const bool swap_fix = (p.u.flags & RG_FLAG_MIS_SWAP_FIX) != 0;
     Pcg rng = pcg_seed((uint64_t)(p.u.frame * 31u + (uint32_t)p.iter), (uint64_t)((uint32_t)y * 10007u + (uint32_t)x));
@@ -623,8 +622,7 @@ __device__ __forceinline__ void spatial_biased_tile(const SpatialParams &p, int 
         float ph[R];
 #pragma unroll
         for (int q = 0; q < R; ++q)
-            ph[q] = eval_phat_wo(t.wpos, xyz(rr.pos_lum[q]), wo, t.normal, xyz(rr.nrm[q]), rr.nrm[q].w > 0.5f,
-                                 albedo_lum, rr.pos_lum[q].w, t.roughness, t.metallic);
+            ph[q] = eval_phat_px(pp, xyz(rr.pos_lum[q]), xyz(rr.nrm[q]), rr.nrm[q].w > 0.5f, rr.pos_lum[q].w);
         combine_res(r, rr, ph, swap_fix, rng);
     }
     store_resv(p.out, i, r);
@@ -708,6 +706,7 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
         const float albedo_lum = luminance(t.albedo.x, t.albedo.y, t.albedo.z);
         const f3 cam = mk(p.u.camera_pos[0], p.u.camera_pos[1], p.u.camera_pos[2]);
         const f3 wo = view_dir(cam, t.wpos);
+        const PhatPx pp = phat_px(t.wpos, wo, t.normal, albedo_lum, t.roughness, t.metallic);
         own_wpos = t.wpos;
         ResV<R, MIS> r = load_resv<R, MIS>(p.in, i);
         orig_m = r.m;
@@ -736,9 +735,8 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
             r.m += rr.m;
 #pragma unroll
             for (int q = 0; q < R; ++q) {
-                const float ph = eval_phat_wo(t.wpos, xyz(rr.pos_lum[q]), wo, t.normal, xyz(rr.nrm[q]),
-                                              rr.nrm[q].w > 0.5f, albedo_lum, rr.pos_lum[q].w, t.roughness,
-                                              t.metallic);
+                const float ph = eval_phat_px(pp, xyz(rr.pos_lum[q]), xyz(rr.nrm[q]), rr.nrm[q].w > 0.5f,
+                                              rr.pos_lum[q].w);
                 const float weight = ph * rr.w[q] * (float)rr.m;
                 if (weight > 0.0f)
                     update_at(r, q, weight, rr.pos_lum[q], rr.nrm[q], rr.idx[q], ph, rr.w[q],

@@ -163,6 +163,57 @@ RG_HD float eval_phat_wo(f3 wpos, f3 lpos, f3 wo, f3 n, f3 ln, bool use_ln, floa
     if (use_ln) geometry *= fabsf(dot(wi, ln));
     return emission_lum * brdf_lum(cos_in, cos_out, cos_half, cos_in_half, albedo_lum, roughness, metallic) * geometry;
 }
+// eval_phat_wo with the terms that depend on the shading point only (the
+// view-side cosine, Fresnel and Smith term, alpha, the specular base)
+// computed once per pixel: the same operations on the same values, so the
+// same result.
+struct PhatPx {
+    f3 wpos, wo, n;
+    float lum, roughness, metallic;
+    float cos_out, f_out, a, g_out, spec0;
+};
+RG_HD PhatPx phat_px(f3 wpos, f3 wo, f3 n, float albedo_lum, float roughness, float metallic) {
+    PhatPx p;
+    p.wpos = wpos;
+    p.wo = wo;
+    p.n = n;
+    p.lum = albedo_lum;
+    p.roughness = roughness;
+    p.metallic = metallic;
+    p.cos_out = dot(n, wo);
+    p.f_out = schlick_fresnel(p.cos_out);
+    p.a = gmax(0.001f, roughness * roughness);
+    p.g_out = smith_g_ggx(p.cos_out, p.a);
+    p.spec0 = gmix(0.04f, albedo_lum, metallic);
+    return p;
+}
+RG_HD float eval_phat_px(const PhatPx &p, f3 lpos, f3 ln, bool use_ln, float emission_lum) {
+    f3 wi = lpos - p.wpos;
+    if (dot(wi, p.n) < 0.0f) return 0.0f;
+    const float sqr_dist = dot(wi, wi);
+    wi = divs(wi, sqrtf(sqr_dist));
+    const float cos_in = dot(p.n, wi);
+    const f3 h = normalize(wi + p.wo);
+    const float cos_half = dot(p.n, h);
+    const float cos_in_half = dot(wi, h);
+    float geometry = cos_in / sqr_dist;
+    if (use_ln) geometry *= fabsf(dot(wi, ln));
+    float b = 0.0f;  // brdf_lum
+    if (!(cos_in < 0.0f)) {
+        const float f_in = schlick_fresnel(cos_in);
+        const float fd90 = 0.5f + 2.0f * cos_in_half * cos_in_half * p.roughness;
+        const float fd = gmix(1.0f, fd90, f_in) * gmix(1.0f, fd90, p.f_out);
+        const float diffuse = p.lum * (fd * (1.0f - p.metallic) / kPi);
+        const float fr = schlick_fresnel(cos_in_half);
+        const float ds = gtr2(cos_half, p.a);
+        float gs = smith_g_ggx(cos_in, p.a);
+        gs *= p.g_out;
+        const float gd = gs * ds;
+        const float fs = gmix(p.spec0, 1.0f, fr);
+        b = diffuse + fs * gd;
+    }
+    return emission_lum * b * geometry;
+}
 RG_HD f3 eval_phat_full(f3 wpos, f3 lpos, f3 cam, f3 n, f3 ln, bool use_ln, f3 albedo, f3 emission, float roughness,
                         float metallic) {
     f3 wi = lpos - wpos;
