@@ -314,8 +314,9 @@ int rg_set_tree_layout(rg_context *ctx, int32_t layout);
  * the scene and the two points, and an upload clears the record.  The record
  * lives in the context (32 bytes per pixel and sample, two buffers), so
  * passes of one context must run in order: on one stream, or with the
- * caller synchronising between streams; turn the cache off otherwise.  The
- * batched-view and allocation-free entry points do not use it. */
+ * caller synchronising between streams; turn the cache off otherwise.  A
+ * batch created while the cache is on keeps a cache of its own
+ * (rg_batch_create); the allocation-free entry point does not use it. */
 int rg_set_visibility_cache(rg_context *ctx, int32_t enable);
 
 /* ---- scene upload (host pointers; copied to device, synchronous) ---- */
@@ -450,7 +451,9 @@ typedef struct rg_batch rg_batch;
  * proposal's weights as they are at each run (training between runs is
  * fine); once the proposal is re-created, rg_batch_run fails and a captured
  * graph of the batch must not be replayed.  Training stays a separate call
- * (rg_proposal_train on a view's G-buffer and reservoirs). */
+ * (rg_proposal_train on a view's G-buffer and reservoirs).  With the
+ * context's visibility cache on at creation, unbiased batches keep their own
+ * cache (64 bytes per pixel of all views) with the same results. */
 int rg_batch_create(rg_context *ctx, const rg_view *views, int32_t n_views, const rg_frame_params *params,
                     const rg_batch_tuning *tuning, rg_batch **out);
 /* One frame of every view on `stream`. */

@@ -66,6 +66,7 @@ struct rg_batch {
     unsigned char *initial[2] = {nullptr, nullptr};  // [n] parameter records per parity
     unsigned char *spatial_p[2] = {nullptr, nullptr};  // [spatial][n]
     unsigned char *shade[2] = {nullptr, nullptr};
+    float4 *vcache[2] = {nullptr, nullptr};  // visibility cache, 2 float4 per pixel of all views, per buffer
     uint32_t *start_frame = nullptr, *runs = nullptr;
     unsigned *counters = nullptr;  // 2 + spatial
     TileMap maps[3];               // RIS, spatial, shade (for the current tuning)
@@ -93,6 +94,10 @@ struct rg_batch {
             if (spatial_p[k]) cudaFree(spatial_p[k]);
             if (shade[k]) cudaFree(shade[k]);
             initial[k] = spatial_p[k] = shade[k] = nullptr;
+        }
+        for (int k = 0; k < 2; ++k) {
+            if (vcache[k]) cudaFree(vcache[k]);
+            vcache[k] = nullptr;
         }
         if (start_frame) cudaFree(start_frame);
         if (runs) cudaFree(runs);
@@ -286,6 +291,23 @@ int rg_batch_create(rg_context *ctx, const rg_view *views, int32_t n_views, cons
         }
         b->tuning = *tuning;
     }
+    // the visibility cache (rg_set_visibility_cache): the RIS pass writes
+    // buffer 1, unbiased pass k reads buffer (k + 1) % 2 and writes k % 2, so
+    // every pass reads what the pass before it wrote; each pass rewrites every
+    // pixel's entry, and the tag of a pass position pairs an entry's halves
+    const bool vcache = b->unbiased && rg_internal_vcache_on(ctx);
+    if (vcache) {
+        cudaError_t ev = cudaSuccess;
+        for (int k = 0; k < 2 && ev == cudaSuccess; ++k) {
+            ev = cudaMalloc(&b->vcache[k], (size_t)b->rows * 2 * sizeof(float4));
+            if (ev == cudaSuccess) ev = cudaMemset(b->vcache[k], 0, (size_t)b->rows * 2 * sizeof(float4));
+        }
+        if (ev != cudaSuccess) {
+            b->release();
+            delete b;
+            return bcuda(ev, "visibility cache");
+        }
+    }
     // parameter records: the same pointer choices as rg_render_frame
     const size_t ri = view_params_size(0), rs = view_params_size(1), rh = view_params_size(2);
     std::vector<unsigned char> hi(ri * n_views), hs(rs * n_views * (size_t)(b->spatial > 0 ? b->spatial : 1)),
@@ -304,14 +326,27 @@ int rg_batch_create(rg_context *ctx, const rg_view *views, int32_t n_views, cons
             if (b->unbiased && passes % 2 == 1) first = w.tmp;
             mlp::LearnedRis vlr = lr;
             if (learned) vlr.cand = b->cand + (size_t)first_row[(size_t)v] * mlp::kCand;
+            const size_t px = (size_t)u.screen_size[0] * u.screen_size[1];
+            auto vc_of = [&](int read_buf, int write_buf, uint32_t tag) {
+                VisCache c;
+                if (!vcache) return c;
+                const size_t off = 2 * (size_t)first_row[(size_t)v];
+                c.in = read_buf < 0 ? nullptr : b->vcache[read_buf] + off;
+                c.out = b->vcache[write_buf] + off;
+                c.tag = tag;
+                c.n = (uint32_t)px;
+                return c;
+            };
+            const VisCache vc_ris = vc_of(-1, 1, 1u);
             make_initial_params(hi.data() + ri * v, *s, cur, temporal ? &prev : nullptr, temporal ? prev_res : nullptr,
-                                first, u, learned ? &vlr : nullptr);
+                                first, u, learned ? &vlr : nullptr, &vc_ris);
             if (b->unbiased) {
                 rg_reservoir *src = first;
                 for (int k = 0; k < passes; ++k) {
                     rg_reservoir *dst = (src == w.tmp) ? cur_res : w.tmp;
+                    const VisCache vc_k = vc_of((k + 1) % 2, k % 2, 2u + (uint32_t)k);
                     make_spatial_params(hs.data() + rs * ((size_t)k * n_views + v), *s, cur, src, dst, u, true, k,
-                                        b->neighbors);
+                                        b->neighbors, &vc_k);
                     src = dst;
                 }
             } else {

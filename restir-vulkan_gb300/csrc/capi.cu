@@ -746,6 +746,8 @@ int rg_render_frame_host(rg_context *ctx, int32_t w, int32_t h, const uint8_t *a
 // per-thread error message and the uploaded scene of a context.
 int rg_internal_fail(int code, const char *msg) { return fail(code, "%s", msg); }
 
+bool rg_internal_vcache_on(rg_context *ctx) { return ctx->vc_on; }
+
 ProposalState **rg_internal_proposal(rg_context *ctx) {
     cudaSetDevice(ctx->device);
     return &ctx->proposal;

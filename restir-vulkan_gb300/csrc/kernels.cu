@@ -1219,8 +1219,9 @@ size_t view_params_size(int kind) {
 
 void make_initial_params(void *dst, const DevScene &s, const GBufView &cur, const GBufView *prev,
                          const rg_reservoir *prev_res, rg_reservoir *out, const rg_restir_uniforms &u,
-                         const mlp::LearnedRis *learned) {
+                         const mlp::LearnedRis *learned, const VisCache *vc) {
     InitialParams p;
+    if (vc) p.vc = *vc;
     p.learned = learned ? *learned : mlp::LearnedRis{};
     p.s = s;
     p.cur = cur;
@@ -1233,8 +1234,10 @@ void make_initial_params(void *dst, const DevScene &s, const GBufView &cur, cons
 }
 
 void make_spatial_params(void *dst, const DevScene &s, const GBufView &g, const rg_reservoir *in, rg_reservoir *out,
-                         const rg_restir_uniforms &u, bool unbiased, int iter_or_pass, int num_neighbors) {
+                         const rg_restir_uniforms &u, bool unbiased, int iter_or_pass, int num_neighbors,
+                         const VisCache *vc) {
     SpatialParams p;
+    if (vc) p.vc = *vc;
     p.s = s;
     p.g = g;
     p.in = in;

@@ -161,9 +161,10 @@ struct ViewTiles {
 size_t view_params_size(int kind);
 void make_initial_params(void *dst, const DevScene &s, const GBufView &cur, const GBufView *prev,
                          const rg_reservoir *prev_res, rg_reservoir *out, const rg_restir_uniforms &u,
-                         const mlp::LearnedRis *learned);
+                         const mlp::LearnedRis *learned, const VisCache *vc = nullptr);
 void make_spatial_params(void *dst, const DevScene &s, const GBufView &g, const rg_reservoir *in, rg_reservoir *out,
-                         const rg_restir_uniforms &u, bool unbiased, int iter_or_pass, int num_neighbors);
+                         const rg_restir_uniforms &u, bool unbiased, int iter_or_pass, int num_neighbors,
+                         const VisCache *vc = nullptr);
 void make_shade_params(void *dst, const DevScene &s, const GBufView &g, const rg_reservoir *res,
                        const rg_lighting_uniforms &u, float4 *out);
 // tile of pass `kind` for tuning variant `variant` (RIS: pixels per thread 1/2/4;
@@ -210,6 +211,8 @@ int gpu_build_bvh(const float *xyz, int n, rg_aabb_tree_node *nodes, rg_triangle
 // proposal.cu: the learned proposal attached to a context.
 struct ProposalState;
 ProposalState **rg_internal_proposal(rg_context *ctx);
+// Whether the context's visibility cache is on (rg_set_visibility_cache).
+bool rg_internal_vcache_on(rg_context *ctx);
 void proposal_release(ProposalState *ps);
 // Learned RIS inputs for a frame of w x h with `count` candidates, or an
 // RG_ERR_* code when the context's candidates do not match that frame.
