@@ -1045,9 +1045,13 @@ def reference_arm(args, rank: int, world: int) -> dict | None:
     finally:
         scenes.set_preprocessing()
     gb = [ob.trace_gbuffer(s, 0), ob.trace_gbuffer(s, 1)]
+    # a whole 1080p frame takes the oracle about 6 s on 16 cores: beyond 16
+    # steps each step times a centred 512x512 crop (per-pixel cost of each
+    # pass scaled to the frame), so the arm ends within a few minutes
+    crop = args.cpu_crop if args.cpu_crop > 0 else (0 if args.steps + args.warmup <= 16 else 512)
     vals = []
     for k in range(args.warmup + args.steps):
-        r = cpu_sample(s, gb, args.cpu_crop)
+        r = cpu_sample(s, gb, crop)
         if k >= args.warmup:
             vals.append(r)
     value = statistics.median(v["value"] for v in vals)
