@@ -108,3 +108,11 @@ def test_upload_clears_the_cache(ctx, cuda, seq_scene):
     # the moved scene shadows nothing: every reservoir with a positive p-hat keeps a positive w
     ok = results[1]["p_hat"] > 0
     assert ok.any() and np.all(results[1]["w"][ok] >= 0)
+
+
+def test_setters_reject_bad_values(ctx, restir_lib):
+    L = restir_lib
+    assert L.rg_set_visibility_cache(ctx._h, 2) == -1 and b"enable" in L.rg_last_error()
+    assert L.rg_set_tree_layout(ctx._h, 3) == -1 and b"tree layout" in L.rg_last_error()
+    assert L.rg_set_visibility_cache(None, 1) == -1
+    assert L.rg_set_tree_layout(ctx._h, 2) == 0 and L.rg_set_visibility_cache(ctx._h, 1) == 0
