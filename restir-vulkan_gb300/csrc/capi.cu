@@ -355,7 +355,7 @@ int rg_upload_scene(rg_context *ctx, const rg_scene_desc *sc) {
     if (ctx->tree_layout == RG_TREE_QUANT4 && sc->n_nodes > 0 && !box_nan)
         n_q = host_pack_quant(sc->nodes, sc->n_nodes, t12.data(), q16, ql16, &q_depth);
     if (n_q > 0 && 3 * q_depth + 1 > RG_MAX_TREE_DEPTH + 1) n_q = -1;
-    if (n_q > (1 << 27)) n_q = -1;  // parked leaves are held as node << 4
+    if (n_q > (1 << 27) || sc->n_triangles >= (1 << 27)) n_q = -1;  // node << 4, lane << 27 | leaf record
     e = dev_alloc(&ctx->nodes, (size_t)sc->n_nodes);
     if (e == cudaSuccess && sc->n_nodes) e = cudaMemcpy(ctx->nodes, n16.data(), n16.size() * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && n_wide > 0) {

@@ -641,6 +641,17 @@ __device__ __forceinline__ bool qleaf_hit(const QLeaf *lp, f3 o, f3 d, f3 inv) {
 #define RG_QWALK_STEPS 16
 #endif
 
+// RG_LEAF_COMPACT: the leaf phase lists the leaves every holding lane has
+// parked and tests them with all lanes of the warp (1 KB of shared memory per
+// warp), instead of each lane looping over its own.
+#ifndef RG_LEAF_COMPACT
+#define RG_LEAF_COMPACT 1
+#endif
+#ifndef RG_UNBIASED_BT
+#define RG_UNBIASED_BT 128
+#endif
+constexpr int kLeafQueueWarps = (RG_UNBIASED_BT > 128 ? RG_UNBIASED_BT : 128) / 32;  // the largest pool block
+
 // The parked leaves of one node ((node << 4) | mask of its leaf slots): the
 // exact box gate and the triangle test of each until one hits.
 __device__ __forceinline__ bool qparked_hit(const DevScene &s, unsigned e, f3 o, f3 d, f3 inv, TraceStats &ts) {
@@ -667,6 +678,9 @@ template <typename Fetch, typename Endpoint, typename Emit>
 __device__ void trace_quant_loop(const DevScene &s, Fetch fetch, int n, int *next, TraceStats &ts, Endpoint endpoint,
                                  Emit emit) {
     constexpr unsigned kFull = 0xffffffffu;
+#if RG_LEAF_COMPACT
+    __shared__ uint32_t s_leafq[kLeafQueueWarps][32 * 8];  // per warp: up to 8 parked leaves per lane
+#endif
     int my_stack[RG_MAX_TREE_DEPTH + 1];
     int cur = -1;          // pool index of this lane's segment, -1: none
     bool retired = false;  // the pool has no segment left for this lane
@@ -709,6 +723,63 @@ __device__ void trace_quant_loop(const DevScene &s, Fetch fetch, int n, int *nex
         const unsigned m_block = __ballot_sync(kFull, blocked);
         const unsigned m_walk = __ballot_sync(kFull, cur >= 0 && !blocked);
         if (m_block != 0u && (__popc(m_block) >= RG_LEAF_MIN || m_walk == 0u)) {
+#if RG_LEAF_COMPACT
+            // the holders' leaves go to the warp's queue ((lane << 27) |
+            // record), and every lane tests queued leaves, a chunk of 32 at a
+            // time, with the owning lane's ray taken by shuffles; a ray's
+            // remaining leaves are skipped once one of its leaves hits
+            const int lane = (threadIdx.x + threadIdx.y * blockDim.x) & 31;
+            uint32_t *q = s_leafq[(threadIdx.x + threadIdx.y * blockDim.x) >> 5];
+            const bool holder = cur >= 0 && park0 != 0u;
+            const int cnt = holder ? __popc(park0 & 15u) + __popc(park1 & 15u) : 0;
+            int incl = cnt;
+#pragma unroll
+            for (int sh = 1; sh < 32; sh <<= 1) {
+                const int t = __shfl_up_sync(kFull, incl, sh);
+                if (lane >= sh) incl += t;
+            }
+            const int total = __shfl_sync(kFull, incl, 31);
+            if (cnt != 0) {
+                int at = incl - cnt;
+#pragma unroll
+                for (int slot = 0; slot < 2; ++slot) {
+                    const unsigned e = slot == 0 ? park0 : park1;
+                    if (e == 0u) continue;
+                    const int4 ch = __ldg(&s.qnodes[e >> 4].d);
+                    for (unsigned m = e & 15u; m != 0u; m &= m - 1u) {
+                        const int k = __ffs(m) - 1;
+                        const int link = k == 0 ? ch.x : k == 1 ? ch.y : k == 2 ? ch.z : ch.w;
+                        q[at++] = ((unsigned)lane << 27) | (unsigned)(~link);
+                    }
+                }
+            }
+            __syncwarp();
+            unsigned hits = 0u;  // bit l: lane l's segment is shadowed
+            for (int base = 0; base < total; base += 32) {
+                const int j = base + lane;
+                const unsigned e = j < total ? q[j] : 0u;
+                const int src = (int)(e >> 27);
+                const f3 so = mk(__shfl_sync(kFull, o.x, src), __shfl_sync(kFull, o.y, src), __shfl_sync(kFull, o.z, src));
+                const f3 sd = mk(__shfl_sync(kFull, d.x, src), __shfl_sync(kFull, d.y, src), __shfl_sync(kFull, d.z, src));
+                const f3 si =
+                    mk(__shfl_sync(kFull, inv.x, src), __shfl_sync(kFull, inv.y, src), __shfl_sync(kFull, inv.z, src));
+                bool h = false;
+                if (j < total && ((hits >> src) & 1u) == 0u) {
+                    h = qleaf_hit(s.qleaves + (e & 0x7ffffffu), so, sd, si);
+                    ++ts.tri_tests;
+                }
+                hits |= __reduce_or_sync(kFull, h ? 1u << src : 0u);
+            }
+            __syncwarp();
+            if (holder) {
+                const bool hit = ((hits >> lane) & 1u) != 0u;
+                park0 = park1 = 0u;
+                if (hit || walked) {
+                    emit(owner, hit);
+                    cur = -1;
+                }
+            }
+#else
             if (cur >= 0 && park0 != 0u) {
                 bool hit = qparked_hit(s, park0, o, d, inv, ts);
                 if (!hit && park1 != 0u) hit = qparked_hit(s, park1, o, d, inv, ts);
@@ -718,6 +789,7 @@ __device__ void trace_quant_loop(const DevScene &s, Fetch fetch, int n, int *nex
                     cur = -1;
                 }
             }
+#endif
             continue;
         }
         // 3. up to RG_QWALK_STEPS nodes per walking lane
