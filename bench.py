@@ -418,15 +418,18 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         e_samples = 0
+        w0 = time.perf_counter()
         for k in range(args.steps):
             f = 1 + ((args.warmup + k) % (s.frames - 1))
             ctx.render_frame_host(host_frames[f], s.frame_params(f), out, stream)
             e_samples += s.samples_per_frame(f)
         e1.record(stream)
         torch.cuda.synchronize()
+        wall_ms = (time.perf_counter() - w0) * 1000.0
         e_ms = e0.elapsed_time(e1)
         line["e2e"] = {"value": e_samples / (e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": n * (4 + 8 + 4 + 16 + 4),
                        "d2h_bytes_per_step": n * 16, "ms_per_step": e_ms / args.steps,
+                       "wall_ms_per_step": round(wall_ms / args.steps, 3),
                        "api": "rg_render_frame_host (pinned host planes)"}
 
     # the learned proposal and the batched views on this GPU (rank 0)
