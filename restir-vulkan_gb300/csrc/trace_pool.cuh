@@ -641,6 +641,7 @@ __device__ __forceinline__ bool qleaf_hit(const QLeaf *lp, f3 o, f3 d, f3 inv) {
 #define RG_QWALK_STEPS 16
 #endif
 
+
 // RG_LEAF_COMPACT: the leaf phase lists the leaves every holding lane has
 // parked and tests them with all lanes of the warp (1 KB of shared memory per
 // warp), instead of each lane looping over its own.
@@ -792,18 +793,23 @@ __device__ void trace_quant_loop(const DevScene &s, Fetch fetch, int n, int *nex
 #endif
             continue;
         }
-        // 3. up to RG_QWALK_STEPS nodes per walking lane
+        // 3. up to RG_QWALK_STEPS nodes per walking lane.  The copy is built on
+        //    the host from a validated tree (a tree, stack bound checked at
+        //    upload), so a walk visits each node at most once; the visit count
+        //    is checked here, once per pass through this loop rather than per
+        //    visit (at most RG_QWALK_STEPS visits past the limit)
+        if (cur >= 0 && !walked && visits > s.n_qnodes) {
+            ts.err = true;
+            emit(owner, false);
+            cur = -1;
+            park0 = park1 = 0u;
+        }
 #pragma unroll 1
         for (int step = 0; step < RG_QWALK_STEPS && cur >= 0 && !walked &&
                            (RG_LEAF_SLOTS == 1 ? park0 : park1) == 0u;
              ++step) {
             ++ts.visits;
-            if (++visits > s.n_qnodes) {
-                ts.err = true;
-                emit(owner, false);
-                cur = -1;
-                continue;
-            }
+            ++visits;
             const QNode *np = s.qnodes + node;
             const float4 base = __ldg(&np->base);
             const uint4 qa = __ldg(&np->qxy), qb = __ldg(&np->qz);
