@@ -475,8 +475,8 @@ int32_t host_pack_wide(const rg_aabb_tree_node *src, int32_t n, std::vector<floa
 // Node (16 words): bases xyz (float), biased exponents (bytes 0-2 of word 3)
 // and the slot masks (byte 3: bit k child k is a leaf, bit 4+k an inner
 // node), then per axis a word of lower codes and a word of upper codes (byte
-// k = child k; x, y in words 4-7, z in words 8-9; 10-11 unused), then 4 links
-// (node index, ~leaf record index, or kNoChild).  Leaf record (16 floats):
+// k = child k; x, y in words 4-7, z in words 8-9), s of x and y as floats
+// (words 10-11), then 4 links (node index, ~leaf record index, or kNoChild).  Leaf record (16 floats):
 // lo.xyz hi.xyz, p1.xyz e1.xyz e2.xyz, 0.
 namespace {
 inline float pow2f(int eb) {
@@ -534,6 +534,8 @@ struct QuantBuilder {
         uint32_t leafbits = 0, innerbits = 0;
         for (int k = 0; k < n; ++k) (e[k].ref < 0 ? leafbits : innerbits) |= 1u << k;
         w[3] = (uint32_t)eb[0] | ((uint32_t)eb[1] << 8) | ((uint32_t)eb[2] << 16) | ((leafbits | innerbits << 4) << 24);
+        w[10] = (uint32_t)eb[0] << 23;  // s of x and y as floats (the walk reads them directly)
+        w[11] = (uint32_t)eb[1] << 23;
         for (int k = 0; k < 4 && ok; ++k) {
             const WEntry &c = e[k < n ? k : n - 1];  // an empty slot repeats the last child (ignored)
             for (int a = 0; a < 3; ++a) {

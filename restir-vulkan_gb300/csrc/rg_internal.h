@@ -53,7 +53,7 @@ constexpr int32_t kWideNoChild = INT32_MIN;
 struct QNode {
     float4 base; // c.xyz, exponent bytes (x, y, z) and slot masks (leaf bits 0-3, inner bits 4-7)
     uint4 qxy;   // lo x, hi x, lo y, hi y (byte k: child k)
-    uint4 qz;    // lo z, hi z, 0, 0
+    uint4 qz;    // lo z, hi z, s of x, s of y (float bits)
     int4 d;      // links of children 0..3
 };
 // QLeaf 64 B: a leaf of the quantized copy, the triangle's exact box from

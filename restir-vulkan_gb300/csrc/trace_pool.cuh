@@ -696,6 +696,8 @@ __device__ void trace_quant_loop(const DevScene &s, Fetch fetch, int n, int *nex
         const unsigned m_busy = __ballot_sync(kFull, cur >= 0);
         if (m_idle != 0u && (__popc(m_idle) >= RG_FETCH_MIN || m_busy == 0u)) {
             if (idle) {
+                ts.visits += (unsigned)visits;  // the finished segment's node visits
+                visits = 0;
                 const int k = atomicAdd(next, 1);
                 f3 p1;
                 if (k >= n) {
@@ -808,14 +810,13 @@ __device__ void trace_quant_loop(const DevScene &s, Fetch fetch, int n, int *nex
         for (int step = 0; step < RG_QWALK_STEPS && cur >= 0 && !walked &&
                            (RG_LEAF_SLOTS == 1 ? park0 : park1) == 0u;
              ++step) {
-            ++ts.visits;
             ++visits;
             const QNode *np = s.qnodes + node;
             const float4 base = __ldg(&np->base);
             const uint4 qa = __ldg(&np->qxy), qb = __ldg(&np->qz);
             const int4 ch = __ldg(&np->d);
             const unsigned eb = __float_as_uint(base.w);
-            const float ex = __uint_as_float((eb & 0xffu) << 23), ey = __uint_as_float(((eb >> 8) & 0xffu) << 23),
+            const float ex = __uint_as_float(qb.z), ey = __uint_as_float(qb.w),
                         ez = __uint_as_float(((eb >> 16) & 0xffu) << 23);
             const float2 sx = make_float2(ex, ex), sy = make_float2(ey, ey), sz = make_float2(ez, ez);
             const QAxes w = qaxes(inv, qa, qb);

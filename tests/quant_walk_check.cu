@@ -90,12 +90,18 @@ void quant_set(const Scene &s, f3 o, f3 d, f3 inv, std::set<int> &gated, bool &a
         const unsigned meta = w[3] >> 24;
         int32_t links[4];
         memcpy(links, &w[12], sizeof(links));
+        // the walk reads the x and y scales as floats from words 10 and 11
+        const float scale[3] = {f_of(w[10]), f_of(w[11]), f_of((uint32_t)eb[2] << 23)};
+        if (w[10] != ((uint32_t)eb[0] << 23) || w[11] != ((uint32_t)eb[1] << 23)) {
+            printf("scale words differ from the exponent bytes\n");
+            exit(4);
+        }
         for (int k = 0; k < 4; ++k) {
             const bool leaf = ((meta >> k) & 1u) != 0, inner = ((meta >> (4 + k)) & 1u) != 0;
             if (!leaf && !inner) continue;
             float tn[3], tf[3];
             for (int a = 0; a < 3; ++a) {
-                const float sc = f_of((uint32_t)eb[a] << 23);
+                const float sc = scale[a];
                 const unsigned ql = (w[4 + 2 * a] >> (8 * k)) & 255u, qh = (w[5 + 2 * a] >> (8 * k)) & 255u;
                 const float lo = fmaf(f_of(0x4B000000u | ql), sc, base[a]);
                 const float hi = fmaf(f_of(0x4B000000u | qh), sc, base[a]);
