@@ -13,10 +13,20 @@ Reported (one JSON line on rank 0):
             + spatial neighbour merges), device-timed with CUDA events;
   e2e       the same metric through rg_render_frame_host: host G-buffer in,
             image out, copies inside the timed region;
-  roofline  the dominant kernel's algorithmic bytes per launch over its mean
-            event-timed duration, against the measured HBM copy bandwidth;
-  cpu_baseline  the CPU oracle on a crop of the same frame (all host threads),
-            scaled per pixel.
+  roofline  the dominant kernel (the unbiased pass, bound by its shadow-ray
+            walk): the tree bytes its walk fetches per launch over its mean
+            event-timed duration against a measured L2 copy rate, with the
+            HBM view (algorithmic bytes against the measured HBM copy rate)
+            in roofline.hbm;
+  mrays_per_s / reference_equivalent_mrays_per_s  segments traced per
+            second, and that rate scaled by the reference's segment count
+            for frame 1 over this library's (segments whose answer cannot
+            change a result, or that repeat the previous pass's, are not
+            traced);
+  hbm_passes  shading and biased spatial reuse timed alone;
+  rmse_vs_fp64, rmse_vs_fp64_config2  image error of the benched sequence
+            and of the reference's default one against the FP64 judge;
+  cpu_baseline  the CPU oracle over the whole frame (all host threads).
   learned_proposal  config 4's workload: inference, learned vs plain RIS, one
             Adam step, and the tensor-core rate of the inference;
   batched_views     config 5's 64 views through one persistent launch per pass
