@@ -139,6 +139,28 @@ __device__ __forceinline__ ResV<R, MIS> load_resv(const rg_reservoir *base, size
     r.m = __float_as_uint(__ldg(p + R * L::kSample4).x);
     return r;
 }
+// load_resv with coherent loads, for a reservoir this thread wrote earlier in
+// the same kernel (the read-only path may only read data that no thread of
+// the kernel writes).
+template <int R, bool MIS>
+__device__ __forceinline__ ResV<R, MIS> load_resv_own(const rg_reservoir *base, size_t i) {
+    using L = ResLayout<R, MIS>;
+    const float4 *p = reinterpret_cast<const float4 *>(base) + i * L::kWords;
+    ResV<R, MIS> r;
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        r.pos_lum[j] = p[j * L::kSample4];
+        r.nrm[j] = p[j * L::kSample4 + 1];
+        const float4 c = p[j * L::kSample4 + 2];
+        r.idx[j] = __float_as_int(c.x);
+        r.p_hat[j] = c.y;
+        r.sum_w[j] = c.z;
+        r.w[j] = c.w;
+        if (MIS) r.sum_phat[j] = p[j * L::kSample4 + 3].x;
+    }
+    r.m = __float_as_uint(p[R * L::kSample4].x);
+    return r;
+}
 template <int R, bool MIS>
 __device__ __forceinline__ void store_resv(rg_reservoir *base, size_t i, const ResV<R, MIS> &r) {
     using L = ResLayout<R, MIS>;
@@ -513,7 +535,7 @@ __device__ __forceinline__ void initial_temporal_tile(const InitialParams &p, in
         const int y = y0 + 4 * j;
         if (x >= W || y >= H) continue;
         const size_t i = (size_t)y * (size_t)W + (size_t)x;
-        ResV<R, MIS> r = load_resv<R, MIS>(p.out, i);
+        ResV<R, MIS> r = load_resv_own<R, MIS>(p.out, i);
 #pragma unroll
         for (int q = 0; q < R; ++q) {
             const int owner = (j * 128 + tid) * R + q;
@@ -818,7 +840,11 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
         [&](int owner, bool hit) { if (hit) flag[owner] = 1; });
     __syncthreads();
     if (valid) {
-        ResV<R, MIS> r = load_resv<R, MIS>(p.out, i);
+        // the merged reservoir went to `out` before the trace; only each
+        // sample's (index, p-hat, sumWeights, W) word and, with MIS, its
+        // sumPHat word change (coherent loads: this thread wrote them)
+        using L = ResLayout<R, MIS>;
+        float4 *rw = reinterpret_cast<float4 *>(p.out) + i * L::kWords;
         const f3 wp = p.vc.out ? load_wpos(p.g, i) : mk(0.f, 0.f, 0.f);
 #pragma unroll
         for (int q = 0; q < R; ++q) {
@@ -827,17 +853,20 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
                 const float4 e = endp[q * BT + tid];
                 vcache_put(p.vc, (size_t)q * p.vc.n + i, wp, mk(e.x, e.y, e.z), vis ? (int)fq[K * BT + tid] : -1);
             }
+            const float4 c = rw[q * L::kSample4 + 2];  // index, p-hat, sumWeights, W
+            const float p_hat = c.y;
+            float sum_w = c.z, w = c.w;
             if (MIS) {
                 float sp = orig_sp[q];
                 for (int k = 0; k < K; ++k)
                     if (!fq[k * BT + tid]) sp += nsp[(q * kp + k) * BT + tid];
                 if (vis && fq[K * BT + tid]) sp = 0.0f;
                 if (sp > 0.0f) {
-                    r.w[q] = r.sum_w[q] * r.p_hat[q] / (sp * r.p_hat[q]);
+                    w = sum_w * p_hat / (sp * p_hat);
                 } else {
-                    r.w[q] = 0.0f;
-                    r.sum_w[q] = 0.0f;
-                    r.sum_phat[q] = 0.0f;
+                    w = 0.0f;
+                    sum_w = 0.0f;
+                    rw[q * L::kSample4 + 3] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // sumPHat
                 }
             } else {
                 uint32_t ns = orig_m;
@@ -845,14 +874,14 @@ __device__ __forceinline__ void spatial_unbiased_tile(const SpatialParams &p, in
                     if (!fq[k * BT + tid]) ns += nm[k * BT + tid];
                 if (vis && fq[K * BT + tid]) ns = 0;
                 if (ns > 0) {
-                    r.w[q] = r.sum_w[q] / ((float)ns * r.p_hat[q]);
+                    w = sum_w / ((float)ns * p_hat);
                 } else {
-                    r.w[q] = 0.0f;
-                    r.sum_w[q] = 0.0f;
+                    w = 0.0f;
+                    sum_w = 0.0f;
                 }
             }
+            rw[q * L::kSample4 + 2] = make_float4(c.x, p_hat, sum_w, w);
         }
-        store_resv(p.out, i, r);
     }
     count_block_rays(s, tid == 0 ? s_count : 0, ts);
 }
